@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 block-FIM Eikonal solver (one JSON line on rank 0).
+
+Workload (the plain-FIM-at-scale configuration): a 65^3 vertex grid on the unit
+cube, every cube Kuhn-split into 6 tets (274,625 vertices, 1,572,864 tets),
+interior vertices jittered by U(-0.2h, 0.2h)^3 (seed 1), per-tet speed
+log-uniform in [0.5, 2] (seed 2) given to the solver as the scalar metric 1/v^2,
+one seed at the centre vertex, 64 vertices per block.  A step is one complete
+solve (seed -> every block converged).
+
+  value  vertex-updates/s of the device-resident solve (mesh, partition and metric
+         terms resident in HBM), timed with CUDA events on the solver's stream;
+         L2 is flushed (512 MB write) before every timed solve, outside the events
+  e2e    the same metric through the C ABI with host buffers: seeds copied in,
+         solve, travel times copied out, wall clock per step
+  roofline  the block-sweep kernel: algorithmic bytes of its launches / their
+         device-timer spans, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU restatement of the reference scheme (oracle/) with all
+         host threads on a bounded sample of the same solve
+
+--impl reference times that CPU restatement alone (the reference has no CPU
+driver of its own).  With N > 1 ranks every rank runs its own
+replica (no collective in the solve path); value sums all ranks' updates over
+the slowest rank's time.
+"""
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "vertex-updates/s & solves/s, batched vs plain FIM; p50/p99 solve latency"
+WORKLOAD = ("plain FIM 3D at scale: 65^3 jittered Kuhn cube (274,625 verts, 1,572,864 tets), "
+            "log-uniform per-tet speed [0.5, 2] as metric 1/v^2, seed at the centre vertex, 64 verts/block")
+N_GRID = 65
+MAX_ITERS = 100  # the reference default (src/Eikonal.cu:19); the workload converges in 81
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cpu-sample-iters", type=int, default=0, help="0 = choose automatically")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_workload():
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    xyz, tets = mg.kuhn_cube(N_GRID, 0.2, seed=1)
+    speed = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=2)
+    metric = (1.0 / (speed.astype(np.float64) ** 2)).astype(np.float32)
+    seed = mg.center_vertex(N_GRID)
+    return xyz, tets, metric, seed
+
+
+def algorithmic_bytes(st):
+    """Bytes the block-sweep kernel must move: per visited slot 6 float metric terms +
+    4 u16 corner ids (32 B), owned + halo travel times read (4 B each), owned times
+    written (4 B), one block flag (4 B)."""
+    return (32 * st["fim_slots"] + 4 * (st["fim_owned"] + st["fim_halo"]) + 4 * st["fim_owned"]
+            + 4 * st["fim_visits"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{gpu_index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(xyz, tets, metric, seed, labels, nb, sample_iters):
+    """The oracle on the first `sample_iters` outer iterations of the same solve."""
+    from oracle import oracle as O  # CPU baseline only
+    M = O.metrics_from_speeds(tets.shape[0], metric)
+    threads = O.num_threads()
+    t0 = time.perf_counter()
+    r = O.solve3d(xyz, tets, M, labels, nb, [seed], max_iters=sample_iters, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": r["vertex_updates"] / dt, "unit": "vertex-updates/s", "cores": threads, "kind": "port",
+            "sample": f"first {r['iterations']} outer iterations of the same solve "
+                      f"({r['vertex_updates']} vertex updates in {dt:.1f} s)",
+            "seconds": dt, "iterations": r["iterations"]}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    E = importlib.import_module("sci-solver_eikonal_gb300")
+    xyz, tets, metric, seed = build_workload()
+    # the same partition as the product's arm (recursive coordinate bisection)
+    labels, nb = partition_host(E, xyz, tets, metric)
+    from oracle import oracle as O
+    sample_iters = args.cpu_sample_iters or MAX_ITERS
+    vals = []
+    for i in range(args.warmup + args.steps):
+        res = cpu_sample(xyz, tets, metric, seed, labels, nb, sample_iters)
+        if i >= args.warmup:
+            vals.append(res)
+    v = statistics.median(r["value"] for r in vals)
+    secs = [r["seconds"] for r in vals]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "vertex-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "partition": f"recursive coordinate bisection, {nb} blocks",
+                       "step": vals[0]["sample"]},
+            "cpu_baseline": {"value": v, "unit": "vertex-updates/s", "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "vertex-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def partition_host(E, xyz, tets, metric):
+    """Labels from the product's partitioner (host-only call, no GPU work)."""
+    e = E.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.initSpeedMtxMultipliers(metric)
+    e.maxVertsPerBlock_ = 64
+    e.prepare()
+    return e.getPartition()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    E = importlib.import_module("sci-solver_eikonal_gb300")
+    xyz, tets, metric, seed = build_workload()
+    e = E.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.initSpeedMtxMultipliers(metric)
+    e.setSeeds([seed])
+    e.maxVertsPerBlock_ = 64
+    e.maxIterations_ = MAX_ITERS
+    e.keepHistory_ = 0
+    t0 = time.perf_counter()
+    e.solveEikonal()  # partition, layout, upload, graph build, first solve
+    setup_s = time.perf_counter() - t0
+    st0 = e.stats()
+    stream = torch.cuda.ExternalStream(e.stream())
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        e.solveEikonal()
+    sampler = ClockSampler(local)
+    sampler.start()
+    times, upd, fim_ms, fim_bytes, iters, launches = [], 0, 0.0, 0, [], 0
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e.solveEikonal()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+        st = e.stats()
+        upd += st["vertex_updates"]
+        fim_ms += st["fim_kernel_ms"]
+        fim_bytes += algorithmic_bytes(st)
+        iters.append(st["iterations"])
+        launches += 1 + 4 * st["iterations"]
+    barrier()
+    clocks = sampler.stop()
+    total_ms = sum(times)
+    if world > 1:
+        tt = torch.tensor([total_ms, float(upd)], dtype=torch.float64, device="cuda")
+        mx = tt.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm = tt.clone()
+        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+        total_ms, upd_all = float(mx[0]), float(sm[1])
+    else:
+        upd_all = float(upd)
+    value = upd_all / (total_ms * 1e-3)
+
+    # end to end through the C ABI with host buffers
+    nv = xyz.shape[0]
+    out = np.empty(nv, dtype=np.float32)
+    seeds = np.array([seed], dtype=np.int32)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e.setSeeds(seeds)
+        e.solveEikonal()
+        out[:] = e.getFinalResult()
+        dt = time.perf_counter() - t
+        if i >= args.warmup:
+            e2e_times.append(dt)
+    st = e.stats()
+    e2e_value = st["vertex_updates"] * len(e2e_times) / sum(e2e_times)
+    h2d = st["h2d_bytes"] + seeds.nbytes
+    d2h = 4 * nv + 8 * 4 * (MAX_ITERS + 1) + 256
+
+    if rank != 0:
+        return 0
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = json.load(open(peaks_path))["hbm_gbs"]
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = fim_bytes / (fim_ms * 1e-3) / 1e9 if fim_ms > 0 else 0.0
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "fim3d_visit_c3d.md")
+    if os.path.exists(prof):
+        for line in open(prof):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
+    lat = sorted(times)
+    res = {
+        "metric": METRIC, "value": value, "unit": "vertex-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "blocks": st0["num_blocks"], "iterations_per_solve": iters[0],
+                   "vertex_updates_per_solve": upd // args.steps, "max_iterations": MAX_ITERS,
+                   "l2": "flushed before every timed solve (512 MB write, outside the timed events)",
+                   "partition": "recursive coordinate bisection", "parallelism": f"replicas x{world}"},
+        "solves_per_s": world * args.steps / (total_ms * 1e-3),
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+        "setup_s": setup_s,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                     "kernel": "k_visit3d<false> (block sweeps)",
+                     "kernel_ms_per_step": fim_ms / args.steps,
+                     "note": "the sweep kernel is FP32-issue bound (tet local solver); see DESIGN.md"},
+        "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times)},
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        labels, nb = e.getPartition()
+        res["cpu_baseline"] = {k: v for k, v in cpu_sample(xyz, tets, metric, seed, labels, nb,
+                                                           args.cpu_sample_iters or MAX_ITERS).items()
+                               if k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(res), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

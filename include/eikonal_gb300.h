@@ -1,0 +1,166 @@
+/* eikonal_gb300.h — C ABI of the GB300 block-FIM Eikonal solver.
+ *
+ * This is the drop-in boundary for the reference's `Eikonal` class
+ * (SCI-Solver_Eikonal src/Eikonal.h:14-61, src/Eikonal.cu): plain pointers and
+ * sizes, status codes instead of exit(), no C++ or torch types.  A C++ class with
+ * the reference's member names sits on top of it (Eikonal.h in this directory).
+ *
+ * Call order: create -> set_options (optional) -> set_mesh / load_mesh ->
+ * set_speeds / set_initial_values / set_seeds / set_partition (optional, any
+ * order) -> solve -> get_result / get_iteration.  A handle may be solved again
+ * after changing speeds or seeds; unchanged mesh + partition data stay resident
+ * on the GPU between solves.
+ *
+ * Every function returns EIK_OK (0) or an error code; eik_last_error() gives the
+ * message of the last failure on that handle.  Handles are not thread-safe; use
+ * one handle per host thread.
+ */
+#ifndef EIKONAL_GB300_H
+#define EIKONAL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EIK_OK 0
+#define EIK_ERR_ARG 1    /* bad argument: null pointer, size mismatch, index out of range */
+#define EIK_ERR_STATE 2  /* call order: e.g. solve() before a mesh is set */
+#define EIK_ERR_MESH 3   /* unreadable or invalid mesh (the reference calls exit(1)) */
+#define EIK_ERR_CUDA 4   /* CUDA runtime failure (the reference calls exit(-1)) */
+#define EIK_ERR_LIMIT 5  /* a block does not fit in shared memory; use smaller blocks */
+#define EIK_ERR_DEVICE 6 /* a device-side bounded wait expired */
+#define EIK_ERR_IO 7     /* file output failed */
+
+#define EIK_SPEED_ONE 1 /* the reference's speedType_ ONE (src/core2d/include/TriMesh.h:15-16) */
+
+typedef struct eik_solver eik_solver;
+
+/* Public fields of the reference's Eikonal class (src/Eikonal.h:43-60) with its
+ * constructor defaults (src/Eikonal.cu:4-24), plus two additions at the end. */
+typedef struct eik_options {
+  int max_blocks;          /* maxBlocks_ (16); overwritten by the partitioner like the reference */
+  int max_verts_per_block; /* maxVertsPerBlock_ (64) */
+  float stop_distance;     /* stopDistance_ (50000); stored, unused by the scheme as in the reference */
+  int is_structured;       /* isStructured_ (0): lexicographic grid tiling instead of graph partition */
+  int speed_type;          /* speedType_ (EIK_SPEED_ONE) */
+  int square_length, square_width, square_depth;                 /* squareLength_/Width_/Depth_ (16) */
+  int square_block_length, square_block_width, square_block_depth; /* squareBlock*_ (1) */
+  int max_iterations;      /* maxIterations_ (100) */
+  int verbose;             /* verbose_ (0) */
+  int keep_history;        /* 1 (default): keep every iteration for eik_get_iteration */
+  int fim_sweeps;          /* sweeps per active-block visit; -1 = reference (3D 2, 2D 7) */
+} eik_options;
+
+typedef struct eik_stats {
+  int iterations;            /* outer iterations run (= numIterations()) */
+  int num_blocks;
+  long long vertex_updates;  /* owned vertices x sweeps summed over block visits */
+  long long fim_visits;      /* active-block visits */
+  long long check_visits;    /* neighbour-check visits */
+  long long slot_visits;     /* element slots streamed */
+  long long halo_visits;     /* halo vertices gathered */
+  long long owned_visits;    /* owned vertices loaded/stored */
+  float solve_ms;            /* device time of the last solve (CUDA events) */
+  float setup_ms;            /* host setup of the last solve (partition, layout, upload) */
+  int max_slots_per_block;
+  int max_local_vertices;
+  int total_slots;
+  double mean_slots_per_block;
+  double mean_halo_per_block;
+  int device_error;          /* device error flags of the last solve */
+  /* per-kernel figures of the last solve, from a device timer around every launch */
+  float fim_kernel_ms;       /* summed launch spans of the block-sweep kernel */
+  float check_kernel_ms;     /* summed launch spans of the neighbour-check kernel */
+  int fim_launches, check_launches;
+  long long fim_slots, fim_halo, fim_owned; /* inputs streamed by the block-sweep kernel */
+  long long h2d_bytes;       /* host-to-device bytes copied by the last solve (initial state) */
+} eik_stats;
+
+/* Fills `o` with the reference's defaults (src/Eikonal.cu:4-24). */
+void eik_default_options(eik_options* o);
+
+/* Eikonal(isTriMesh, ...) — src/Eikonal.cu:4-24.  is_tri_mesh: 1 = 2D triangles, 0 = 3D tets. */
+int eik_create(int is_tri_mesh, eik_solver** out);
+/* ~Eikonal — src/Eikonal.cu:26-35.  Null is ignored. */
+void eik_destroy(eik_solver* h);
+
+int eik_set_options(eik_solver* h, const eik_options* o);
+int eik_get_options(const eik_solver* h, eik_options* o);
+
+/* initializeMesh from memory — src/Eikonal.cu:99-133 (TriMesh::read /
+ * tetgenio::load_tetmesh + TetMesh::init).  xyz: 3*nv floats; elems: 3*ne (2D)
+ * or 4*ne (3D) vertex ids starting at 0 or 1 (tetmesh.cu:27-52). */
+int eik_set_mesh(eik_solver* h, const float* xyz, int nv, const int* elems, int ne);
+/* initializeMesh from a file: 2D ASCII .ply, 3D TetGen basename (.node/.ele).
+ * Returns EIK_ERR_MESH where the reference exits with status 1. */
+int eik_load_mesh(eik_solver* h, const char* filename);
+
+/* initSpeedMtxMultipliers — src/Eikonal.cu:62-67.  2D: ne speeds (inverse speed
+ * 1/s per triangle, TriMesh_stats.cu:64-68); 3D: ne scalars (metric s*I) or 6*ne
+ * metric entries M00 M01 M02 M11 M12 M22 (tetmesh.cu:54-79); any other count
+ * means unit speed, as in the reference.  n = 0 clears. */
+int eik_set_speeds(eik_solver* h, const float* vals, long long n);
+
+/* initializeVertices — src/Eikonal.cu:69-97: vertices whose value is 0 are seeds. */
+int eik_set_initial_values(eik_solver* h, const float* vals, int nv);
+
+/* Explicit seed list (same effect as initial values with zeros at the seeds). */
+int eik_set_seeds(eik_solver* h, const int* seeds, int n);
+
+/* Use these block labels (0..nblocks-1 per vertex) instead of the built-in
+ * partitioner (the reference calls METIS_PartGraphKway here,
+ * meshFIM2d_eikonal.cu:111-204 / meshFIM3dEikonal.cu:153-237).  labels = NULL
+ * returns to the built-in partitioner. */
+int eik_set_partition(eik_solver* h, const int* labels, int nv, int nblocks);
+
+/* solveEikonal — src/Eikonal.cu:135-231. */
+int eik_solve(eik_solver* h);
+
+/* The host half of solveEikonal alone (partition, block layout, metric terms),
+ * without touching the GPU; afterwards eik_get_partition / eik_get_stats describe
+ * the layout the next solve will use. */
+int eik_prepare(eik_solver* h);
+
+int eik_num_vertices(const eik_solver* h);
+/* numIterations — src/Eikonal.cu:46-48. */
+int eik_num_iterations(const eik_solver* h);
+/* getFinalResult — src/Eikonal.cu:38-40 (nv floats, original vertex order). */
+int eik_get_result(const eik_solver* h, float* out, int nv);
+/* Same, into device memory (out_dev must hold nv floats on the current device). */
+int eik_get_result_device(const eik_solver* h, float* out_dev, int nv);
+/* getResultAtIteration — src/Eikonal.cu:42-44 (needs keep_history). */
+int eik_get_iteration(const eik_solver* h, int i, float* out, int nv);
+/* Block labels used by the last solve. */
+int eik_get_partition(const eik_solver* h, int* labels, int nv, int* nblocks);
+int eik_get_stats(const eik_solver* h, eik_stats* s);
+/* writeVTK — src/Eikonal.cu:50-60: <prefix><i>.vtk for the last (all=0) or every
+ * (all=1) iteration; the reference's prefix is "result". */
+int eik_write_vtk(const eik_solver* h, const char* prefix, int all);
+
+/* 2D mesh preparation as the solver sees it after eik_set_mesh: oriented faces
+ * and the virtual faces that unfold obtuse corners (meshFIM2d_eikonal.h:40-72).
+ * Call with null arrays to get the sizes first. */
+int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned char* obtuse,
+                 int* vf_off, int* vf_verts);
+
+/* Self-test of the device local updates on host arrays, element-wise:
+ *   which = 0: tet update (localSolverTet1, core3d/cuda/CUDA_kernels.cu:69-225),
+ *              9 inputs per case (TA TB TC ACAC ACBC ACCD BCBC BCCD CDCD), 1 output;
+ *   which = 1: triangle update (core2d/cuda/CUDA_kernels.cu:143-204),
+ *              7 inputs per case (TA TB TC LenAB LenBC LenAC speedInv), 1 output;
+ *   which = 2: the FP32 forms of the reference's FP64 quotients, 2 inputs
+ *              (num, h) -> 2 outputs (num/(h+1e-8), num/(2h)). */
+int eik_selftest_local_update(int which, const float* in, float* out, int n);
+
+/* The CUDA stream (cudaStream_t) the handle's solves and copies run on, or null
+ * before the first solve.  Lets callers order their own work or time with events. */
+void* eik_stream(const eik_solver* h);
+
+const char* eik_last_error(const eik_solver* h);
+/* Library build string (version, CUDA arch). */
+const char* eik_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EIKONAL_GB300_H */

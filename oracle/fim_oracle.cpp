@@ -1,0 +1,102 @@
+// fim_oracle.cpp — TEST INFRASTRUCTURE ONLY.
+//
+// A CPU restatement of the reference block-partitioned Fast Iterative Method
+// (SCI-Solver_Eikonal) used as the checker for the GB300 CUDA path: the parity
+// tests, smoke() and bench.py's cpu_baseline leg call it.  Nothing in the product
+// library links or calls this file.
+//
+// It follows the reference's own data layout (padded per-block element slots that
+// each carry their own copy of the vertex travel times, plus per-vertex lists of
+// slot addresses) and its host schedule line by line, so that it is an independent
+// second implementation of the same scheme rather than a copy of the product's
+// compact layout.  Citations are paths inside the reference project.
+//
+//   3D:  src/core3d/cuda/meshFIM3dEikonal.cu  (PartitionTets :568-648,
+//        GenerateData :285-566, GetTetMem :680-827, GetVertMem :829-923)
+//        src/core3d/cuda/CUDA_kernels.cu     (FIMCuda :383-489,
+//        run_check_neghbor :493-602, CopyOutBack :604-668, run_reduction :7-33,
+//        localSolverTet1 :69-225)
+//   2D:  src/core2d/cuda/meshFIM2d_eikonal.cu (PartitionFaces :254-347,
+//        GenerateData :349-864)
+//        src/core2d/cuda/CUDA_kernels.cu     (FIMCuda :36-409,
+//        run_check_neighbor :415-799, run_reduction :8-30; triangle update :143-204)
+//
+// Every routine is instantiated for float (the reference arithmetic: FP32 with the
+// two FP64 divisions the reference source writes) and for double (the "FP64 run of
+// the same scheme" used to state the error of every FP32 result).
+//
+// Build: g++ -O2 -ffp-contract=off -fopenmp -shared -fPIC (oracle/build_oracle.py).
+// -ffp-contract=off keeps every product rounded on its own, like the reference's
+// host compile on x86-64; the GPU contracts a*b+c into FMA, so GPU-vs-oracle
+// comparisons carry a tolerance while GPU-vs-reference-kernel comparisons are
+// bitwise.
+
+#include "oracle_scheme.hpp"
+
+using namespace oracle;
+
+extern "C" {
+
+// Local updates, exposed for unit tests (precision 32 or 64).
+float oracle_tet_update_f32(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                            float BCBC, float BCCD, float CDCD) {
+  return tet_update<float>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+}
+double oracle_tet_update_f64(double TA, double TB, double TC, double ACAC, double ACBC,
+                             double ACCD, double BCBC, double BCCD, double CDCD) {
+  return tet_update<double>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+}
+float oracle_tri_update_f32(float TA, float TB, float TC, float LAB, float LBC, float LAC, float F) {
+  return tri_update<float>(TA, TB, TC, LAB, LBC, LAC, F);
+}
+
+// Whole 3D solve.  tets are 0-based; M holds 6 metric entries per tet.  Returns the
+// number of outer iterations (the length of the reference's iteration history), or
+// -1 on bad input.  `out_final` receives the last snapshot of d_vertT mapped to
+// vertices (0 for blocks that never ran, like the reference's cudaMemset buffer).
+int oracle3d_solve(int nv, const float* xyz, int nt, const int* tets, const float* M,
+                   const int* part, int nb, const int* seeds, int nseeds, int max_iters,
+                   int nsweeps, int precision, int nthreads, float* out_final, float* history,
+                   int hist_cap, long long* updates, int* max_tets) {
+  if (nv <= 0 || nt <= 0 || nb <= 0) return -1;
+  for (int v = 0; v < nv; ++v) if (part[v] < 0 || part[v] >= nb) return -1;
+  auto run = [&](auto& o) {
+    o.nv = nv; o.nt = nt; o.nb = nb; o.xyz = xyz; o.tets = tets; o.M = M; o.part = part;
+    const int it = o.solve(seeds, nseeds, max_iters, nsweeps, nthreads, out_final, history, hist_cap, updates);
+    if (max_tets) *max_tets = o.maxTets;
+    return it;
+  };
+  if (precision == 64) { Oracle3D<double> o; return run(o); }
+  Oracle3D<float> o;
+  return run(o);
+}
+
+// Whole 2D solve on an oriented mesh with its virtual faces (see the product's
+// triangle-mesh preparation).  speed_inv is per face; init_vals are the vertex
+// values the reference keeps in TriMesh::vertT (used by its all-vertices
+// convergence test).  Same return convention as oracle3d_solve.
+int oracle2d_solve(int nv, const float* xyz, int nf, const int* faces, const float* speed_inv,
+                   const uint8_t* obtuse, const int* vf_off, const int* vf_verts,
+                   const float* vf_speed_inv, const int* part, int nb, const int* seeds,
+                   int nseeds, const float* init_vals, int max_iters, int nsweeps, int precision,
+                   int nthreads, float* out_final, float* history, int hist_cap,
+                   long long* updates, int* max_faces) {
+  if (nv <= 0 || nf <= 0 || nb <= 0) return -1;
+  for (int v = 0; v < nv; ++v) if (part[v] < 0 || part[v] >= nb) return -1;
+  auto run = [&](auto& o) {
+    o.nv = nv; o.nf = nf; o.nb = nb; o.xyz = xyz; o.faces = faces; o.speedInv = speed_inv;
+    o.obtuse = obtuse; o.vfOff = vf_off; o.vfVerts = vf_verts; o.vfSpeedInv = vf_speed_inv;
+    o.part = part;
+    const int it = o.solve(seeds, nseeds, init_vals, max_iters, nsweeps, nthreads, out_final,
+                           history, hist_cap, updates);
+    if (max_faces) *max_faces = o.maxFaces;
+    return it;
+  };
+  if (precision == 64) { Oracle2D<double> o; return run(o); }
+  Oracle2D<float> o;
+  return run(o);
+}
+
+int oracle_num_threads(void) { return n_threads(0); }
+
+}  // extern "C"

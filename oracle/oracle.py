@@ -1,0 +1,230 @@
+"""ctypes binding of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, and only as the checker.  It wraps liboracle.so (fim_oracle.cpp, the CPU
+restatement of the reference scheme) and, where built, the reference's own tet
+local solver compiled for the host (_ref/libref_tet.so).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_FP = ctypes.POINTER(ctypes.c_float)
+_IP = ctypes.POINTER(ctypes.c_int)
+_UP = ctypes.POINTER(ctypes.c_ubyte)
+_LP = ctypes.POINTER(ctypes.c_longlong)
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            from . import build_oracle  # noqa: F401  (package-relative import when available)
+        _lib = ctypes.CDLL(path)
+        f = _lib.oracle_tet_update_f32
+        f.restype = ctypes.c_float
+        f.argtypes = [ctypes.c_float] * 9
+        f = _lib.oracle_tet_update_f64
+        f.restype = ctypes.c_double
+        f.argtypes = [ctypes.c_double] * 9
+        f = _lib.oracle_tri_update_f32
+        f.restype = ctypes.c_float
+        f.argtypes = [ctypes.c_float] * 7
+        _lib.oracle3d_solve.restype = ctypes.c_int
+        _lib.oracle3d_solve.argtypes = [ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _IP, ctypes.c_int, _IP,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        _FP, _FP, ctypes.c_int, _LP, _IP]
+        _lib.oracle2d_solve.restype = ctypes.c_int
+        _lib.oracle2d_solve.argtypes = [ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _UP, _IP, _IP, _FP, _IP,
+                                        ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, _FP, _FP, ctypes.c_int, _LP, _IP]
+        _lib.oracle_num_threads.restype = ctypes.c_int
+    return _lib
+
+
+def ref_lib():
+    """The reference's tet local solver compiled for the host, or None."""
+    global _ref
+    path = os.path.join(HERE, "_ref", "libref_tet.so")
+    if _ref is None and os.path.exists(path):
+        _ref = ctypes.CDLL(path)
+        _ref.ref_tet_local_solver.restype = ctypes.c_float
+        _ref.ref_tet_local_solver.argtypes = [ctypes.c_float] * 9
+    return _ref
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def metrics_from_speeds(nt, vals):
+    """Per-tet metric entries as TetMesh::init builds them (6*nt / nt / identity)."""
+    vals = None if vals is None else np.asarray(vals, dtype=np.float32).ravel()
+    M = np.zeros((nt, 6), dtype=np.float32)
+    if vals is not None and vals.size == 6 * nt:
+        return vals.reshape(nt, 6).copy()
+    if vals is not None and vals.size == nt:
+        M[:, 0] = M[:, 3] = M[:, 5] = vals
+        return M
+    M[:, 0] = M[:, 3] = M[:, 5] = 1.0
+    return M
+
+
+def solve3d(xyz, tets, metric6, labels, nblocks, seeds, max_iters=100, nsweeps=2, precision=32,
+            nthreads=0, history=False):
+    xyz, tets, M, lab, sd = _f(xyz), _i(tets), _f(metric6), _i(labels), _i(seeds)
+    nv, nt = xyz.shape[0], tets.shape[0]
+    out = np.empty(nv, dtype=np.float32)
+    hist = np.empty((max_iters, nv), dtype=np.float32) if history else None
+    upd = ctypes.c_longlong()
+    mt = ctypes.c_int()
+    it = lib().oracle3d_solve(nv, xyz.ctypes.data_as(_FP), nt, tets.ctypes.data_as(_IP), M.ctypes.data_as(_FP),
+                              lab.ctypes.data_as(_IP), int(nblocks), sd.ctypes.data_as(_IP), sd.size,
+                              int(max_iters), int(nsweeps), int(precision), int(nthreads),
+                              out.ctypes.data_as(_FP), hist.ctypes.data_as(_FP) if history else None,
+                              int(max_iters) if history else 0, ctypes.byref(upd), ctypes.byref(mt))
+    if it < 0:
+        raise ValueError("oracle3d_solve rejected its input")
+    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_tets": mt.value}
+    if history:
+        res["history"] = hist[:it]
+    return res
+
+
+def solve2d(xyz, faces, speed_inv, obtuse, vf_off, vf_verts, labels, nblocks, seeds, init_vals,
+            max_iters=100, nsweeps=7, precision=32, nthreads=0, vf_speed_inv=None, history=False):
+    xyz, faces, sinv, lab, sd, iv = _f(xyz), _i(faces), _f(speed_inv), _i(labels), _i(seeds), _f(init_vals)
+    obt = np.ascontiguousarray(obtuse, dtype=np.uint8)
+    off = _i(vf_off)
+    vfv = _i(vf_verts).reshape(-1)
+    if vfv.size == 0:
+        vfv = np.zeros(3, dtype=np.int32)
+    nvf = int(off[-1])
+    vsp = _f(np.ones(max(nvf, 1)) if vf_speed_inv is None else vf_speed_inv)
+    nv, nf = xyz.shape[0], faces.shape[0]
+    out = np.empty(nv, dtype=np.float32)
+    hist = np.empty((max_iters, nv), dtype=np.float32) if history else None
+    upd = ctypes.c_longlong()
+    mf = ctypes.c_int()
+    it = lib().oracle2d_solve(nv, xyz.ctypes.data_as(_FP), nf, faces.ctypes.data_as(_IP),
+                              sinv.ctypes.data_as(_FP), obt.ctypes.data_as(_UP), off.ctypes.data_as(_IP),
+                              vfv.ctypes.data_as(_IP), vsp.ctypes.data_as(_FP), lab.ctypes.data_as(_IP),
+                              int(nblocks), sd.ctypes.data_as(_IP), sd.size, iv.ctypes.data_as(_FP),
+                              int(max_iters), int(nsweeps), int(precision), int(nthreads),
+                              out.ctypes.data_as(_FP), hist.ctypes.data_as(_FP) if history else None,
+                              int(max_iters) if history else 0, ctypes.byref(upd), ctypes.byref(mf))
+    if it < 0:
+        raise ValueError("oracle2d_solve rejected its input")
+    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_faces": mf.value}
+    if history:
+        res["history"] = hist[:it]
+    return res
+
+
+def num_threads():
+    return lib().oracle_num_threads()
+
+
+# ---------------------------------------------------------------------------
+# the reference's own kernels (cubins built from the reference tree) driven by
+# the restated host loop in ref_gpu_driver.cpp
+# ---------------------------------------------------------------------------
+_gpu = None
+CUBIN3D = os.path.join(HERE, "_ref", "ref3d.cubin")
+CUBIN2D = os.path.join(HERE, "_ref", "ref2d.cubin")
+
+
+def ref_gpu():
+    """libref_gpu.so, or None when it or the cubins are missing."""
+    global _gpu
+    path = os.path.join(HERE, "libref_gpu.so")
+    if _gpu is None:
+        if not (os.path.exists(path) and os.path.exists(CUBIN3D) and os.path.exists(CUBIN2D)):
+            return None
+        g = ctypes.CDLL(path)
+        g.refgpu_last_error.restype = ctypes.c_char_p
+        g.refgpu_tet_local_solver.restype = ctypes.c_int
+        g.refgpu_tet_local_solver.argtypes = [ctypes.c_char_p, _FP, _FP, ctypes.c_int]
+        g.refgpu_solve3d.restype = ctypes.c_int
+        g.refgpu_solve3d.argtypes = [ctypes.c_char_p, ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _IP, ctypes.c_int,
+                                     _IP, ctypes.c_int, ctypes.c_int, _FP, _FP, ctypes.c_int, _LP, _IP]
+        g.refgpu_solve2d.restype = ctypes.c_int
+        g.refgpu_solve2d.argtypes = [ctypes.c_char_p, ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _UP, _IP, _IP, _FP,
+                                     _IP, ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_int, _FP, _FP, ctypes.c_int,
+                                     _LP, _IP]
+        _gpu = g
+    return _gpu
+
+
+class ReferenceUnavailable(RuntimeError):
+    pass
+
+
+def _gpu_check(rc):
+    if rc == -1:
+        raise ReferenceUnavailable(ref_gpu().refgpu_last_error().decode())
+    if rc < 0:
+        raise RuntimeError("reference kernels failed: " + ref_gpu().refgpu_last_error().decode())
+    return rc
+
+
+def ref_gpu_tet_local_solver(inputs9):
+    a = _f(inputs9).reshape(-1, 9)
+    out = np.empty(a.shape[0], dtype=np.float32)
+    _gpu_check(ref_gpu().refgpu_tet_local_solver(CUBIN3D.encode(), a.ctypes.data_as(_FP), out.ctypes.data_as(_FP),
+                                                 a.shape[0]))
+    return out
+
+
+def ref_gpu_solve3d(xyz, tets, metric6, labels, nblocks, seeds, max_iters=100, history=False):
+    xyz, tets, M, lab, sd = _f(xyz), _i(tets), _f(metric6), _i(labels), _i(seeds)
+    nv = xyz.shape[0]
+    out = np.empty(nv, dtype=np.float32)
+    hist = np.empty((max_iters, nv), dtype=np.float32) if history else None
+    upd, mt = ctypes.c_longlong(), ctypes.c_int()
+    it = _gpu_check(ref_gpu().refgpu_solve3d(
+        CUBIN3D.encode(), nv, xyz.ctypes.data_as(_FP), tets.shape[0], tets.ctypes.data_as(_IP),
+        M.ctypes.data_as(_FP), lab.ctypes.data_as(_IP), int(nblocks), sd.ctypes.data_as(_IP), sd.size,
+        int(max_iters), out.ctypes.data_as(_FP), hist.ctypes.data_as(_FP) if history else None,
+        int(max_iters) if history else 0, ctypes.byref(upd), ctypes.byref(mt)))
+    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_tets": mt.value}
+    if history:
+        res["history"] = hist[:it]
+    return res
+
+
+def ref_gpu_solve2d(xyz, faces, speed_inv, obtuse, vf_off, vf_verts, labels, nblocks, seeds, init_vals,
+                    max_iters=100, vf_speed_inv=None, history=False):
+    xyz, faces, sinv, lab, sd, iv = _f(xyz), _i(faces), _f(speed_inv), _i(labels), _i(seeds), _f(init_vals)
+    obt = np.ascontiguousarray(obtuse, dtype=np.uint8)
+    off = _i(vf_off)
+    vfv = _i(vf_verts).reshape(-1)
+    if vfv.size == 0:
+        vfv = np.zeros(3, dtype=np.int32)
+    nvf = int(off[-1])
+    vsp = _f(np.ones(max(nvf, 1)) if vf_speed_inv is None else vf_speed_inv)
+    nv = xyz.shape[0]
+    out = np.empty(nv, dtype=np.float32)
+    hist = np.empty((max_iters, nv), dtype=np.float32) if history else None
+    upd, mf = ctypes.c_longlong(), ctypes.c_int()
+    it = _gpu_check(ref_gpu().refgpu_solve2d(
+        CUBIN2D.encode(), nv, xyz.ctypes.data_as(_FP), faces.shape[0], faces.ctypes.data_as(_IP),
+        sinv.ctypes.data_as(_FP), obt.ctypes.data_as(_UP), off.ctypes.data_as(_IP), vfv.ctypes.data_as(_IP),
+        vsp.ctypes.data_as(_FP), lab.ctypes.data_as(_IP), int(nblocks), sd.ctypes.data_as(_IP), sd.size,
+        iv.ctypes.data_as(_FP), int(max_iters), out.ctypes.data_as(_FP),
+        hist.ctypes.data_as(_FP) if history else None, int(max_iters) if history else 0, ctypes.byref(upd),
+        ctypes.byref(mf)))
+    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_faces": mf.value}
+    if history:
+        res["history"] = hist[:it]
+    return res

@@ -1,0 +1,328 @@
+"""Python binding of the GB300 block-FIM Eikonal solver.
+
+The product is the C ABI in include/eikonal_gb300.h (libeikonal_gb300.so, built
+by build.py next to this file).  This module loads that library with ctypes and
+offers `Eikonal`, a class with the reference's member names and methods
+(SCI-Solver_Eikonal src/Eikonal.h:14-61), so tests and scripts read like the
+reference's own tests.  Importing never falls back to a CPU path: a missing or
+unloadable library raises ImportError.
+
+The directory name contains a hyphen, so import it with
+``importlib.import_module("sci-solver_eikonal_gb300")``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libeikonal_gb300.so")
+
+EIK_OK = 0
+ERRORS = {1: "EIK_ERR_ARG", 2: "EIK_ERR_STATE", 3: "EIK_ERR_MESH", 4: "EIK_ERR_CUDA",
+          5: "EIK_ERR_LIMIT", 6: "EIK_ERR_DEVICE", 7: "EIK_ERR_IO"}
+ONE = 1  # speed type ONE
+
+
+class EikOptions(ctypes.Structure):
+    _fields_ = [
+        ("max_blocks", ctypes.c_int), ("max_verts_per_block", ctypes.c_int),
+        ("stop_distance", ctypes.c_float), ("is_structured", ctypes.c_int),
+        ("speed_type", ctypes.c_int),
+        ("square_length", ctypes.c_int), ("square_width", ctypes.c_int), ("square_depth", ctypes.c_int),
+        ("square_block_length", ctypes.c_int), ("square_block_width", ctypes.c_int),
+        ("square_block_depth", ctypes.c_int),
+        ("max_iterations", ctypes.c_int), ("verbose", ctypes.c_int), ("keep_history", ctypes.c_int),
+        ("fim_sweeps", ctypes.c_int),
+    ]
+
+
+class EikStats(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int), ("num_blocks", ctypes.c_int),
+        ("vertex_updates", ctypes.c_longlong), ("fim_visits", ctypes.c_longlong),
+        ("check_visits", ctypes.c_longlong), ("slot_visits", ctypes.c_longlong),
+        ("halo_visits", ctypes.c_longlong), ("owned_visits", ctypes.c_longlong),
+        ("solve_ms", ctypes.c_float), ("setup_ms", ctypes.c_float),
+        ("max_slots_per_block", ctypes.c_int), ("max_local_vertices", ctypes.c_int),
+        ("total_slots", ctypes.c_int), ("mean_slots_per_block", ctypes.c_double),
+        ("mean_halo_per_block", ctypes.c_double), ("device_error", ctypes.c_int),
+        ("fim_kernel_ms", ctypes.c_float), ("check_kernel_ms", ctypes.c_float),
+        ("fim_launches", ctypes.c_int), ("check_launches", ctypes.c_int),
+        ("fim_slots", ctypes.c_longlong), ("fim_halo", ctypes.c_longlong), ("fim_owned", ctypes.c_longlong),
+        ("h2d_bytes", ctypes.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_P = ctypes.c_void_p
+_FP = ctypes.POINTER(ctypes.c_float)
+_IP = ctypes.POINTER(ctypes.c_int)
+_UP = ctypes.POINTER(ctypes.c_ubyte)
+
+# name: (restype, argtypes) — every symbol declared in include/eikonal_gb300.h
+SIGNATURES = {
+    "eik_default_options": (None, [ctypes.POINTER(EikOptions)]),
+    "eik_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
+    "eik_destroy": (None, [_P]),
+    "eik_set_options": (ctypes.c_int, [_P, ctypes.POINTER(EikOptions)]),
+    "eik_get_options": (ctypes.c_int, [_P, ctypes.POINTER(EikOptions)]),
+    "eik_set_mesh": (ctypes.c_int, [_P, _FP, ctypes.c_int, _IP, ctypes.c_int]),
+    "eik_load_mesh": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "eik_set_speeds": (ctypes.c_int, [_P, _FP, ctypes.c_longlong]),
+    "eik_set_initial_values": (ctypes.c_int, [_P, _FP, ctypes.c_int]),
+    "eik_set_seeds": (ctypes.c_int, [_P, _IP, ctypes.c_int]),
+    "eik_set_partition": (ctypes.c_int, [_P, _IP, ctypes.c_int, ctypes.c_int]),
+    "eik_solve": (ctypes.c_int, [_P]),
+    "eik_prepare": (ctypes.c_int, [_P]),
+    "eik_num_vertices": (ctypes.c_int, [_P]),
+    "eik_num_iterations": (ctypes.c_int, [_P]),
+    "eik_get_result": (ctypes.c_int, [_P, _FP, ctypes.c_int]),
+    "eik_get_result_device": (ctypes.c_int, [_P, _P, ctypes.c_int]),
+    "eik_get_iteration": (ctypes.c_int, [_P, ctypes.c_int, _FP, ctypes.c_int]),
+    "eik_get_partition": (ctypes.c_int, [_P, _IP, ctypes.c_int, _IP]),
+    "eik_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(EikStats)]),
+    "eik_write_vtk": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
+    "eik_tri_prep": (ctypes.c_int, [_P, _IP, _IP, _IP, _UP, _IP, _IP]),
+    "eik_selftest_local_update": (ctypes.c_int, [ctypes.c_int, _FP, _FP, ctypes.c_int]),
+    "eik_stream": (_P, [_P]),
+    "eik_last_error": (ctypes.c_char_p, [_P]),
+    "eik_version": (ctypes.c_char_p, []),
+}
+
+
+def load_library(path=LIB_PATH):
+    """Loads the C ABI library and declares every entry point; raises ImportError."""
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with sci-solver_eikonal_gb300/build.py "
+                          "(or __graft_entry__.build())")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = load_library()
+    return _lib
+
+
+class EikonalError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_FP)
+
+
+def _iptr(a):
+    return a.ctypes.data_as(_IP)
+
+
+class Eikonal:
+    """The reference's Eikonal class over the C ABI.
+
+    Attribute names follow src/Eikonal.h:43-60 (verbose_, filename_, maxBlocks_,
+    maxVertsPerBlock_, ...).  Meshes come from a file (filename_) or from arrays
+    (set_mesh); results are numpy float32 arrays.
+    """
+
+    _OPT_FIELDS = {
+        "maxBlocks_": "max_blocks", "maxVertsPerBlock_": "max_verts_per_block",
+        "stopDistance_": "stop_distance", "isStructured_": "is_structured", "speedType_": "speed_type",
+        "squareLength_": "square_length", "squareWidth_": "square_width", "squareDepth_": "square_depth",
+        "squareBlockLength_": "square_block_length", "squareBlockWidth_": "square_block_width",
+        "squareBlockDepth_": "square_block_depth", "maxIterations_": "max_iterations",
+        "verbose_": "verbose", "keepHistory_": "keep_history", "fimSweeps_": "fim_sweeps",
+    }
+
+    def __init__(self, isTriMesh, fname="../src/test/test_data/sphere_74verts.ply", verbose=False):
+        self._lib = lib()
+        h = _P()
+        rc = self._lib.eik_create(1 if isTriMesh else 0, ctypes.byref(h))
+        if rc:
+            raise EikonalError(rc, "eik_create failed")
+        self._h = h
+        opts = EikOptions()
+        self._lib.eik_default_options(ctypes.byref(opts))
+        for py, c in self._OPT_FIELDS.items():
+            object.__setattr__(self, py, getattr(opts, c))
+        self.verbose_ = bool(verbose)
+        self.isTriMesh_ = bool(isTriMesh)
+        self.filename_ = fname
+        self.userSetInitial_ = False
+        self.speedMtxMultipliers_ = []
+        self._mesh_loaded = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.eik_destroy(h)
+            self._h = None
+
+    # -- helpers ---------------------------------------------------------------
+    def _check(self, rc):
+        if rc:
+            raise EikonalError(rc, self._lib.eik_last_error(self._h).decode())
+
+    def _push_options(self):
+        opts = EikOptions()
+        for py, c in self._OPT_FIELDS.items():
+            setattr(opts, c, type(getattr(opts, c))(getattr(self, py)))
+        self._check(self._lib.eik_set_options(self._h, ctypes.byref(opts)))
+
+    def _pull_options(self):
+        opts = EikOptions()
+        self._check(self._lib.eik_get_options(self._h, ctypes.byref(opts)))
+        for py, c in self._OPT_FIELDS.items():
+            object.__setattr__(self, py, getattr(opts, c))
+
+    # -- reference API ------------------------------------------------------------
+    def set_mesh(self, xyz, elems):
+        """initializeMesh from arrays (nv x 3 floats, ne x 3 or ne x 4 ints)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        per = 3 if self.isTriMesh_ else 4
+        elems = np.ascontiguousarray(elems, dtype=np.int32).reshape(-1, per)
+        self._check(self._lib.eik_set_mesh(self._h, _fptr(xyz), xyz.shape[0], _iptr(elems), elems.shape[0]))
+        self._mesh_loaded = True
+
+    def initializeMesh(self):
+        """src/Eikonal.cu:99-133: loads filename_ (raises EikonalError EIK_ERR_MESH on failure)."""
+        if not self._mesh_loaded:
+            self._check(self._lib.eik_load_mesh(self._h, str(self.filename_).encode()))
+            self._mesh_loaded = True
+
+    def initializeVertices(self, values):
+        v = np.ascontiguousarray(values, dtype=np.float32)
+        self._check(self._lib.eik_set_initial_values(self._h, _fptr(v), v.size))
+        self.userSetInitial_ = True
+
+    def initSpeedMtxMultipliers(self, values):
+        self.speedMtxMultipliers_ = np.ascontiguousarray(values, dtype=np.float32)
+        v = self.speedMtxMultipliers_
+        self._check(self._lib.eik_set_speeds(self._h, _fptr(v) if v.size else None, v.size))
+
+    def setSeeds(self, seeds):
+        s = np.ascontiguousarray(seeds, dtype=np.int32)
+        self._check(self._lib.eik_set_seeds(self._h, _iptr(s), s.size))
+
+    def setPartition(self, labels, nblocks=None):
+        if labels is None:
+            self._check(self._lib.eik_set_partition(self._h, None, 0, 0))
+            return
+        lab = np.ascontiguousarray(labels, dtype=np.int32)
+        nb = int(lab.max()) + 1 if nblocks is None else int(nblocks)
+        self._check(self._lib.eik_set_partition(self._h, _iptr(lab), lab.size, nb))
+
+    def solveEikonal(self):
+        if not self._mesh_loaded:
+            self.initializeMesh()
+        self._push_options()
+        self._check(self._lib.eik_solve(self._h))
+        self._pull_options()
+
+    def prepare(self):
+        """Partition and block layout on the host only (no GPU needed)."""
+        if not self._mesh_loaded:
+            self.initializeMesh()
+        self._push_options()
+        self._check(self._lib.eik_prepare(self._h))
+        self._pull_options()
+
+    def numVertices(self):
+        return self._lib.eik_num_vertices(self._h)
+
+    def numIterations(self):
+        return self._lib.eik_num_iterations(self._h)
+
+    def getFinalResult(self):
+        out = np.empty(self.numVertices(), dtype=np.float32)
+        self._check(self._lib.eik_get_result(self._h, _fptr(out), out.size))
+        return out
+
+    def getResultDevice(self, dev_ptr):
+        self._check(self._lib.eik_get_result_device(self._h, ctypes.c_void_p(dev_ptr), self.numVertices()))
+
+    def getResultAtIteration(self, i):
+        out = np.empty(self.numVertices(), dtype=np.float32)
+        self._check(self._lib.eik_get_iteration(self._h, int(i), _fptr(out), out.size))
+        return out
+
+    def getPartition(self):
+        nb = ctypes.c_int()
+        lab = np.empty(self.numVertices(), dtype=np.int32)
+        self._check(self._lib.eik_get_partition(self._h, _iptr(lab), lab.size, ctypes.byref(nb)))
+        return lab, nb.value
+
+    def stream(self):
+        """cudaStream_t (as an int) the solves run on, or 0 before the first solve."""
+        return self._lib.eik_stream(self._h) or 0
+
+    def stats(self):
+        s = EikStats()
+        self._check(self._lib.eik_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def writeVTK(self, all_iterations=False, prefix="result"):
+        self._check(self._lib.eik_write_vtk(self._h, prefix.encode(), 1 if all_iterations else 0))
+
+    def triPrep(self):
+        """Oriented faces, obtuse-corner bits and virtual faces of a 2D mesh."""
+        nf, nvf = ctypes.c_int(), ctypes.c_int()
+        self._check(self._lib.eik_tri_prep(self._h, ctypes.byref(nf), ctypes.byref(nvf), None, None, None, None))
+        faces = np.empty((nf.value, 3), dtype=np.int32)
+        obt = np.empty(nf.value, dtype=np.uint8)
+        off = np.empty(nf.value + 1, dtype=np.int32)
+        vfv = np.empty((max(nvf.value, 1), 3), dtype=np.int32)
+        self._check(self._lib.eik_tri_prep(self._h, None, None, _iptr(faces), obt.ctypes.data_as(_UP),
+                                           _iptr(off), _iptr(vfv)))
+        return faces, obt, off, vfv[:nvf.value]
+
+    def printErrorGraph(self, solution):
+        """src/Eikonal.cu:233-279: ASCII plot of the RMS error per iteration."""
+        sol = np.asarray(solution, dtype=np.float32)
+        rms = [float(np.sqrt(np.mean((sol - self.getResultAtIteration(i)) ** 2)))
+               for i in range(self.numIterations())]
+        if not rms:
+            return
+        mx, mn = rms[0], rms[-1]
+        hi, lo = -10, 10
+        while 10.0 ** hi < mx:
+            hi += 1
+        while 10.0 ** lo > mn:
+            lo -= 1
+        print("\n\nlog(Err)|")
+        tick = True
+        for i in range(hi, lo - 1, -1):
+            row = "".join("*" if 10.0 ** i < r < 10.0 ** (i + 1) else " " for r in rms)
+            print((f"   10^{i:2d}|" if tick else "        |") + row)
+            tick = not tick
+        print("--------|------------------------------------------" + f"  Converged to: {rms[-1]:.4f}")
+        print("        |1   5    10   15   20   25   30   35")
+        print("                   Iteration")
+
+
+def selftest_local_update(which, inputs):
+    """Evaluates the device local updates element-wise (see eik_selftest_local_update)."""
+    nin, nout = {0: (9, 1), 1: (7, 1), 2: (2, 2)}[which]
+    a = np.ascontiguousarray(inputs, dtype=np.float32).reshape(-1, nin)
+    out = np.empty((a.shape[0], nout), dtype=np.float32)
+    rc = lib().eik_selftest_local_update(which, _fptr(a), _fptr(out), a.shape[0])
+    if rc:
+        raise EikonalError(rc, "self-test kernel failed")
+    return out if nout > 1 else out[:, 0]
+
+
+def version():
+    return lib().eik_version().decode()

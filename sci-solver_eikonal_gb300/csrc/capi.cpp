@@ -1,0 +1,443 @@
+// capi.cpp — the C ABI (include/eikonal_gb300.h) over the host setup and the
+// device-resident solve.  Mirrors the reference's Eikonal facade
+// (src/Eikonal.cu:4-279): same defaults, same seed rules, same partition-size
+// rules, status codes where the reference exits.
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/eikonal_gb300.h"
+#include "device.hpp"
+#include "mesh_io.hpp"
+#include "setup.hpp"
+
+using namespace eikgb;
+
+struct eik_solver {
+  int dim = 3;
+  eik_options opt{};
+  std::string err;
+  // mesh as given (0-based after normalisation)
+  std::vector<float> xyz;
+  std::vector<int> elems;
+  int nv = 0, ne = 0;
+  unsigned mesh_ver = 0;
+  // inputs
+  std::vector<float> speeds;
+  bool speeds_set = false;
+  unsigned speed_ver = 0;
+  std::vector<float> init_vals;
+  bool user_initial = false;
+  std::vector<int> seeds;
+  bool user_seeds = false;
+  std::vector<int> user_labels;
+  int user_nb = 0;
+  unsigned part_ver = 0;
+  // derived
+  TriPrep prep;
+  unsigned prep_mesh = ~0u;
+  std::vector<int> labels;
+  int nb = 0;
+  unsigned lay_mesh = ~0u, lay_part = ~0u, lay_speed = ~0u;
+  std::string lay_key;
+  Layout layout;
+  std::unique_ptr<DeviceSolve> dev;
+  bool uploaded = false;
+  bool solved = false;
+  eik_stats stats{};
+};
+
+namespace {
+
+int fail(eik_solver* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+std::string partition_key(const eik_solver* h) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%u|%d|%d|%d|%d,%d,%d|%d,%d,%d", h->part_ver, h->opt.is_structured,
+                h->opt.max_verts_per_block, h->dim, h->opt.square_length, h->opt.square_width, h->opt.square_depth,
+                h->opt.square_block_length, h->opt.square_block_width, h->opt.square_block_depth);
+  return buf;
+}
+
+// Block labels as the reference chooses them (src/Eikonal.cu:162-174, 204-220).
+int make_partition(eik_solver* h) {
+  if (!h->user_labels.empty()) {
+    h->labels = h->user_labels;
+    h->nb = h->user_nb;
+  } else if (h->opt.is_structured) {
+    std::string e = partition_square(h->nv, h->dim, h->opt.square_length, h->opt.square_width, h->opt.square_depth,
+                                     h->opt.square_block_length, h->opt.square_block_width,
+                                     h->opt.square_block_depth, h->labels, h->nb);
+    if (!e.empty()) return fail(h, EIK_ERR_ARG, e);
+  } else {
+    h->nb = metis_rule_blocks(h->nv, h->opt.max_verts_per_block, h->dim);
+    partition_rcb(h->nv, h->xyz.data(), h->nb, h->labels);
+  }
+  h->opt.max_blocks = h->nb;  // the reference overwrites maxBlocks_ the same way
+  return EIK_OK;
+}
+
+std::vector<float> speed_inverse(const eik_solver* h) {
+  // TriMesh::InitializeAttributes (TriMesh_stats.cu:64-68): 1/speed per face when
+  // the vector matches the face count, else 1
+  std::vector<float> inv(h->ne, 1.0f);
+  if (h->speeds_set && (int)h->speeds.size() == h->ne)
+    for (int i = 0; i < h->ne; ++i) inv[i] = 1.f / h->speeds[i];
+  return inv;
+}
+
+// Partition + block layout on the host, cached while the mesh, the partition
+// inputs and the speeds are unchanged; refreshes only the metric terms when just
+// the speeds changed.
+int host_prepare(eik_solver* h, bool* new_layout_out) {
+  bool new_layout = false;
+  const std::string key = partition_key(h);
+  if (h->lay_mesh != h->mesh_ver || h->lay_key != key) {
+    int rc = make_partition(h);
+    if (rc) return rc;
+    std::string e;
+    if (h->dim == 3) {
+      std::vector<float> M;
+      tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), M);
+      e = build_layout3d(h->nv, h->xyz.data(), h->ne, h->elems.data(), M.data(), h->labels.data(), h->nb,
+                         h->layout);
+    } else {
+      const std::vector<float> inv = speed_inverse(h);
+      e = build_layout2d(h->nv, h->xyz.data(), h->prep, inv.data(), h->labels.data(), h->nb, h->layout);
+    }
+    if (!e.empty()) return fail(h, EIK_ERR_MESH, e);
+    h->lay_mesh = h->mesh_ver;
+    h->lay_key = key;
+    h->lay_speed = h->speed_ver;
+    h->uploaded = false;  // device copy is stale until the next solve uploads it
+    new_layout = true;
+  } else if (h->lay_speed != h->speed_ver) {
+    if (h->dim == 3) {
+      std::vector<float> M;
+      tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), M);
+      refresh_gram3d(h->xyz.data(), h->elems.data(), M.data(), h->layout);
+    } else {
+      const std::vector<float> inv = speed_inverse(h);
+      refresh_speed2d(h->prep, inv.data(), h->layout);
+    }
+    h->lay_speed = h->speed_ver;
+    if (h->uploaded) {
+      std::string e = h->dev->upload_coef(h->layout);
+      if (!e.empty()) return fail(h, EIK_ERR_CUDA, e);
+    }
+  }
+  *new_layout_out = new_layout;
+  return EIK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void eik_default_options(eik_options* o) {
+  if (!o) return;
+  o->max_blocks = 16;
+  o->max_verts_per_block = 64;
+  o->stop_distance = 50000.f;
+  o->is_structured = 0;
+  o->speed_type = EIK_SPEED_ONE;
+  o->square_length = o->square_width = o->square_depth = 16;
+  o->square_block_length = o->square_block_width = o->square_block_depth = 1;
+  o->max_iterations = 100;
+  o->verbose = 0;
+  o->keep_history = 1;
+  o->fim_sweeps = -1;
+}
+
+int eik_create(int is_tri_mesh, eik_solver** out) {
+  if (!out) return EIK_ERR_ARG;
+  *out = nullptr;
+  eik_solver* h = new eik_solver;
+  h->dim = is_tri_mesh ? 2 : 3;
+  eik_default_options(&h->opt);
+  *out = h;
+  return EIK_OK;
+}
+
+void eik_destroy(eik_solver* h) { delete h; }
+
+int eik_set_options(eik_solver* h, const eik_options* o) {
+  if (!h || !o) return fail(h, EIK_ERR_ARG, "null argument");
+  if (o->max_verts_per_block <= 0) return fail(h, EIK_ERR_ARG, "max_verts_per_block must be positive");
+  if (o->max_iterations < 0) return fail(h, EIK_ERR_ARG, "max_iterations must be >= 0");
+  if (o->speed_type != EIK_SPEED_ONE) return fail(h, EIK_ERR_ARG, "only speed type ONE is supported");
+  h->opt = *o;
+  return EIK_OK;
+}
+
+int eik_get_options(const eik_solver* h, eik_options* o) {
+  if (!h || !o) return EIK_ERR_ARG;
+  *o = h->opt;
+  return EIK_OK;
+}
+
+int eik_set_mesh(eik_solver* h, const float* xyz, int nv, const int* elems, int ne) {
+  if (!h || !xyz || !elems || nv <= 0 || ne <= 0) return fail(h, EIK_ERR_ARG, "invalid mesh arrays");
+  const int per = (h->dim == 3) ? 4 : 3;
+  std::vector<int> e(elems, elems + (size_t)per * ne);
+  std::string msg = normalize_index_base(e, nv);
+  if (!msg.empty()) return fail(h, EIK_ERR_MESH, msg);
+  h->xyz.assign(xyz, xyz + 3 * (size_t)nv);
+  h->elems.swap(e);
+  h->nv = nv;
+  h->ne = ne;
+  h->mesh_ver++;
+  h->solved = false;
+  if (h->dim == 2) {
+    msg = prepare_trimesh(nv, h->xyz.data(), ne, h->elems.data(), h->prep);
+    if (!msg.empty()) return fail(h, EIK_ERR_MESH, msg);
+    h->prep_mesh = h->mesh_ver;
+  }
+  return EIK_OK;
+}
+
+int eik_load_mesh(eik_solver* h, const char* filename) {
+  if (!h || !filename) return fail(h, EIK_ERR_ARG, "null argument");
+  std::vector<float> xyz;
+  std::vector<int> el;
+  std::string msg = (h->dim == 2) ? read_ply(filename, xyz, el) : read_tetgen(filename, xyz, el);
+  if (!msg.empty()) return fail(h, EIK_ERR_MESH, msg);
+  const int per = (h->dim == 3) ? 4 : 3;
+  return eik_set_mesh(h, xyz.data(), (int)(xyz.size() / 3), el.data(), (int)(el.size() / per));
+}
+
+int eik_set_speeds(eik_solver* h, const float* vals, long long n) {
+  if (!h || (n > 0 && !vals) || n < 0) return fail(h, EIK_ERR_ARG, "invalid speed array");
+  h->speeds.assign(vals, vals + n);
+  h->speeds_set = n > 0;
+  h->speed_ver++;
+  return EIK_OK;
+}
+
+int eik_set_initial_values(eik_solver* h, const float* vals, int nv) {
+  if (!h || !vals) return fail(h, EIK_ERR_ARG, "null argument");
+  if (h->nv == 0) return fail(h, EIK_ERR_STATE, "You must initialize the mesh first!");
+  if (nv != h->nv) return fail(h, EIK_ERR_ARG, "Initialize values size does not match number of vertices!");
+  h->init_vals.assign(vals, vals + nv);
+  h->user_initial = true;
+  h->user_seeds = false;
+  return EIK_OK;
+}
+
+int eik_set_seeds(eik_solver* h, const int* seeds, int n) {
+  if (!h || (n > 0 && !seeds) || n < 0) return fail(h, EIK_ERR_ARG, "invalid seed array");
+  for (int i = 0; i < n; ++i)
+    if (seeds[i] < 0 || (h->nv > 0 && seeds[i] >= h->nv)) return fail(h, EIK_ERR_ARG, "seed out of range");
+  h->seeds.assign(seeds, seeds + n);
+  h->user_seeds = true;
+  h->user_initial = false;
+  return EIK_OK;
+}
+
+int eik_set_partition(eik_solver* h, const int* labels, int nv, int nblocks) {
+  if (!h) return EIK_ERR_ARG;
+  if (!labels) {
+    h->user_labels.clear();
+    h->user_nb = 0;
+    h->part_ver++;
+    return EIK_OK;
+  }
+  if (h->nv == 0) return fail(h, EIK_ERR_STATE, "set the mesh before the partition");
+  if (nv != h->nv || nblocks <= 0) return fail(h, EIK_ERR_ARG, "partition size mismatch");
+  for (int i = 0; i < nv; ++i)
+    if (labels[i] < 0 || labels[i] >= nblocks) return fail(h, EIK_ERR_ARG, "partition label out of range");
+  h->user_labels.assign(labels, labels + nv);
+  h->user_nb = nblocks;
+  h->part_ver++;
+  return EIK_OK;
+}
+
+int eik_solve(eik_solver* h) {
+  if (!h) return EIK_ERR_ARG;
+  if (h->nv == 0) return fail(h, EIK_ERR_STATE, "no mesh: call eik_set_mesh or eik_load_mesh first");
+  const auto t0 = std::chrono::steady_clock::now();
+  // seeds (src/Eikonal.cu:143-159, 186-202)
+  std::vector<int> seeds;
+  const float* init = nullptr;
+  if (h->user_initial) {
+    for (int v = 0; v < h->nv; ++v)
+      if (h->init_vals[v] == 0.) seeds.push_back(v);
+    init = h->init_vals.data();
+  } else if (h->user_seeds) {
+    seeds = h->seeds;
+  } else {
+    seeds.push_back(0);
+  }
+  for (int s : seeds)
+    if (s >= h->nv) return fail(h, EIK_ERR_ARG, "seed out of range");
+  bool new_layout = false;
+  int rc = host_prepare(h, &new_layout);
+  if (rc) return rc;
+  if (!h->dev) h->dev.reset(new DeviceSolve);
+  if (new_layout || !h->uploaded) {
+    std::string e = h->dev->upload(h->layout);
+    if (!e.empty()) {
+      h->uploaded = false;
+      return fail(h, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+    }
+    h->uploaded = true;
+  }
+  std::string e = h->dev->set_seeds(seeds, (h->dim == 2) ? init : nullptr);
+  if (!e.empty()) return fail(h, EIK_ERR_ARG, e);
+  const auto t1 = std::chrono::steady_clock::now();
+  SolveOptions so;
+  so.max_iterations = h->opt.max_iterations;
+  so.fim_sweeps = h->opt.fim_sweeps;
+  so.keep_history = h->opt.keep_history != 0;
+  so.history_cap = h->opt.max_iterations;
+  e = h->dev->solve(so);
+  if (!e.empty()) {
+    h->solved = false;
+    return fail(h, h->dev->stats().error ? EIK_ERR_DEVICE : EIK_ERR_CUDA, e);
+  }
+  h->solved = true;
+  const SolveStats& st = h->dev->stats();
+  eik_stats& s = h->stats;
+  s.iterations = st.iterations;
+  s.num_blocks = h->nb;
+  s.vertex_updates = st.vertex_updates;
+  s.fim_visits = st.fim_visits;
+  s.check_visits = st.check_visits;
+  s.slot_visits = st.slot_visits;
+  s.halo_visits = st.halo_visits;
+  s.owned_visits = st.owned_visits;
+  s.solve_ms = st.solve_ms;
+  s.setup_ms = std::chrono::duration<float, std::milli>(t1 - t0).count();
+  s.max_slots_per_block = h->layout.max_slots;
+  s.max_local_vertices = h->layout.max_local;
+  s.total_slots = h->layout.total_slots;
+  s.mean_slots_per_block = h->layout.mean_slots_per_block;
+  s.mean_halo_per_block = h->layout.mean_halo_per_block;
+  s.device_error = st.error;
+  s.fim_kernel_ms = st.fim_kernel_ms;
+  s.check_kernel_ms = st.check_kernel_ms;
+  s.fim_launches = st.fim_launches;
+  s.check_launches = st.check_launches;
+  s.fim_slots = st.fim_slots;
+  s.fim_halo = st.fim_halo;
+  s.fim_owned = st.fim_owned;
+  s.h2d_bytes = st.h2d_bytes;
+  if (h->opt.verbose) {
+    std::printf("Eikonal GB300: %d blocks, %d iterations, %.3f ms solve, %.3f ms setup\n", h->nb, st.iterations,
+                st.solve_ms, s.setup_ms);
+  }
+  return EIK_OK;
+}
+
+int eik_prepare(eik_solver* h) {
+  if (!h) return EIK_ERR_ARG;
+  if (h->nv == 0) return fail(h, EIK_ERR_STATE, "no mesh: call eik_set_mesh or eik_load_mesh first");
+  bool nl = false;
+  return host_prepare(h, &nl);
+}
+
+int eik_num_vertices(const eik_solver* h) { return h ? h->nv : 0; }
+
+int eik_num_iterations(const eik_solver* h) { return (h && h->solved) ? h->stats.iterations : 0; }
+
+int eik_get_result(const eik_solver* h, float* out, int nv) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h || !out) return fail(m, EIK_ERR_ARG, "null argument");
+  if (!h->solved) return fail(m, EIK_ERR_STATE, "no solve has completed");
+  if (nv != h->nv) return fail(m, EIK_ERR_ARG, "output size mismatch");
+  std::string e = h->dev->result(out);
+  return e.empty() ? EIK_OK : fail(m, EIK_ERR_CUDA, e);
+}
+
+int eik_get_result_device(const eik_solver* h, float* out_dev, int nv) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h || !out_dev) return fail(m, EIK_ERR_ARG, "null argument");
+  if (!h->solved) return fail(m, EIK_ERR_STATE, "no solve has completed");
+  if (nv != h->nv) return fail(m, EIK_ERR_ARG, "output size mismatch");
+  std::string e = h->dev->result_device(out_dev);
+  return e.empty() ? EIK_OK : fail(m, EIK_ERR_CUDA, e);
+}
+
+int eik_get_iteration(const eik_solver* h, int i, float* out, int nv) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h || !out) return fail(m, EIK_ERR_ARG, "null argument");
+  if (!h->solved) return fail(m, EIK_ERR_STATE, "no solve has completed");
+  if (nv != h->nv) return fail(m, EIK_ERR_ARG, "output size mismatch");
+  if (i < 0 || i >= h->stats.iterations) return fail(m, EIK_ERR_ARG, "iteration index out of range");
+  if (!h->opt.keep_history) return fail(m, EIK_ERR_STATE, "history was not kept (keep_history = 0)");
+  std::string e = h->dev->history(i, out);
+  return e.empty() ? EIK_OK : fail(m, EIK_ERR_CUDA, e);
+}
+
+int eik_get_partition(const eik_solver* h, int* labels, int nv, int* nblocks) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h) return EIK_ERR_ARG;
+  if (h->labels.empty()) return fail(m, EIK_ERR_STATE, "no partition yet");
+  if (nblocks) *nblocks = h->nb;
+  if (labels) {
+    if (nv != h->nv) return fail(m, EIK_ERR_ARG, "size mismatch");
+    std::memcpy(labels, h->labels.data(), sizeof(int) * nv);
+  }
+  return EIK_OK;
+}
+
+int eik_get_stats(const eik_solver* h, eik_stats* s) {
+  if (!h || !s) return EIK_ERR_ARG;
+  *s = h->stats;
+  return EIK_OK;
+}
+
+int eik_write_vtk(const eik_solver* h, const char* prefix, int all) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h || !prefix) return fail(m, EIK_ERR_ARG, "null argument");
+  if (!h->solved) return fail(m, EIK_ERR_STATE, "no solve has completed");
+  std::vector<float> vals(h->nv);
+  const std::vector<int>& el = (h->dim == 2) ? h->prep.faces : h->elems;
+  const int nit = h->stats.iterations;
+  std::vector<int> which;
+  if (all && h->opt.keep_history) for (int i = 0; i < nit; ++i) which.push_back(i);
+  else which.push_back(-1);
+  int j = 0;
+  for (int i : which) {
+    int rc = (i < 0) ? eik_get_result(h, vals.data(), h->nv) : eik_get_iteration(h, i, vals.data(), h->nv);
+    if (rc) return rc;
+    const std::string path = std::string(prefix) + std::to_string(j++) + ".vtk";
+    std::string e = write_vtk(path, h->dim, h->xyz, el, vals.data(), h->nv);
+    if (!e.empty()) return fail(m, EIK_ERR_IO, e);
+  }
+  return EIK_OK;
+}
+
+int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned char* obtuse, int* vf_off,
+                 int* vf_verts) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h) return EIK_ERR_ARG;
+  if (h->dim != 2 || h->prep_mesh != h->mesh_ver) return fail(m, EIK_ERR_STATE, "no triangle mesh set");
+  const TriPrep& P = h->prep;
+  if (nf) *nf = P.nf;
+  if (nvirt) *nvirt = (int)(P.vf_verts.size() / 3);
+  if (faces) std::memcpy(faces, P.faces.data(), sizeof(int) * P.faces.size());
+  if (obtuse) std::memcpy(obtuse, P.obtuse.data(), P.obtuse.size());
+  if (vf_off) std::memcpy(vf_off, P.vf_off.data(), sizeof(int) * P.vf_off.size());
+  if (vf_verts && !P.vf_verts.empty()) std::memcpy(vf_verts, P.vf_verts.data(), sizeof(int) * P.vf_verts.size());
+  return EIK_OK;
+}
+
+int eik_selftest_local_update(int which, const float* in, float* out, int n) {
+  if (which < 0 || which > 2 || n < 0 || (n > 0 && (!in || !out))) return EIK_ERR_ARG;
+  return selftest_device(which, in, out, n).empty() ? EIK_OK : EIK_ERR_CUDA;
+}
+
+void* eik_stream(const eik_solver* h) { return (h && h->dev) ? h->dev->stream() : nullptr; }
+
+const char* eik_last_error(const eik_solver* h) { return h ? h->err.c_str() : "null handle"; }
+
+const char* eik_version(void) { return "eikonal-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

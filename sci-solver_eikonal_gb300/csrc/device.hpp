@@ -1,0 +1,83 @@
+// device.hpp — the device-resident block-FIM solve (host side of the CUDA code).
+//
+// One DeviceSolve owns the device copy of a block layout (slots, metric terms,
+// local vertex ids, halos, block graph) and the per-solve state (vertex travel
+// times, block flags, active lists, control block).  A solve is one launch of a
+// CUDA graph whose conditional while-node runs the reference's outer iteration
+// (src/core3d/cuda/meshFIM3dEikonal.cu:411-542, src/core2d/cuda/meshFIM2d_eikonal.cu:683-816)
+// entirely on the device: block visits, commit, neighbour activation and list
+// compaction, with no host round trip per iteration.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "setup.hpp"
+
+namespace eikgb {
+
+struct SolveStats {
+  int iterations = 0;
+  long long vertex_updates = 0;  // owned vertices x sweeps over all block visits
+  long long block_visits = 0;    // sweep visits + check visits
+  long long fim_visits = 0;
+  long long check_visits = 0;
+  long long slot_visits = 0;     // element slots streamed over all visits
+  long long halo_visits = 0;     // halo vertices gathered over all visits
+  long long owned_visits = 0;    // owned vertices over all visits
+  float solve_ms = 0.0f;         // device time of the last solve
+  int error = 0;                 // device-side error flags (0 = none)
+  long long fim_slots = 0, fim_halo = 0, fim_owned = 0;  // inputs of the sweep-kernel visits
+  float fim_kernel_ms = 0.0f;    // summed launch spans of the sweep kernel (device timer)
+  float check_kernel_ms = 0.0f;  // same for the neighbour-check kernel
+  int fim_launches = 0, check_launches = 0;
+  long long h2d_bytes = 0;       // host-to-device bytes the last solve copied (initial state)
+};
+
+struct SolveOptions {
+  int max_iterations = 100;  // reference default (src/Eikonal.cu:19)
+  int fim_sweeps = -1;       // -1: reference value (3D: 2, 2D: 7)
+  bool keep_history = false; // per-iteration snapshots (getResultAtIteration)
+  int history_cap = 0;       // snapshots kept when keep_history
+  int threads = 256;         // CTA size of the visit kernels
+};
+
+class DeviceSolve {
+ public:
+  DeviceSolve();
+  ~DeviceSolve();
+  DeviceSolve(const DeviceSolve&) = delete;
+  DeviceSolve& operator=(const DeviceSolve&) = delete;
+
+  // Upload (or re-upload) a layout.  Keeps the device arrays until the next call.
+  std::string upload(const Layout& L);
+  // Refresh only the per-slot coefficients (speed/metric change).
+  std::string upload_coef(const Layout& L);
+  // Seeds are original vertex ids.  init_vals (2D only, may be null) are the
+  // vertex values the reference's all-vertex convergence test starts from.
+  std::string set_seeds(const std::vector<int>& seeds_orig, const float* init_vals);
+  // Runs the solve to completion on the solver's stream.
+  std::string solve(const SolveOptions& opt);
+  // Final travel times in original vertex order.
+  std::string result(float* out_host) const;
+  std::string result_device(float* out_dev) const;  // device pointer, original order
+  std::string history(int i, float* out_host) const;
+  const SolveStats& stats() const { return stats_; }
+  const Layout* layout() const { return L_; }
+  void* stream() const { return stream_; }
+
+ private:
+  struct Impl;
+  Impl* p_;
+  const Layout* L_ = nullptr;
+  SolveStats stats_;
+  void* stream_ = nullptr;
+};
+
+// Runs the device local updates element-wise: which = 0 tet (9 inputs per case),
+// 1 triangle (7 inputs), 2 the two exact quotients (num, den -> small_quot,
+// root_quot).  Host arrays.
+std::string selftest_device(int which, const float* in, float* out, int n);
+
+}  // namespace eikgb

@@ -1,0 +1,1074 @@
+// fim_device.cu — GB300 (sm_103a) kernels and the device-resident outer loop of
+// the block-partitioned Fast Iterative Method.
+//
+// Reference mapping (paths inside SCI-Solver_Eikonal):
+//   k_visit3d<false>  FIMCuda           src/core3d/cuda/CUDA_kernels.cu:383-489   (2 sweeps)
+//   k_commit3d        CopyOutBack + host activation, meshFIM3dEikonal.cu:438-488, CUDA_kernels.cu:604-668
+//   k_visit3d<true>   run_check_neghbor CUDA_kernels.cu:493-602                    (1 sweep, flags only)
+//   k_visit2d<false>  FIMCuda           src/core2d/cuda/CUDA_kernels.cu:36-409    (7 sweeps)
+//   k_activate2d      host activation   src/core2d/cuda/meshFIM2d_eikonal.cu:734-756
+//   k_visit2d<true>   run_check_neighbor CUDA_kernels.cu:415-799                   (1 sweep, writes values)
+//   k_vertex_test2d   all-vertex convergence test, meshFIM2d_eikonal.cu:801-815
+//   run_reduction (both dims) is a __syncthreads_and inside the visit kernels.
+//
+// Design (GB300-first, not a translation):
+//   * One CTA visits one block at a time and pulls blocks from a device work
+//     counter; grids are sized by occupancy x 152 SMs and stay fixed so the whole
+//     iteration is a CUDA-graph body.  A conditional while-node repeats the body
+//     until no block is active: no host round trip per iteration.
+//   * A block's metric terms and corner ids are contiguous in HBM (block-major
+//     slots, SoA coefficient runs, 16-byte aligned) and arrive in shared memory by
+//     two cp.async.bulk copies completing on an mbarrier, while the threads gather
+//     owned and halo travel times.
+//   * Travel times live once per vertex in HBM (block-contiguous renumbering).
+//     Owned vertices keep one shared-memory copy per visit; every slot corner that
+//     belongs to another block keeps its own per-slot copy, as the reference's
+//     per-slot storage does, and the per-vertex minimum is a shared-memory atomic.
+//   * Sweeps after the first recompute a slot only when one of its values changed
+//     in the previous sweep; unchanged inputs reproduce the previous candidates
+//     bit for bit, so skipping them cannot change any result.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "device.hpp"
+#include "local_update.cuh"
+
+namespace eikgb {
+namespace {
+
+// ---------------------------------------------------------------------------
+// device control block
+// ---------------------------------------------------------------------------
+struct Ctl {
+  int iter;       // completed outer iterations
+  int max_iters;
+  int nact;       // active blocks this iteration
+  int nnew;       // newly activated blocks this iteration
+  int nnext;      // active list being built for the next iteration
+  int work_a, work_b, work_c, work_d;
+  int done_c, done_d;
+  int conv_fail;  // 2D: a vertex failed the all-vertex test this iteration
+  int error;
+  int pad_;
+  unsigned long long updates, fim_visits, chk_visits, slot_visits, halo_visits, owned_visits;
+  unsigned long long fim_slots, fim_halo, fim_owned;  // per-visit inputs of the sweep kernel only
+};
+
+enum : int { kErrWait = 1, kErrSmem = 2 };
+
+struct DevArgs {
+  const BlockDesc* blocks;
+  const float* coef;
+  const uint2* lv;
+  const int* halo;
+  const int* nbr_off;
+  const int* nbr;
+  const int* vblock;   // renumbered vertex -> block
+  int nb, nv;
+  float* Ta;           // 3D: committed times; 2D: main buffer
+  float* Tb;           // 3D: visit outputs;   2D: out buffer
+  const float* Tinit;  // 2D: value of never-refreshed copies
+  float* prev;         // 2D: all-vertex test
+  int* conv;
+  int* stampA;         // 3D: block unconverged this iteration; 2D: block in active list
+  int* stampC;         // block already queued for a check this iteration
+  unsigned char* visited;
+  int* list0;
+  int* list1;
+  int* list_new;
+  Ctl* ctl;
+  float* hist;
+  int hist_cap;
+  unsigned long long* ktime;  // per iteration: [fim start, fim end, check start, check end] (globaltimer ns)
+  int ktime_cap;
+  int fim_sweeps;
+  int max_slots_pad, max_local, max_owned;
+  cudaGraphConditionalHandle cond;
+};
+
+constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
+constexpr float kEps2D = 1e-5f;
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier + 1D bulk copy (TMA engine)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait (a few seconds at most); false means the copy never completed.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  for (int i = 0; i < (1 << 24); ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (i > 16) __nanosleep(256);
+  }
+  return false;
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// launch span of a visit kernel: earliest CTA start, latest CTA end
+__device__ __forceinline__ void stamp_start(const DevArgs& a, int iter, int which) {
+  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap) atomicMin(&a.ktime[4 * iter + 2 * which], global_ns());
+}
+__device__ __forceinline__ void stamp_end(const DevArgs& a, int iter, int which) {
+  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap) atomicMax(&a.ktime[4 * iter + 2 * which + 1], global_ns());
+}
+
+// order-preserving float <-> int keys for shared-memory atomicMin
+__device__ __forceinline__ int fkey(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : (i ^ 0x7fffffff);
+}
+__device__ __forceinline__ float fval(int k) { return __int_as_float(k >= 0 ? k : (k ^ 0x7fffffff)); }
+
+__device__ __forceinline__ int* act_list(const DevArgs& a, int iter) { return (iter & 1) ? a.list1 : a.list0; }
+__device__ __forceinline__ int* next_list(const DevArgs& a, int iter) { return (iter & 1) ? a.list0 : a.list1; }
+
+// shared-memory carve shared by the 2D and 3D visit kernels
+struct Smem {
+  float* coef;          // ncoef runs of max_slots_pad
+  uint2* lv;            // max_slots_pad
+  float* h0;            // 4 * max_slots_pad per-slot copies (current)
+  float* h1;            // next
+  unsigned char* m0;    // per-slot changed-corner masks (current)
+  unsigned char* m1;
+  float* vt;            // max_local: owned values then halo values
+  int* vnew;            // max_owned keys
+  unsigned char* vchg;  // max_owned
+};
+
+__device__ __forceinline__ Smem carve(unsigned char* sm, const DevArgs& a, int ncoef) {
+  Smem s;
+  const int np = a.max_slots_pad;
+  s.coef = reinterpret_cast<float*>(sm);
+  s.lv = reinterpret_cast<uint2*>(s.coef + (size_t)ncoef * np);
+  s.h0 = reinterpret_cast<float*>(s.lv + np);
+  s.h1 = s.h0 + 4 * (size_t)np;
+  s.m0 = reinterpret_cast<unsigned char*>(s.h1 + 4 * (size_t)np);
+  s.m1 = s.m0 + np;
+  s.vt = reinterpret_cast<float*>(s.m1 + np);
+  s.vnew = reinterpret_cast<int*>(s.vt + a.max_local);
+  s.vchg = reinterpret_cast<unsigned char*>(s.vnew + a.max_owned);
+  return s;
+}
+
+size_t smem_bytes(int ncoef, int max_slots_pad, int max_local, int max_owned) {
+  size_t n = (size_t)ncoef * max_slots_pad * 4 + (size_t)max_slots_pad * 8 + 2 * 16 * (size_t)max_slots_pad +
+             2 * (size_t)max_slots_pad + 4 * (size_t)max_local + 4 * (size_t)max_owned + (size_t)max_owned;
+  return (n + 15) & ~(size_t)15;
+}
+
+// Issue the two bulk copies of block `bd` (coefficients + corner ids) and gather
+// the owned / halo travel times from `Tsrc`.  Returns false on a copy timeout.
+__device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd, int ncoef, const Smem& s,
+                                           unsigned long long* bar, unsigned& parity, const float* Tsrc) {
+  const int tid = threadIdx.x, NT = blockDim.x;
+  if (tid == 0) {
+    fence_proxy_async();
+    const unsigned bc = 4u * ncoef * bd.nslots_pad, bl = 8u * bd.nslots_pad;
+    if (bc + bl > 0) {
+      mbar_expect_tx(bar, bc + bl);
+      bulk_g2s(s.coef, a.coef + (size_t)ncoef * bd.slot_begin, bc, bar);
+      bulk_g2s(s.lv, a.lv + bd.slot_begin, bl, bar);
+    } else {
+      mbar_expect_tx(bar, 0);
+    }
+  }
+  for (int k = tid; k < bd.nowned; k += NT) {
+    const float v = Tsrc[bd.vbase + k];
+    s.vt[k] = v;
+    s.vnew[k] = fkey(v);
+  }
+  for (int k = tid; k < bd.nhalo; k += NT) s.vt[bd.nowned + k] = Tsrc[a.halo[bd.halo_begin + k]];
+  const bool ok = mbar_wait(bar, parity);
+  parity ^= 1u;
+  return ok;
+}
+
+// ===========================================================================
+// 3D visit: kCheck = false -> FIMCuda (fim_sweeps sweeps, writes visit outputs);
+//           kCheck = true  -> run_check_neghbor (1 sweep, flags only)
+// ===========================================================================
+template <bool kCheck>
+__global__ void __launch_bounds__(256) k_visit3d(DevArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int s_item;
+  const Smem s0 = carve(sm, a, 6);
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const Ctl* ctl = a.ctl;
+  const int iter = ctl->iter;
+  const int stamp = iter + 1;
+  const int count = kCheck ? ctl->nnew : ctl->nact;
+  const int* list = kCheck ? a.list_new : act_list(a, iter);
+  int* nxt = next_list(a, iter);
+  const int nsweeps = kCheck ? 1 : a.fim_sweeps;
+  stamp_start(a, iter, kCheck ? 1 : 0);
+  if (tid == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  unsigned parity = 0;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(kCheck ? &a.ctl->work_c : &a.ctl->work_a, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= count) break;
+    const int b = list[item];
+    const BlockDesc bd = a.blocks[b];
+    Smem s = s0;
+    const bool ok = load_block(a, bd, 6, s, &bar, parity, a.Ta);
+    if (!ok) {
+      if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
+      (void)mbar_wait(&bar, parity ^ 1u);
+      __syncthreads();
+      continue;
+    }
+    __syncthreads();
+    const int ns = bd.nslots, np = bd.nslots_pad, nown = bd.nowned;
+    // per-slot copies of corners owned by other blocks start from the halo values
+    for (int j = bd.ninside + tid; j < ns; j += NT) {
+      const uint2 l = s.lv[j];
+      const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s.h0[4 * j + k] = (id[k] < nown) ? 0.0f : s.vt[id[k]];
+      s.m0[j] = 0;
+    }
+    __syncthreads();
+    int myconv = 1;
+    for (int sw = 0; sw < nsweeps; ++sw) {
+      for (int j = tid; j < ns; j += NT) {
+        const uint2 l = s.lv[j];
+        const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+        bool own[4];
+        float T[4];
+        unsigned ch = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          own[k] = id[k] < nown;
+          T[k] = own[k] ? s.vt[id[k]] : s.h0[4 * j + k];
+          const unsigned c = own[k] ? (unsigned)s.vchg[id[k]] : ((unsigned)s.m0[j] >> k) & 1u;
+          ch |= c << k;
+        }
+        if (sw == 0) ch = 0xfu;
+        const float ACBC = s.coef[0 * np + j], BCCD = s.coef[1 * np + j], ACCD = s.coef[2 * np + j];
+        const float ADBD = s.coef[3 * np + j], ACAD = s.coef[4 * np + j], BCBD = s.coef[5 * np + j];
+        // remaining metric edge products (CUDA_kernels.cu:429-437)
+        const float ADBC = ACBC + BCCD;
+        const float ACBD = ACBC + ACCD;
+        const float CDBD = ADBD - ACBD;
+        const float ADCD = ADBD - ADBC;
+        const float CDCD = ADCD - ACCD;
+        const float ADAD = ADCD + ACAD;
+        const float ACAC = ACAD - ACCD;
+        const float BDBD = BCBD + CDBD;
+        const float BCBC = BCBD - BCCD;
+        float nw[4] = {T[0], T[1], T[2], T[3]};
+        // The four apex updates run together, in the reference's order and with its
+        // argument expressions, so the compiler forms the same fused multiply-adds
+        // as in FIMCuda.  A slot whose four values did not change in the previous
+        // sweep would reproduce its previous candidates exactly and is skipped.
+        if (ch) {
+          const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
+          nw[3] = fminf(TD, tet_update(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD));
+          nw[0] = fminf(TA, tet_update(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC));
+          nw[1] = fminf(TB, tet_update(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC));
+          nw[2] = fminf(TC, tet_update(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD));
+        }
+        unsigned m = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (own[k]) {
+            if (nw[k] < T[k]) atomicMin(&s.vnew[id[k]], fkey(nw[k]));
+          } else {
+            s.h1[4 * j + k] = nw[k];
+            m |= (nw[k] != T[k] ? 1u : 0u) << k;
+          }
+        }
+        s.m1[j] = (unsigned char)m;
+      }
+      __syncthreads();
+      const bool last = (sw == nsweeps - 1);
+      for (int k = tid; k < nown; k += NT) {
+        const float nv = fval(s.vnew[k]);
+        const float ov = s.vt[k];
+        if (last) {
+          float res = ov - nv;
+          if (!kCheck && res < 0.0f) res = -res;
+          myconv &= (res <= kEps3DLe) ? 1 : 0;
+        }
+        s.vchg[k] = (nv != ov) ? 1 : 0;
+        s.vt[k] = nv;
+      }
+      float* th = s.h0; s.h0 = s.h1; s.h1 = th;
+      unsigned char* tm = s.m0; s.m0 = s.m1; s.m1 = tm;
+      __syncthreads();
+    }
+    const int allc = __syncthreads_and(myconv);
+    if (!kCheck)
+      for (int k = tid; k < nown; k += NT) a.Tb[bd.vbase + k] = s.vt[k];
+    if (tid == 0) {
+      if (!kCheck) {
+        a.conv[b] = allc;
+        if (!allc) a.stampA[b] = stamp;
+        atomicAdd(&a.ctl->fim_visits, 1ull);
+      } else {
+        if (!allc) nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+        atomicAdd(&a.ctl->chk_visits, 1ull);
+      }
+      atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
+      atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
+      atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
+      atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+      if (!kCheck) {
+        atomicAdd(&a.ctl->fim_slots, (unsigned long long)ns);
+        atomicAdd(&a.ctl->fim_halo, (unsigned long long)bd.nhalo);
+        atomicAdd(&a.ctl->fim_owned, (unsigned long long)nown);
+      }
+    }
+    __syncthreads();
+  }
+  stamp_end(a, iter, kCheck ? 1 : 0);
+}
+
+// ===========================================================================
+// 2D visit: kCheck = false -> FIMCuda (reads main, writes out, fim_sweeps sweeps)
+//           kCheck = true  -> run_check_neighbor (reads out, writes main, 1 sweep)
+// Corner ids carry bit 15 when the reference never refreshes that slot copy.
+// ===========================================================================
+template <bool kCheck>
+__global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int s_item;
+  const Smem s0 = carve(sm, a, 4);
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const Ctl* ctl = a.ctl;
+  const int iter = ctl->iter;
+  const int stamp = iter + 1;
+  const int nact = ctl->nact;
+  const int count = kCheck ? nact + ctl->nnew : nact;
+  const int* act = act_list(a, iter);
+  int* nxt = next_list(a, iter);
+  const int nsweeps = kCheck ? 1 : a.fim_sweeps;
+  const float* Tsrc = kCheck ? a.Tb : a.Ta;
+  float* Tdst = kCheck ? a.Ta : a.Tb;
+  stamp_start(a, iter, kCheck ? 1 : 0);
+  if (tid == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  unsigned parity = 0;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(kCheck ? &a.ctl->work_c : &a.ctl->work_a, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= count) break;
+    const int b = (item < nact) ? act[item] : a.list_new[item - nact];
+    const BlockDesc bd = a.blocks[b];
+    Smem s = s0;
+    const bool ok = load_block(a, bd, 4, s, &bar, parity, Tsrc);
+    if (!ok) {
+      if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
+      (void)mbar_wait(&bar, parity ^ 1u);
+      __syncthreads();
+      continue;
+    }
+    __syncthreads();
+    const int ns = bd.nslots, np = bd.nslots_pad, nown = bd.nowned;
+    for (int j = tid; j < ns; j += NT) {
+      const uint2 l = s.lv[j];
+      const int raw[3] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu)};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int id = raw[k] & 0x7fff;
+        float v = 0.0f;
+        if (raw[k] & 0x8000) {
+          const int g = (id < nown) ? bd.vbase + id : a.halo[bd.halo_begin + id - nown];
+          v = a.Tinit[g];
+        } else if (id >= nown) {
+          v = s.vt[id];
+        }
+        s.h0[4 * j + k] = v;
+      }
+      s.m0[j] = 0;
+    }
+    __syncthreads();
+    int myconv = 1;
+    for (int sw = 0; sw < nsweeps; ++sw) {
+      for (int j = tid; j < ns; j += NT) {
+        const uint2 l = s.lv[j];
+        const int raw[3] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu)};
+        int id[3];
+        bool live[3];
+        float T[3];
+        unsigned ch = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          id[k] = raw[k] & 0x7fff;
+          live[k] = !(raw[k] & 0x8000) && id[k] < nown;  // owned copy refreshed by reconciliation
+          T[k] = live[k] ? s.vt[id[k]] : s.h0[4 * j + k];
+          const unsigned c = live[k] ? (unsigned)s.vchg[id[k]] : ((unsigned)s.m0[j] >> k) & 1u;
+          ch |= c << k;
+        }
+        if (sw == 0) ch = 0x7u;
+        float nw[3] = {T[0], T[1], T[2]};
+        // all three corners together, as the reference's unrolled update does; a
+        // slot with no changed value since the previous sweep is skipped
+        if (!(T[0] >= kLarge2DDev && T[1] >= kLarge2DDev && T[2] >= kLarge2DDev) &&
+            (ch || T[0] != T[0] || T[1] != T[1] || T[2] != T[2])) {
+          const float e0 = s.coef[0 * np + j], e1 = s.coef[1 * np + j], e2 = s.coef[2 * np + j];
+          const float F = s.coef[3 * np + j];
+          // corner 0 from (v1, v2); corner 1 from (v2, v0); corner 2 from (v0, v1)
+          nw[0] = tri_update(T[1], T[2], T[0], e1, e2, e0, F);
+          nw[1] = tri_update(T[2], T[0], T[1], e2, e0, e1, F);
+          nw[2] = tri_update(T[0], T[1], T[2], e0, e1, e2, F);
+        }
+        unsigned m = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (live[k]) {
+            if (nw[k] < T[k]) atomicMin(&s.vnew[id[k]], fkey(nw[k]));
+          } else {
+            s.h1[4 * j + k] = nw[k];
+            m |= (nw[k] != T[k] ? 1u : 0u) << k;
+          }
+        }
+        s.m1[j] = (unsigned char)m;
+      }
+      __syncthreads();
+      const bool last = (sw == nsweeps - 1);
+      for (int k = tid; k < nown; k += NT) {
+        const float nv = fval(s.vnew[k]);
+        const float ov = s.vt[k];
+        if (last && k < kReduceCap2D) {
+          if (kCheck) {
+            myconv &= ((ov - nv) < kEps2D) ? 1 : 0;
+          } else {
+            float res = ov - nv;
+            if (res < 0.0f) res = -res;
+            myconv &= (res <= kEps2D) ? 1 : 0;
+          }
+        }
+        s.vchg[k] = (nv != ov) ? 1 : 0;
+        s.vt[k] = nv;
+      }
+      float* th = s.h0; s.h0 = s.h1; s.h1 = th;
+      unsigned char* tm = s.m0; s.m0 = s.m1; s.m1 = tm;
+      __syncthreads();
+    }
+    const int allc = __syncthreads_and(myconv);
+    for (int k = tid; k < nown; k += NT) Tdst[bd.vbase + k] = s.vt[k];
+    if (tid == 0) {
+      if (!kCheck) {
+        a.conv[b] = allc;
+        atomicAdd(&a.ctl->fim_visits, 1ull);
+      } else {
+        if (!allc) {
+          nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+          a.stampA[b] = stamp + 1;  // member of the next iteration's active list
+        }
+        atomicAdd(&a.ctl->chk_visits, 1ull);
+      }
+      atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
+      atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
+      atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
+      atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+      if (!kCheck) {
+        atomicAdd(&a.ctl->fim_slots, (unsigned long long)ns);
+        atomicAdd(&a.ctl->fim_halo, (unsigned long long)bd.nhalo);
+        atomicAdd(&a.ctl->fim_owned, (unsigned long long)nown);
+      }
+    }
+    __syncthreads();
+  }
+  stamp_end(a, iter, kCheck ? 1 : 0);
+}
+
+// ===========================================================================
+// 3D: commit visit outputs (CopyOutBack), mark visited blocks, queue the
+// neighbours of converged blocks for a check and carry unconverged blocks over.
+// One warp per active block.
+// ===========================================================================
+__global__ void k_commit3d(DevArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int iter = a.ctl->iter, stamp = iter + 1;
+  const int count = a.ctl->nact;
+  const int* act = act_list(a, iter);
+  int* nxt = next_list(a, iter);
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(&a.ctl->work_b, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= count) break;
+    const int b = act[item];
+    const BlockDesc bd = a.blocks[b];
+    for (int k = lane; k < bd.nowned; k += 32) a.Ta[bd.vbase + k] = a.Tb[bd.vbase + k];
+    if (lane == 0) a.visited[b] = 1;
+    if (a.conv[b]) {
+      for (int e = a.nbr_off[b] + lane; e < a.nbr_off[b + 1]; e += 32) {
+        const int nb = a.nbr[e];
+        if (a.stampA[nb] != stamp && atomicExch(&a.stampC[nb], stamp) != stamp)
+          a.list_new[atomicAdd(&a.ctl->nnew, 1)] = nb;
+      }
+    } else if (lane == 0) {
+      nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+    }
+  }
+}
+
+// 2D: queue the neighbours of converged active blocks that are not active.
+__global__ void k_activate2d(DevArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int iter = a.ctl->iter, stamp = iter + 1;
+  const int count = a.ctl->nact;
+  const int* act = act_list(a, iter);
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(&a.ctl->work_b, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= count) break;
+    const int b = act[item];
+    if (!a.conv[b]) continue;
+    for (int e = a.nbr_off[b] + lane; e < a.nbr_off[b + 1]; e += 32) {
+      const int nb = a.nbr[e];
+      if (a.stampA[nb] != stamp && atomicExch(&a.stampC[nb], stamp) != stamp)
+        a.list_new[atomicAdd(&a.ctl->nnew, 1)] = nb;
+    }
+  }
+}
+
+// End of an outer iteration (run by the last CTA of the iteration's last kernel).
+__device__ void finish_iteration(const DevArgs& a, bool all_vertices_converged) {
+  Ctl* c = a.ctl;
+  c->iter += 1;
+  c->nact = c->nnext;
+  c->nnext = 0;
+  c->nnew = 0;
+  c->work_a = c->work_b = c->work_c = c->work_d = 0;
+  c->done_c = c->done_d = 0;
+  c->conv_fail = 0;
+  const bool go = c->nact > 0 && c->iter < c->max_iters && !all_vertices_converged && c->error == 0;
+  cudaGraphSetConditional(a.cond, go ? 1u : 0u);
+}
+
+// last-CTA detection without any waiting: every CTA bumps the counter once
+__device__ __forceinline__ bool last_cta(int* counter) {
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = (atomicAdd(counter, 1) == (int)gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last != 0;
+}
+
+// 2D all-vertex convergence test (meshFIM2d_eikonal.cu:804-815) + iteration close
+__global__ void k_vertex_test2d(DevArgs a) {
+  int fail = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x) {
+    const float cur = a.Ta[v];
+    float diff = a.prev[v] - cur;
+    if (diff < 0.0f) diff = -diff;
+    const bool ok = (diff <= kEps2D) && (cur < kLarge2DDev);
+    fail |= ok ? 0 : 1;
+    a.prev[v] = cur;
+  }
+  fail = __syncthreads_or(fail);
+  if (threadIdx.x == 0 && fail) atomicOr(&a.ctl->conv_fail, 1);
+  if (last_cta(&a.ctl->done_d)) {
+    if (threadIdx.x == 0) {
+      const bool allc = (atomicAdd(&a.ctl->conv_fail, 0) == 0);
+      finish_iteration(a, allc);
+    }
+  }
+}
+
+// 3D close: a tiny single-CTA kernel after the check visits.
+__global__ void k_close3d(DevArgs a) {
+  if (threadIdx.x == 0) finish_iteration(a, false);
+}
+
+// start of a solve: set the while-condition from the initial active list
+__global__ void k_start(DevArgs a) {
+  if (threadIdx.x == 0) {
+    const Ctl* c = a.ctl;
+    cudaGraphSetConditional(a.cond, (c->nact > 0 && c->max_iters > 0) ? 1u : 0u);
+  }
+}
+
+// per-iteration snapshot in renumbered order (iteration index = iter - 1)
+__global__ void k_snapshot(DevArgs a, int dim) {
+  const int slot = a.ctl->iter - 1;
+  if (slot < 0 || slot >= a.hist_cap) return;
+  float* dst = a.hist + (size_t)slot * a.nv;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x)
+    dst[v] = (dim == 3) ? (a.visited[a.vblock[v]] ? a.Ta[v] : 0.0f) : a.Ta[v];
+}
+
+// final values to original vertex order
+__global__ void k_gather_result(const float* Ta, const unsigned char* visited, const int* vblock, const int* perm,
+                                int nv, int dim, float* out) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    const int r = perm[v];
+    out[v] = (dim == 3) ? (visited[vblock[r]] ? Ta[r] : 0.0f) : Ta[r];
+  }
+}
+__global__ void k_gather_hist(const float* h, const int* perm, int nv, float* out) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) out[v] = h[perm[v]];
+}
+
+// element-wise evaluation of the device local updates (self-test entry points)
+__global__ void k_selftest_tet(const float* in, float* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float* a = in + 9 * (size_t)i;
+    out[i] = tet_update(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
+  }
+}
+__global__ void k_selftest_tri(const float* in, float* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float* a = in + 7 * (size_t)i;
+    out[i] = tri_update(a[0], a[1], a[2], a[3], a[4], a[5], a[6]);
+  }
+}
+__global__ void k_selftest_quot(const float* in, float* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    out[2 * i] = small_quot(in[2 * i], in[2 * i + 1]);
+    out[2 * i + 1] = root_quot(in[2 * i], in[2 * i + 1]);
+  }
+}
+
+#define CK(x)                                                                           \
+  do {                                                                                  \
+    cudaError_t e_ = (x);                                                               \
+    if (e_ != cudaSuccess) return std::string(#x ": ") + cudaGetErrorString(e_);       \
+  } while (0)
+
+template <typename T>
+std::string dev_alloc(T*& p, size_t n) {
+  if (p) { cudaFree(p); p = nullptr; }
+  if (n == 0) n = 1;
+  CK(cudaMalloc((void**)&p, n * sizeof(T)));
+  return "";
+}
+
+}  // namespace
+
+// ===========================================================================
+// host side
+// ===========================================================================
+struct DeviceSolve::Impl {
+  int dim = 3, nv = 0, nb = 0;
+  BlockDesc* blocks = nullptr;
+  float* coef = nullptr;
+  uint2* lv = nullptr;
+  int* halo = nullptr;
+  int* nbr_off = nullptr;
+  int* nbr = nullptr;
+  int* vblock = nullptr;
+  int* perm = nullptr;
+  float* Ta = nullptr;
+  float* Tb = nullptr;
+  float* Tinit = nullptr;
+  float* prev = nullptr;
+  int* conv = nullptr;
+  int* stampA = nullptr;
+  int* stampC = nullptr;
+  unsigned char* visited = nullptr;
+  int* list0 = nullptr;
+  int* list1 = nullptr;
+  int* list_new = nullptr;
+  Ctl* ctl = nullptr;
+  float* hist = nullptr;
+  int hist_cap = 0;
+  unsigned long long* ktime = nullptr;
+  int ktime_cap = 0;
+  float* out_tmp = nullptr;
+  size_t coef_n = 0;
+  // host staging for the initial state
+  std::vector<float> h_init, h_prev;
+  std::vector<int> h_stampA, h_act, h_vblock;
+  std::vector<unsigned long long> h_ktime;
+  // graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  DevArgs args{};
+  int g_sweeps = -1, g_threads = -1;
+  bool g_hist = false;
+  int g_histcap = -1;
+  size_t smem = 0;
+  int grid_visit = 0, grid_aux = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int max_slots_pad = 0, max_local = 0, max_owned = 0;
+
+  void free_all() {
+    void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
+                  stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp};
+    for (void* p : ps)
+      if (p) cudaFree(p);
+    blocks = nullptr; coef = nullptr; lv = nullptr; halo = nullptr; nbr_off = nullptr; nbr = nullptr;
+    vblock = nullptr; perm = nullptr; Ta = nullptr; Tb = nullptr; Tinit = nullptr; prev = nullptr;
+    conv = nullptr; stampA = nullptr; stampC = nullptr; visited = nullptr; list0 = nullptr;
+    list1 = nullptr; list_new = nullptr; ctl = nullptr; hist = nullptr; ktime = nullptr; out_tmp = nullptr;
+    hist_cap = 0;
+    ktime_cap = 0;
+    drop_graph();
+  }
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    g_sweeps = g_threads = g_histcap = -1;
+  }
+};
+
+DeviceSolve::DeviceSolve() : p_(new Impl) {
+  cudaStream_t s;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess) stream_ = s;
+  cudaEventCreate(&p_->ev0);
+  cudaEventCreate(&p_->ev1);
+}
+
+DeviceSolve::~DeviceSolve() {
+  p_->free_all();
+  if (p_->ev0) cudaEventDestroy(p_->ev0);
+  if (p_->ev1) cudaEventDestroy(p_->ev1);
+  if (stream_) cudaStreamDestroy((cudaStream_t)stream_);
+  delete p_;
+}
+
+std::string DeviceSolve::upload(const Layout& L) {
+  Impl& P = *p_;
+  if (!stream_) return "CUDA stream creation failed (no usable GPU?)";
+  P.free_all();
+  L_ = &L;
+  P.dim = L.dim;
+  P.nv = L.nv;
+  P.nb = L.nb;
+  const int ncoef = (L.dim == 3) ? 6 : 4;
+  std::string e;
+  if (!(e = dev_alloc(P.blocks, L.nb)).empty()) return e;
+  if (!(e = dev_alloc(P.coef, L.coef.size())).empty()) return e;
+  if (!(e = dev_alloc(P.lv, (size_t)L.total_slots)).empty()) return e;
+  if (!(e = dev_alloc(P.halo, L.halo_ids.size())).empty()) return e;
+  if (!(e = dev_alloc(P.nbr_off, L.nbr_off.size())).empty()) return e;
+  if (!(e = dev_alloc(P.nbr, L.nbr.size())).empty()) return e;
+  if (!(e = dev_alloc(P.vblock, (size_t)L.nv)).empty()) return e;
+  if (!(e = dev_alloc(P.perm, (size_t)L.nv)).empty()) return e;
+  for (float** t : {&P.Ta, &P.Tb, &P.Tinit, &P.prev, &P.out_tmp})
+    if (!(e = dev_alloc(*t, (size_t)L.nv)).empty()) return e;
+  for (int** t : {&P.conv, &P.stampA, &P.stampC, &P.list0, &P.list1, &P.list_new})
+    if (!(e = dev_alloc(*t, (size_t)L.nb)).empty()) return e;
+  if (!(e = dev_alloc(P.visited, (size_t)L.nb)).empty()) return e;
+  if (!(e = dev_alloc(P.ctl, 1)).empty()) return e;
+  cudaStream_t st = (cudaStream_t)stream_;
+  CK(cudaMemcpyAsync(P.blocks, L.blocks.data(), sizeof(BlockDesc) * L.nb, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.lv, L.lv.data(), sizeof(uint16_t) * L.lv.size(), cudaMemcpyHostToDevice, st));
+  if (!L.halo_ids.empty())
+    CK(cudaMemcpyAsync(P.halo, L.halo_ids.data(), sizeof(int) * L.halo_ids.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.nbr_off, L.nbr_off.data(), sizeof(int) * L.nbr_off.size(), cudaMemcpyHostToDevice, st));
+  if (!L.nbr.empty())
+    CK(cudaMemcpyAsync(P.nbr, L.nbr.data(), sizeof(int) * L.nbr.size(), cudaMemcpyHostToDevice, st));
+  std::vector<int>& vb = P.h_vblock;
+  vb.assign(L.nv, 0);
+  for (int b = 0; b < L.nb; ++b)
+    for (int k = 0; k < L.blocks[b].nowned; ++k) vb[L.blocks[b].vbase + k] = b;
+  CK(cudaMemcpyAsync(P.vblock, vb.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.perm, L.perm.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  P.coef_n = L.coef.size();
+  P.max_slots_pad = (L.max_slots + 3) & ~3;
+  P.max_local = std::max(L.max_local, 1);
+  P.max_owned = std::max(L.max_owned, 1);
+  P.smem = smem_bytes(ncoef, P.max_slots_pad, P.max_local, P.max_owned);
+  int dev = 0, maxsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (P.smem + 64 > (size_t)maxsm)
+    return "block too large for shared memory (" + std::to_string(L.max_slots) +
+           " element slots); use fewer vertices per block";
+  return "";
+}
+
+std::string DeviceSolve::upload_coef(const Layout& L) {
+  Impl& P = *p_;
+  if (L.coef.size() != P.coef_n) return "coefficient size changed; upload the layout again";
+  CK(cudaMemcpyAsync(P.coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice,
+                     (cudaStream_t)stream_));
+  CK(cudaStreamSynchronize((cudaStream_t)stream_));
+  return "";
+}
+
+std::string DeviceSolve::set_seeds(const std::vector<int>& seeds, const float* init_vals) {
+  Impl& P = *p_;
+  if (!L_) return "no layout uploaded";
+  const Layout& L = *L_;
+  const float large = (L.dim == 3) ? kLarge3D : kLarge2D;
+  P.h_init.assign(L.nv, large);
+  std::vector<char> act(L.nb, 0);
+  for (int s : seeds) {
+    if (s < 0 || s >= L.nv) return "seed vertex out of range";
+    P.h_init[L.perm[s]] = 0.0f;
+    act[P.h_vblock[L.perm[s]]] = 1;
+  }
+  P.h_act.clear();
+  for (int b = 0; b < L.nb; ++b)
+    if (act[b]) P.h_act.push_back(b);
+  // the reference's TriMesh::vertT: user values, or 0 at seeds and LARGENUM elsewhere
+  P.h_prev.assign(L.nv, large);
+  if (init_vals) {
+    for (int v = 0; v < L.nv; ++v) P.h_prev[L.perm[v]] = init_vals[v];
+  } else {
+    for (int s : seeds) P.h_prev[L.perm[s]] = 0.0f;
+  }
+  P.h_stampA.assign(L.nb, 0);
+  if (L.dim == 2)
+    for (int b : P.h_act) P.h_stampA[b] = 1;
+  return "";
+}
+
+std::string DeviceSolve::solve(const SolveOptions& opt) {
+  Impl& P = *p_;
+  if (!L_) return "no layout uploaded";
+  const Layout& L = *L_;
+  cudaStream_t st = (cudaStream_t)stream_;
+  const int sweeps = (opt.fim_sweeps > 0) ? opt.fim_sweeps : (L.dim == 3 ? 2 : 7);
+  const int threads = (opt.threads == 128 || opt.threads == 256) ? opt.threads : 256;
+  const int hcap = opt.keep_history ? std::max(0, opt.history_cap) : 0;
+  if (hcap > 0 && hcap != P.hist_cap) {
+    if (P.hist) cudaFree(P.hist);
+    P.hist = nullptr;
+    CK(cudaMalloc((void**)&P.hist, sizeof(float) * (size_t)hcap * L.nv));
+    P.hist_cap = hcap;
+    P.drop_graph();
+  }
+  if (opt.max_iterations + 1 > P.ktime_cap) {
+    if (P.ktime) cudaFree(P.ktime);
+    P.ktime = nullptr;
+    P.ktime_cap = opt.max_iterations + 1;
+    CK(cudaMalloc((void**)&P.ktime, sizeof(unsigned long long) * 4 * (size_t)P.ktime_cap));
+    P.drop_graph();
+  }
+  {
+    // starts at +inf, ends at 0
+    std::vector<unsigned long long> kt(4 * (size_t)P.ktime_cap);
+    for (size_t i = 0; i < kt.size(); ++i) kt[i] = (i % 2 == 0) ? ~0ull : 0ull;
+    P.h_ktime.swap(kt);
+    CK(cudaMemcpyAsync(P.ktime, P.h_ktime.data(), sizeof(unsigned long long) * P.h_ktime.size(),
+                       cudaMemcpyHostToDevice, st));
+  }
+  // initial state
+  CK(cudaMemcpyAsync(P.Ta, P.h_init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.Tb, P.h_init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.Tinit, P.h_init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.prev, P.h_prev.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.stampA, P.h_stampA.data(), sizeof(int) * L.nb, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(P.stampC, 0, sizeof(int) * L.nb, st));
+  CK(cudaMemsetAsync(P.visited, 0, L.nb, st));
+  CK(cudaMemsetAsync(P.conv, 0, sizeof(int) * L.nb, st));
+  if (!P.h_act.empty())
+    CK(cudaMemcpyAsync(P.list0, P.h_act.data(), sizeof(int) * P.h_act.size(), cudaMemcpyHostToDevice, st));
+  stats_.h2d_bytes = (long long)sizeof(unsigned long long) * P.h_ktime.size() + 4ll * sizeof(float) * L.nv +
+                     (long long)sizeof(int) * L.nb + (long long)sizeof(int) * P.h_act.size() + (long long)sizeof(Ctl);
+  Ctl c{};
+  c.max_iters = opt.max_iterations;
+  c.nact = (int)P.h_act.size();
+  CK(cudaMemcpyAsync(P.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+
+  // (re)build the graph when the launch shape changes
+  const bool want_hist = hcap > 0;
+  if (!P.exec || P.g_sweeps != sweeps || P.g_threads != threads || P.g_hist != want_hist || P.g_histcap != hcap) {
+    P.drop_graph();
+    DevArgs& a = P.args;
+    a = DevArgs{};
+    a.blocks = P.blocks; a.coef = P.coef; a.lv = P.lv; a.halo = P.halo; a.nbr_off = P.nbr_off; a.nbr = P.nbr;
+    a.vblock = P.vblock; a.nb = L.nb; a.nv = L.nv; a.Ta = P.Ta; a.Tb = P.Tb; a.Tinit = P.Tinit; a.prev = P.prev;
+    a.conv = P.conv; a.stampA = P.stampA; a.stampC = P.stampC; a.visited = P.visited; a.list0 = P.list0;
+    a.list1 = P.list1; a.list_new = P.list_new; a.ctl = P.ctl; a.hist = P.hist; a.hist_cap = hcap;
+    a.ktime = P.ktime; a.ktime_cap = P.ktime_cap;
+    a.fim_sweeps = sweeps; a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local;
+    a.max_owned = P.max_owned;
+    CK(cudaGraphCreate(&P.graph, 0));
+    CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    void* kv_fim = (L.dim == 3) ? (void*)k_visit3d<false> : (void*)k_visit2d<false>;
+    void* kv_chk = (L.dim == 3) ? (void*)k_visit3d<true> : (void*)k_visit2d<true>;
+    for (void* k : {kv_fim, kv_chk})
+      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, threads, P.smem));
+    if (occ < 1) return "visit kernel cannot be resident (shared memory / registers)";
+    P.grid_visit = std::min(occ * nsm, std::max(L.nb, 1));
+    P.grid_aux = nsm * 4;
+    // start node
+    void* args_ptr[] = {&P.args};
+    cudaGraphNode_t n_start, n_while;
+    cudaKernelNodeParams kp{};
+    kp.func = (void*)k_start; kp.gridDim = dim3(1); kp.blockDim = dim3(32); kp.kernelParams = args_ptr;
+    CK(cudaGraphAddKernelNode(&n_start, P.graph, nullptr, 0, &kp));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = a.cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    CK(cudaGraphAddNode(&n_while, P.graph, &n_start, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaGraphNode_t prevn = nullptr, n;
+    auto add = [&](void* f, int grid, int block, size_t sm, void** params) -> std::string {
+      cudaKernelNodeParams q{};
+      q.func = f; q.gridDim = dim3(grid); q.blockDim = dim3(block); q.sharedMemBytes = (unsigned)sm;
+      q.kernelParams = params;
+      CK(cudaGraphAddKernelNode(&n, body, prevn ? &prevn : nullptr, prevn ? 1 : 0, &q));
+      prevn = n;
+      return "";
+    };
+    static int dim3v = 3, dim2v = 2;
+    void* snap_args[] = {&P.args, (L.dim == 3) ? (void*)&dim3v : (void*)&dim2v};
+    std::string e;
+    if (!(e = add(kv_fim, P.grid_visit, threads, P.smem, args_ptr)).empty()) return e;
+    if (L.dim == 3) {
+      if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, P.grid_visit, threads, P.smem, args_ptr)).empty()) return e;
+      if (!(e = add((void*)k_close3d, 1, 32, 0, args_ptr)).empty()) return e;
+    } else {
+      if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, P.grid_visit, threads, P.smem, args_ptr)).empty()) return e;
+      if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+    }
+    if (want_hist)
+      if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
+    CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
+    P.g_sweeps = sweeps;
+    P.g_threads = threads;
+    P.g_hist = want_hist;
+    P.g_histcap = hcap;
+  }
+  CK(cudaEventRecord(P.ev0, st));
+  CK(cudaGraphLaunch(P.exec, st));
+  CK(cudaEventRecord(P.ev1, st));
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  Ctl out{};
+  CK(cudaMemcpy(&out, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  cudaEventElapsedTime(&stats_.solve_ms, P.ev0, P.ev1);
+  stats_.iterations = out.iter;
+  stats_.vertex_updates = (long long)out.updates;
+  stats_.fim_visits = (long long)out.fim_visits;
+  stats_.check_visits = (long long)out.chk_visits;
+  stats_.block_visits = stats_.fim_visits + stats_.check_visits;
+  stats_.slot_visits = (long long)out.slot_visits;
+  stats_.halo_visits = (long long)out.halo_visits;
+  stats_.owned_visits = (long long)out.owned_visits;
+  stats_.error = out.error;
+  stats_.fim_slots = (long long)out.fim_slots;
+  stats_.fim_halo = (long long)out.fim_halo;
+  stats_.fim_owned = (long long)out.fim_owned;
+  {
+    std::vector<unsigned long long> kt(4 * (size_t)P.ktime_cap);
+    CK(cudaMemcpy(kt.data(), P.ktime, sizeof(unsigned long long) * kt.size(), cudaMemcpyDeviceToHost));
+    double fim = 0, chk = 0;
+    int nf = 0, nc = 0;
+    for (int i = 0; i < std::min(out.iter, P.ktime_cap); ++i) {
+      if (kt[4 * i + 1] > kt[4 * i] && kt[4 * i] != ~0ull) { fim += (double)(kt[4 * i + 1] - kt[4 * i]); ++nf; }
+      if (kt[4 * i + 3] > kt[4 * i + 2] && kt[4 * i + 2] != ~0ull) { chk += (double)(kt[4 * i + 3] - kt[4 * i + 2]); ++nc; }
+    }
+    stats_.fim_kernel_ms = (float)(fim * 1e-6);
+    stats_.check_kernel_ms = (float)(chk * 1e-6);
+    stats_.fim_launches = nf;
+    stats_.check_launches = nc;
+  }
+  if (out.error) return "device reported error flags " + std::to_string(out.error);
+  return "";
+}
+
+std::string DeviceSolve::result_device(float* out_dev) const {
+  const Impl& P = *p_;
+  if (!L_) return "no layout uploaded";
+  k_gather_result<<<std::max(1, std::min(1024, (P.nv + 255) / 256)), 256, 0, (cudaStream_t)stream_>>>(
+      P.Ta, P.visited, P.vblock, P.perm, P.nv, P.dim, out_dev);
+  CK(cudaGetLastError());
+  return "";
+}
+
+std::string DeviceSolve::result(float* out_host) const {
+  const Impl& P = *p_;
+  std::string e = result_device(P.out_tmp);
+  if (!e.empty()) return e;
+  CK(cudaMemcpyAsync(out_host, P.out_tmp, sizeof(float) * P.nv, cudaMemcpyDeviceToHost, (cudaStream_t)stream_));
+  CK(cudaStreamSynchronize((cudaStream_t)stream_));
+  return "";
+}
+
+std::string DeviceSolve::history(int i, float* out_host) const {
+  const Impl& P = *p_;
+  if (!P.hist || i < 0 || i >= P.hist_cap || i >= stats_.iterations) return "iteration not recorded";
+  k_gather_hist<<<std::max(1, std::min(1024, (P.nv + 255) / 256)), 256, 0, (cudaStream_t)stream_>>>(
+      P.hist + (size_t)i * P.nv, P.perm, P.nv, P.out_tmp);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out_host, P.out_tmp, sizeof(float) * P.nv, cudaMemcpyDeviceToHost, (cudaStream_t)stream_));
+  CK(cudaStreamSynchronize((cudaStream_t)stream_));
+  return "";
+}
+
+std::string selftest_device(int which, const float* in, float* out, int n) {
+  const int nin = (which == 0) ? 9 : (which == 1) ? 7 : 2;
+  const int nout = (which == 2) ? 2 : 1;
+  float *din = nullptr, *dout = nullptr;
+  CK(cudaMalloc((void**)&din, sizeof(float) * (size_t)nin * n + 16));
+  CK(cudaMalloc((void**)&dout, sizeof(float) * (size_t)nout * n + 16));
+  cudaMemcpy(din, in, sizeof(float) * (size_t)nin * n, cudaMemcpyHostToDevice);
+  const int grid = (n + 127) / 128;
+  if (n > 0) {
+    if (which == 0) k_selftest_tet<<<grid, 128>>>(din, dout, n);
+    else if (which == 1) k_selftest_tri<<<grid, 128>>>(din, dout, n);
+    else k_selftest_quot<<<grid, 128>>>(din, dout, n);
+  }
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(float) * (size_t)nout * n, cudaMemcpyDeviceToHost);
+  cudaFree(din);
+  cudaFree(dout);
+  if (e != cudaSuccess) return std::string("self-test kernel: ") + cudaGetErrorString(e);
+  return "";
+}
+
+}  // namespace eikgb
