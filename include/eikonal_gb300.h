@@ -149,7 +149,11 @@ int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned 
  *   which = 1: triangle update (core2d/cuda/CUDA_kernels.cu:143-204),
  *              7 inputs per case (TA TB TC LenAB LenBC LenAC speedInv), 1 output;
  *   which = 2: the FP32 forms of the reference's FP64 quotients, 2 inputs
- *              (num, h) -> 2 outputs (num/(h+1e-8), num/(2h)). */
+ *              (num, h) -> 2 outputs (num/(h+1e-8), num/(2h));
+ *   which = 3 / 4: each case is a triangle forming its own block (T0 T1 T2 LenAB
+ *              (v0v1) LenBC (v1v2) LenCA (v2v0) speedInv), passed once through the
+ *              2D block-sweep kernel (7 sweeps) / neighbour-check kernel (1 sweep);
+ *              3 outputs per case. */
 int eik_selftest_local_update(int which, const float* in, float* out, int n);
 
 /* The CUDA stream (cudaStream_t) the handle's solves and copies run on, or null

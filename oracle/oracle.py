@@ -25,7 +25,8 @@ def lib():
     if _lib is None:
         path = os.path.join(HERE, "liboracle.so")
         if not os.path.exists(path):
-            from . import build_oracle  # noqa: F401  (package-relative import when available)
+            from oracle import build_oracle
+            build_oracle.build()
         _lib = ctypes.CDLL(path)
         f = _lib.oracle_tet_update_f32
         f.restype = ctypes.c_float
@@ -158,6 +159,8 @@ def ref_gpu():
         g.refgpu_solve3d.restype = ctypes.c_int
         g.refgpu_solve3d.argtypes = [ctypes.c_char_p, ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _IP, ctypes.c_int,
                                      _IP, ctypes.c_int, ctypes.c_int, _FP, _FP, ctypes.c_int, _LP, _IP]
+        g.refgpu_tri_blocks.restype = ctypes.c_int
+        g.refgpu_tri_blocks.argtypes = [ctypes.c_char_p, _FP, ctypes.c_int, ctypes.c_int, _FP]
         g.refgpu_solve2d.restype = ctypes.c_int
         g.refgpu_solve2d.argtypes = [ctypes.c_char_p, ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _UP, _IP, _IP, _FP,
                                      _IP, ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_int, _FP, _FP, ctypes.c_int,
@@ -183,6 +186,16 @@ def ref_gpu_tet_local_solver(inputs9):
     out = np.empty(a.shape[0], dtype=np.float32)
     _gpu_check(ref_gpu().refgpu_tet_local_solver(CUBIN3D.encode(), a.ctypes.data_as(_FP), out.ctypes.data_as(_FP),
                                                  a.shape[0]))
+    return out
+
+
+def ref_gpu_tri_blocks(inputs7, check=False):
+    """Single-triangle blocks through the reference's 2D FIMCuda (7 sweeps) or
+    run_check_neighbor (1 sweep); inputs T0 T1 T2 e01 e12 e20 speedInv."""
+    a = _f(inputs7).reshape(-1, 7)
+    out = np.empty((a.shape[0], 3), dtype=np.float32)
+    _gpu_check(ref_gpu().refgpu_tri_blocks(CUBIN2D.encode(), a.ctypes.data_as(_FP), a.shape[0], int(bool(check)),
+                                           out.ctypes.data_as(_FP)))
     return out
 
 

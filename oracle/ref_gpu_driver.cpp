@@ -333,4 +333,58 @@ int refgpu_solve2d(const char* cubin2d, int nv, const float* xyz, int nf, const 
   return iters;
 }
 
+// Each case is one triangle forming its own block (3 owned vertices, 1 element
+// slot + 2 empty slots); one launch of the reference's 2D FIMCuda (7 sweeps, check
+// = 0) or run_check_neighbor (1 sweep, check = 1).  in: T0 T1 T2 e01 e12 e20
+// speedInv per case; out: the three vertex values the kernel writes back.
+int refgpu_tri_blocks(const char* cubin2d, const float* in, int n, int check, float* out) {
+  TRY(load(g_lib2, cubin2d));
+  cudaKernel_t kfim, kchk;
+  TRY(kernel(g_lib2, "ref2d_fim", &kfim));
+  TRY(kernel(g_lib2, "ref2d_check", &kchk));
+  const int maxF = 3, maxV = 3;
+  const size_t nslot = (size_t)n * maxF;
+  std::vector<float> tm(3 * nslot, (float)kLarge2D), e0(nslot, 1.f), e1(nslot, 1.f), e2(nslot, 1.f), sp(nslot, 1.f);
+  std::vector<int> vm((size_t)n * maxV * 6), vmo((size_t)n * maxV * 6, -1), bs(n, 3), al(n);
+  for (int b = 0; b < n; ++b) {
+    const float* c = in + 7 * (size_t)b;
+    const int base = b * maxF * 3;
+    for (int k = 0; k < 3; ++k) tm[base + k] = c[k];
+    e0[(size_t)b * maxF] = c[3];
+    e1[(size_t)b * maxF] = c[4];
+    e2[(size_t)b * maxF] = c[5];
+    sp[(size_t)b * maxF] = c[6];
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 6; ++j) vm[((size_t)b * maxV + k) * 6 + j] = (j == 0) ? base + k : -1 + base;
+    al[b] = b;
+  }
+  DBuf<float> d_tm, d_tmo, d_e0, d_e1, d_e2, d_sp;
+  DBuf<int> d_vm, d_vmo, d_bs, d_con, d_al;
+  TRY(d_tm.alloc(3 * nslot)); TRY(d_tmo.alloc(3 * nslot)); TRY(d_e0.alloc(nslot)); TRY(d_e1.alloc(nslot));
+  TRY(d_e2.alloc(nslot)); TRY(d_sp.alloc(nslot)); TRY(d_vm.alloc(vm.size())); TRY(d_vmo.alloc(vmo.size()));
+  TRY(d_bs.alloc(n)); TRY(d_con.alloc((size_t)n * 64)); TRY(d_al.alloc(n));
+  TRY(d_tm.put(tm.data(), tm.size())); TRY(d_tmo.put(tm.data(), tm.size())); TRY(d_e0.put(e0.data(), nslot));
+  TRY(d_e1.put(e1.data(), nslot)); TRY(d_e2.put(e2.data(), nslot)); TRY(d_sp.put(sp.data(), nslot));
+  TRY(d_vm.put(vm.data(), vm.size())); TRY(d_vmo.put(vmo.data(), vmo.size())); TRY(d_bs.put(bs.data(), n));
+  TRY(d_al.put(al.data(), n));
+  float* ptm = d_tm.p; float* ptmo = d_tmo.p; int* pvm = d_vm.p; int* pvmo = d_vmo.p; float* pe0 = d_e0.p;
+  float* pe1 = d_e1.p; float* pe2 = d_e2.p; float* psp = d_sp.p; int* pbs = d_bs.p; int* pcon = d_con.p;
+  int* pal = d_al.p;
+  int na = n, mF = maxF, mV = maxV, stopi = 50000;
+  float stopd = 50000.f;
+  const size_t smem = (size_t)maxF * 3 * 4 + (size_t)maxV * 6 * 2;
+  if (!check) {
+    void* a_fim[] = {&ptm, &ptmo, &pvm, &pvmo, &pe0, &pe1, &pe2, &psp, &pbs, &pcon, &pal, &na, &mF, &mV, &stopd};
+    TRY(launch(kfim, n, maxF, smem, a_fim));
+  } else {
+    void* a_chk[] = {&ptm, &ptmo, &pvm, &pvmo, &pe0, &pe1, &pe2, &psp, &pbs, &pcon, &pal, &na, &mF, &mV, &na, &stopi};
+    TRY(launch(kchk, n, maxF, smem, a_chk));
+  }
+  RCK(cudaDeviceSynchronize());
+  TRY(d_tmo.get(tm.data(), tm.size()));
+  for (int b = 0; b < n; ++b)
+    for (int k = 0; k < 3; ++k) out[3 * (size_t)b + k] = tm[(size_t)b * maxF * 3 + k];
+  return 0;
+}
+
 }  // extern "C"

@@ -430,7 +430,7 @@ int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned 
 }
 
 int eik_selftest_local_update(int which, const float* in, float* out, int n) {
-  if (which < 0 || which > 2 || n < 0 || (n > 0 && (!in || !out))) return EIK_ERR_ARG;
+  if (which < 0 || which > 4 || n < 0 || (n > 0 && (!in || !out))) return EIK_ERR_ARG;
   return selftest_device(which, in, out, n).empty() ? EIK_OK : EIK_ERR_CUDA;
 }
 

@@ -63,6 +63,9 @@ class DeviceSolve {
   std::string result(float* out_host) const;
   std::string result_device(float* out_dev) const;  // device pointer, original order
   std::string history(int i, float* out_host) const;
+  // One visit of every block with the 2D kernel on the given vertex values
+  // (renumbered order); sweep visit or neighbour check.  For self-tests.
+  std::string visit_once(bool check, const float* T_host, float* out_host);
   const SolveStats& stats() const { return stats_; }
   const Layout* layout() const { return L_; }
   void* stream() const { return stream_; }
@@ -77,7 +80,8 @@ class DeviceSolve {
 
 // Runs the device local updates element-wise: which = 0 tet (9 inputs per case),
 // 1 triangle (7 inputs), 2 the two exact quotients (num, den -> small_quot,
-// root_quot).  Host arrays.
+// root_quot); 3 / 4: single-triangle blocks through the 2D sweep / check kernel
+// (7 inputs -> 3 outputs).  Host arrays.
 std::string selftest_device(int which, const float* in, float* out, int n);
 
 }  // namespace eikgb

@@ -451,9 +451,9 @@ __global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
           const float e0 = s.coef[0 * np + j], e1 = s.coef[1 * np + j], e2 = s.coef[2 * np + j];
           const float F = s.coef[3 * np + j];
           // corner 0 from (v1, v2); corner 1 from (v2, v0); corner 2 from (v0, v1)
-          nw[0] = tri_update(T[1], T[2], T[0], e1, e2, e0, F);
-          nw[1] = tri_update(T[2], T[0], T[1], e2, e0, e1, F);
-          nw[2] = tri_update(T[0], T[1], T[2], e0, e1, e2, F);
+          nw[0] = tri_update<false>(T[1], T[2], T[0], e1, e2, e0, F, 0.f, 0.f);
+          nw[1] = tri_update<false>(T[2], T[0], T[1], e2, e0, e1, F, 0.f, 0.f);
+          nw[2] = tri_update<false>(T[0], T[1], T[2], e0, e1, e2, F, 0.f, 0.f);
         }
         unsigned m = 0;
 #pragma unroll
@@ -514,6 +514,176 @@ __global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
     __syncthreads();
   }
   stamp_end(a, iter, kCheck ? 1 : 0);
+}
+
+// ===========================================================================
+// 2D visit, one thread per element slot (blocks of up to 1024 slots).  Each
+// thread keeps its slot's edge lengths, inverse speed and the copies of corners
+// that belong to other blocks in registers across the sweeps, and the sweep loop
+// is unrolled at compile time, as in the reference's FIMCuda: the compiler then
+// forms the same fused multiply-adds and the results match it bit for bit.
+// kSweeps = 0 runs a runtime sweep count (fim_sweeps) instead.
+// ===========================================================================
+template <bool kCheck, int kSweeps>
+__global__ void __launch_bounds__(1024) k_visit2d_slot(DevArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int s_item;
+  const int np_max = a.max_slots_pad;
+  float* s_coef = reinterpret_cast<float*>(sm);
+  uint2* s_lv = reinterpret_cast<uint2*>(s_coef + 4 * (size_t)np_max);
+  float* s_vt = reinterpret_cast<float*>(s_lv + np_max);
+  int* s_vnew = reinterpret_cast<int*>(s_vt + a.max_local);
+  unsigned char* s_vchg = reinterpret_cast<unsigned char*>(s_vnew + a.max_owned);
+  Smem sv{};
+  sv.coef = s_coef;
+  sv.lv = s_lv;
+  sv.vt = s_vt;
+  sv.vnew = s_vnew;
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const Ctl* ctl = a.ctl;
+  const int iter = ctl->iter;
+  const int stamp = iter + 1;
+  const int nact = ctl->nact;
+  const int count = kCheck ? nact + ctl->nnew : nact;
+  const int* act = act_list(a, iter);
+  int* nxt = next_list(a, iter);
+  const int nsweeps = kSweeps > 0 ? kSweeps : (kCheck ? 1 : a.fim_sweeps);
+  const float* Tsrc = kCheck ? a.Tb : a.Ta;
+  float* Tdst = kCheck ? a.Ta : a.Tb;
+  stamp_start(a, iter, kCheck ? 1 : 0);
+  if (tid == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  unsigned parity = 0;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(kCheck ? &a.ctl->work_c : &a.ctl->work_a, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= count) break;
+    const int b = (item < nact) ? act[item] : a.list_new[item - nact];
+    const BlockDesc bd = a.blocks[b];
+    const bool ok = load_block(a, bd, 4, sv, &bar, parity, Tsrc);
+    if (!ok) {
+      if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
+      (void)mbar_wait(&bar, parity ^ 1u);
+      __syncthreads();
+      continue;
+    }
+    __syncthreads();
+    const int ns = bd.nslots, np = bd.nslots_pad, nown = bd.nowned;
+    const int j = tid;
+    const bool mine = j < ns;
+    int id[3] = {0, 0, 0};
+    bool live[3] = {true, true, true};
+    float h[3] = {0.f, 0.f, 0.f};
+    float e0 = 0.f, e1 = 0.f, e2 = 0.f, F = 0.f;
+    if (mine) {
+      const uint2 l = s_lv[j];
+      const int raw[3] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu)};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        id[k] = raw[k] & 0x7fff;
+        live[k] = !(raw[k] & 0x8000) && id[k] < nown;
+        if (raw[k] & 0x8000) {
+          const int g = (id[k] < nown) ? bd.vbase + id[k] : a.halo[bd.halo_begin + id[k] - nown];
+          h[k] = a.Tinit[g];
+        } else if (id[k] >= nown) {
+          h[k] = s_vt[id[k]];
+        }
+      }
+      e0 = s_coef[0 * np + j];
+      e1 = s_coef[1 * np + j];
+      e2 = s_coef[2 * np + j];
+      F = s_coef[3 * np + j];
+    }
+    // edge-candidate products, rounded once per visit (see tri_update)
+    const float eF0 = __fmul_rn(e0, F), eF1 = __fmul_rn(e1, F), eF2 = __fmul_rn(e2, F);
+    unsigned hchg = 0;
+    int myconv = 1;
+#pragma unroll
+    for (int sw = 0; sw < (kSweeps > 0 ? kSweeps : 1); ++sw) {
+      for (int rs = 0; rs < (kSweeps > 0 ? 1 : nsweeps); ++rs) {
+        const int swi = (kSweeps > 0) ? sw : rs;
+        if (mine) {
+          float T[3];
+          unsigned ch = 0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            T[k] = live[k] ? s_vt[id[k]] : h[k];
+            const unsigned c = live[k] ? (unsigned)s_vchg[id[k]] : (hchg >> k) & 1u;
+            ch |= c << k;
+          }
+          if (swi == 0) ch = 0x7u;
+          float nw0 = T[0], nw1 = T[1], nw2 = T[2];
+          if (!(T[0] >= kLarge2DDev && T[1] >= kLarge2DDev && T[2] >= kLarge2DDev) &&
+              (ch || T[0] != T[0] || T[1] != T[1] || T[2] != T[2])) {
+            // corner 0 from (v1, v2); corner 1 from (v2, v0); corner 2 from (v0, v1)
+            nw0 = tri_update<!kCheck>(T[1], T[2], T[0], e1, e2, e0, F, eF0, eF2);
+            nw1 = tri_update<!kCheck>(T[2], T[0], T[1], e2, e0, e1, F, eF1, eF0);
+            nw2 = tri_update<!kCheck>(T[0], T[1], T[2], e0, e1, e2, F, eF2, eF1);
+          }
+          const float nw[3] = {nw0, nw1, nw2};
+          hchg = 0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            if (live[k]) {
+              if (nw[k] < T[k]) atomicMin(&s_vnew[id[k]], fkey(nw[k]));
+            } else {
+              hchg |= (nw[k] != h[k] ? 1u : 0u) << k;
+              h[k] = nw[k];
+            }
+          }
+        }
+        __syncthreads();
+        const bool last = (swi == nsweeps - 1);
+        for (int k = tid; k < nown; k += NT) {
+          const float nv = fval(s_vnew[k]);
+          const float ov = s_vt[k];
+          if (last && k < kReduceCap2D) {
+            if (kCheck) {
+              myconv &= ((ov - nv) < kEps2D) ? 1 : 0;
+            } else {
+              float res = ov - nv;
+              if (res < 0.0f) res = -res;
+              myconv &= (res <= kEps2D) ? 1 : 0;
+            }
+          }
+          s_vchg[k] = (nv != ov) ? 1 : 0;
+          s_vt[k] = nv;
+        }
+        __syncthreads();
+      }
+    }
+    const int allc = __syncthreads_and(myconv);
+    for (int k = tid; k < nown; k += NT) Tdst[bd.vbase + k] = s_vt[k];
+    if (tid == 0) {
+      if (!kCheck) {
+        a.conv[b] = allc;
+        atomicAdd(&a.ctl->fim_visits, 1ull);
+        atomicAdd(&a.ctl->fim_slots, (unsigned long long)ns);
+        atomicAdd(&a.ctl->fim_halo, (unsigned long long)bd.nhalo);
+        atomicAdd(&a.ctl->fim_owned, (unsigned long long)nown);
+      } else {
+        if (!allc) {
+          nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+          a.stampA[b] = stamp + 1;
+        }
+        atomicAdd(&a.ctl->chk_visits, 1ull);
+      }
+      atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
+      atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
+      atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
+      atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+    }
+    __syncthreads();
+  }
+  stamp_end(a, iter, kCheck ? 1 : 0);
+}
+
+size_t smem_bytes_slot2d(int max_slots_pad, int max_local, int max_owned) {
+  size_t n = 16 * (size_t)max_slots_pad + 8 * (size_t)max_slots_pad + 4 * (size_t)max_local +
+             4 * (size_t)max_owned + (size_t)max_owned;
+  return (n + 15) & ~(size_t)15;
 }
 
 // ===========================================================================
@@ -663,7 +833,7 @@ __global__ void k_selftest_tri(const float* in, float* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     const float* a = in + 7 * (size_t)i;
-    out[i] = tri_update(a[0], a[1], a[2], a[3], a[4], a[5], a[6]);
+    out[i] = tri_update<false>(a[0], a[1], a[2], a[3], a[4], a[5], a[6], 0.f, 0.f);
   }
 }
 __global__ void k_selftest_quot(const float* in, float* out, int n) {
@@ -931,12 +1101,29 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    void* kv_fim = (L.dim == 3) ? (void*)k_visit3d<false> : (void*)k_visit2d<false>;
-    void* kv_chk = (L.dim == 3) ? (void*)k_visit3d<true> : (void*)k_visit2d<true>;
+    // 2D blocks of up to 1024 slots use the thread-per-slot kernel (bitwise equal
+    // to the reference); larger 2D blocks fall back to the slot-loop kernel
+    const bool slot2d = (L.dim == 2) && P.max_slots_pad <= 1024;
+    int vthreads = threads;
+    size_t vsmem = P.smem;
+    void* kv_fim;
+    void* kv_chk;
+    if (L.dim == 3) {
+      kv_fim = (void*)k_visit3d<false>;
+      kv_chk = (void*)k_visit3d<true>;
+    } else if (slot2d) {
+      vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
+      vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
+      kv_fim = (sweeps == 7) ? (void*)k_visit2d_slot<false, 7> : (void*)k_visit2d_slot<false, 0>;
+      kv_chk = (void*)k_visit2d_slot<true, 1>;
+    } else {
+      kv_fim = (void*)k_visit2d<false>;
+      kv_chk = (void*)k_visit2d<true>;
+    }
     for (void* k : {kv_fim, kv_chk})
-      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
     int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, threads, P.smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, vthreads, vsmem));
     if (occ < 1) return "visit kernel cannot be resident (shared memory / registers)";
     P.grid_visit = std::min(occ * nsm, std::max(L.nb, 1));
     P.grid_aux = nsm * 4;
@@ -965,14 +1152,14 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     static int dim3v = 3, dim2v = 2;
     void* snap_args[] = {&P.args, (L.dim == 3) ? (void*)&dim3v : (void*)&dim2v};
     std::string e;
-    if (!(e = add(kv_fim, P.grid_visit, threads, P.smem, args_ptr)).empty()) return e;
+    if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
     if (L.dim == 3) {
       if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, P.grid_visit, threads, P.smem, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
       if (!(e = add((void*)k_close3d, 1, 32, 0, args_ptr)).empty()) return e;
     } else {
       if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, P.grid_visit, threads, P.smem, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
       if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
     }
     if (want_hist)
@@ -1050,7 +1237,85 @@ std::string DeviceSolve::history(int i, float* out_host) const {
   return "";
 }
 
+std::string DeviceSolve::visit_once(bool check, const float* T_host, float* out_host) {
+  Impl& P = *p_;
+  if (!L_) return "no layout uploaded";
+  const Layout& L = *L_;
+  cudaStream_t st = (cudaStream_t)stream_;
+  std::vector<int> all(L.nb);
+  for (int b = 0; b < L.nb; ++b) all[b] = b;
+  CK(cudaMemcpyAsync(P.Ta, T_host, sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.Tb, T_host, sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.Tinit, T_host, sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.list0, all.data(), sizeof(int) * L.nb, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(P.stampA, 0, sizeof(int) * L.nb, st));
+  Ctl c{};
+  c.max_iters = 1;
+  c.nact = L.nb;
+  CK(cudaMemcpyAsync(P.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+  DevArgs a{};
+  a.blocks = P.blocks; a.coef = P.coef; a.lv = P.lv; a.halo = P.halo; a.nbr_off = P.nbr_off; a.nbr = P.nbr;
+  a.vblock = P.vblock; a.nb = L.nb; a.nv = L.nv; a.Ta = P.Ta; a.Tb = P.Tb; a.Tinit = P.Tinit; a.prev = P.prev;
+  a.conv = P.conv; a.stampA = P.stampA; a.stampC = P.stampC; a.visited = P.visited; a.list0 = P.list0;
+  a.list1 = P.list1; a.list_new = P.list_new; a.ctl = P.ctl; a.fim_sweeps = (L.dim == 3) ? 2 : 7;
+  a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local; a.max_owned = P.max_owned;
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (L.dim != 2 || P.max_slots_pad > 1024) return "visit_once supports 2D blocks of up to 1024 slots";
+  const int vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
+  const size_t vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
+  if (!check) {
+    CK(cudaFuncSetAttribute((const void*)k_visit2d_slot<false, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    k_visit2d_slot<false, 7><<<std::min(L.nb, nsm * 8), vthreads, vsmem, st>>>(a);
+  } else {
+    CK(cudaFuncSetAttribute((const void*)k_visit2d_slot<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    k_visit2d_slot<true, 1><<<std::min(L.nb, nsm * 8), vthreads, vsmem, st>>>(a);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out_host, check ? P.Ta : P.Tb, sizeof(float) * L.nv, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return "";
+}
+
+// n independent triangles, each its own block owning its three corners; one
+// visit with the product's 2D kernel.  in: 7 floats per case (T0 T1 T2 e01 e12
+// e20 speedInv), out: 3 per case.
+std::string selftest_tri_blocks(const float* in, int n, bool check, float* out) {
+  Layout L;
+  L.dim = 2;
+  L.nv = 3 * n;
+  L.ne = n;
+  L.nb = n;
+  L.perm.resize(L.nv);
+  L.iperm.resize(L.nv);
+  for (int v = 0; v < L.nv; ++v) L.perm[v] = L.iperm[v] = v;
+  L.blocks.resize(n);
+  L.total_slots = 4 * n;
+  L.coef.assign(16 * (size_t)n, 0.f);
+  L.lv.assign(16 * (size_t)n, 0);
+  L.slot_elem.assign(4 * (size_t)n, -1);
+  for (int b = 0; b < n; ++b) {
+    BlockDesc& d = L.blocks[b];
+    d.slot_begin = 4 * b; d.nslots = 1; d.nslots_pad = 4; d.vbase = 3 * b; d.nowned = 3;
+    d.halo_begin = 0; d.nhalo = 0; d.ninside = 1;
+    for (int k = 0; k < 4; ++k) L.coef[16 * (size_t)b + 4 * k] = in[7 * (size_t)b + 3 + k];
+    L.lv[16 * (size_t)b + 0] = 0; L.lv[16 * (size_t)b + 1] = 1; L.lv[16 * (size_t)b + 2] = 2;
+    L.slot_elem[4 * (size_t)b] = b;
+  }
+  L.nbr_off.assign(n + 1, 0);
+  L.max_slots = 1; L.max_local = 3; L.max_owned = 3; L.max_halo = 0;
+  std::vector<float> T(3 * (size_t)n);
+  for (int b = 0; b < n; ++b)
+    for (int k = 0; k < 3; ++k) T[3 * (size_t)b + k] = in[7 * (size_t)b + k];
+  DeviceSolve ds;
+  std::string e = ds.upload(L);
+  if (!e.empty()) return e;
+  return ds.visit_once(check, T.data(), out);
+}
+
 std::string selftest_device(int which, const float* in, float* out, int n) {
+  if (which == 3 || which == 4) return selftest_tri_blocks(in, n, which == 4, out);
   const int nin = (which == 0) ? 9 : (which == 1) ? 7 : 2;
   const int nout = (which == 2) ? 2 : 1;
   float *din = nullptr, *dout = nullptr;

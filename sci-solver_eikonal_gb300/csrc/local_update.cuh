@@ -200,13 +200,20 @@ __device__ __forceinline__ float tet_update(float TA, float TB, float TC, float 
 // reference's MIN macro semantics ((a)<(b)?(a):(b)), not fminf.
 __device__ __forceinline__ float mn2(float a, float b) { return (a < b) ? a : b; }
 
+//
+// kHoisted: inside the reference's multi-sweep FIMCuda the products LenAC*F and
+// LenBC*F do not change between sweeps and are rounded once before the sweeps,
+// so the edge candidates there are TA + RN(LenAC*F); the single-sweep check
+// kernel fuses them into one multiply-add.  EA, EB carry the pre-rounded products
+// in the first form and are ignored in the second.
+template <bool kHoisted>
 __device__ __forceinline__ float tri_update(float TA, float TB, float TC, float LenAB, float LenBC,
-                                            float LenAC, float F) {
+                                            float LenAC, float F, float EA, float EB) {
   float TC1 = kLarge2DDev, TC2 = kLarge2DDev;
   const float TAB = TB - TA;
   const float a = (F * F * LenAB * LenAB - TAB * TAB) * LenAB * LenAB;
-  const float EdgeTA = TA + LenAC * F;
-  const float EdgeTB = TB + LenBC * F;
+  const float EdgeTA = kHoisted ? TA + EA : TA + LenAC * F;
+  const float EdgeTB = kHoisted ? TB + EB : TB + LenBC * F;
   if (a > 0.0f) {
     const float cosA = (LenAC * LenAC + LenAB * LenAB - LenBC * LenBC) / (2.0f * LenAC * LenAB);
     const float b = 2.0f * LenAB * LenAC * cosA * (TAB * TAB - F * F * LenAB * LenAB);
