@@ -156,6 +156,34 @@ int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned 
  *              3 outputs per case. */
 int eik_selftest_local_update(int which, const float* in, float* out, int n);
 
+/* Allocation-free 3D solve.  No counterpart in the reference: an addition for
+ * callers that cannot call cudaMalloc, such as code running while another
+ * component captures the stream into a CUDA graph, real-time or embedded hosts
+ * that reserve all device memory at start-up, and plugins whose host application
+ * owns the device memory pool.
+ *
+ * Inputs and the output are host arrays, as in eik_set_mesh / eik_set_speeds /
+ * eik_set_seeds / eik_get_result (nseeds = 0 means vertex 0; speeds follow
+ * eik_set_speeds).  The partition is the built-in one with max_verts_per_block.
+ * Every device buffer of the solve (block layout, travel times, flags, lists,
+ * control block) lives in one fixed 32 MiB array in the library's device image,
+ * which each GPU that loads the library holds until the process exits; the call
+ * makes no cudaMalloc / cudaFree and uses no allocating library routine.
+ *
+ * The first call on a device looks up the array's device address (with that
+ * device current) and caches it; make that first call before any stream capture.
+ * All calls share the array and it keeps the previous call's contents (the call
+ * clears what must start at zero), so calls that overlap on the GPU, on any
+ * stream or thread, race: serialise them.  Work runs on `stream` (a cudaStream_t,
+ * null = the default stream) with one host round trip per outer iteration; the
+ * call returns when the result is in out_times.
+ *
+ * Meshes whose layout and state exceed the array return EIK_ERR_LIMIT (about
+ * 200k tets at 64 vertices per block); errbuf (may be null) receives the reason. */
+int eik_solve3d_noalloc(const float* xyz, int nv, const int* tets, int nt, const float* speeds, long long nspeeds,
+                        const int* seeds, int nseeds, int max_verts_per_block, int max_iterations, float* out_times,
+                        void* stream, int* iterations, char* errbuf, int errlen);
+
 /* The CUDA stream (cudaStream_t) the handle's solves and copies run on, or null
  * before the first solve.  Lets callers order their own work or time with events. */
 void* eik_stream(const eik_solver* h);

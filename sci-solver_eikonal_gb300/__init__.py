@@ -88,6 +88,9 @@ SIGNATURES = {
     "eik_tri_prep": (ctypes.c_int, [_P, _IP, _IP, _IP, _UP, _IP, _IP]),
     "eik_selftest_local_update": (ctypes.c_int, [ctypes.c_int, _FP, _FP, ctypes.c_int]),
     "eik_stream": (_P, [_P]),
+    "eik_solve3d_noalloc": (ctypes.c_int, [_FP, ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_longlong, _IP,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, _FP, _P, _IP, ctypes.c_char_p,
+                                           ctypes.c_int]),
     "eik_last_error": (ctypes.c_char_p, [_P]),
     "eik_version": (ctypes.c_char_p, []),
 }
@@ -322,6 +325,24 @@ def selftest_local_update(which, inputs):
     if rc:
         raise EikonalError(rc, "self-test kernel failed")
     return out if nout > 1 else out[:, 0]
+
+
+def solve3d_noalloc(xyz, tets, speeds=None, seeds=(0,), max_verts_per_block=64, max_iterations=100, stream=0):
+    """The allocation-free 3D solve (eik_solve3d_noalloc): returns (times, iterations)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+    tets = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1, 4)
+    sp = None if speeds is None else np.ascontiguousarray(speeds, dtype=np.float32).ravel()
+    sd = np.ascontiguousarray(seeds, dtype=np.int32)
+    out = np.empty(xyz.shape[0], dtype=np.float32)
+    it = ctypes.c_int()
+    err = ctypes.create_string_buffer(512)
+    rc = lib().eik_solve3d_noalloc(_fptr(xyz), xyz.shape[0], _iptr(tets), tets.shape[0],
+                                   _fptr(sp) if sp is not None else None, 0 if sp is None else sp.size,
+                                   _iptr(sd), sd.size, int(max_verts_per_block), int(max_iterations), _fptr(out),
+                                   ctypes.c_void_p(stream), ctypes.byref(it), err, len(err))
+    if rc:
+        raise EikonalError(rc, err.value.decode())
+    return out, it.value
 
 
 def version():

@@ -434,6 +434,43 @@ int eik_selftest_local_update(int which, const float* in, float* out, int n) {
   return selftest_device(which, in, out, n).empty() ? EIK_OK : EIK_ERR_CUDA;
 }
 
+// Allocation-free 3D solve: see the header.  Builds the partition and the block
+// layout on the host, then runs the solve with every device buffer inside the
+// library's fixed scratch array.
+int eik_solve3d_noalloc(const float* xyz, int nv, const int* tets, int nt, const float* speeds, long long nspeeds,
+                        const int* seeds, int nseeds, int max_verts_per_block, int max_iterations, float* out_times,
+                        void* stream, int* iterations, char* errbuf, int errlen) {
+  auto report = [&](int code, const std::string& msg) {
+    if (errbuf && errlen > 0) {
+      std::snprintf(errbuf, (size_t)errlen, "%s", msg.c_str());
+    }
+    return code;
+  };
+  if (!xyz || !tets || !out_times || nv <= 0 || nt <= 0 || nseeds < 0 || (nseeds > 0 && !seeds) ||
+      (nspeeds > 0 && !speeds) || max_verts_per_block <= 0 || max_iterations < 0)
+    return report(EIK_ERR_ARG, "invalid argument");
+  std::vector<int> el(tets, tets + 4 * (size_t)nt);
+  std::string msg = normalize_index_base(el, nv);
+  if (!msg.empty()) return report(EIK_ERR_MESH, msg);
+  std::vector<int> sd = (nseeds > 0) ? std::vector<int>(seeds, seeds + nseeds) : std::vector<int>(1, 0);
+  for (int v : sd)
+    if (v < 0 || v >= nv) return report(EIK_ERR_ARG, "seed out of range");
+  std::vector<float> M;
+  tet_metrics(nt, nspeeds > 0 ? speeds : nullptr, (size_t)std::max(0ll, nspeeds), M);
+  std::vector<int> labels;
+  const int nb = metis_rule_blocks(nv, max_verts_per_block, 3);
+  partition_rcb(nv, xyz, nb, labels);
+  Layout L;
+  msg = build_layout3d(nv, xyz, nt, el.data(), M.data(), labels.data(), nb, L);
+  if (!msg.empty()) return report(EIK_ERR_MESH, msg);
+  int it = 0;
+  size_t need = 0;
+  msg = solve3d_noalloc(L, sd, max_iterations, out_times, (cudaStream_t)stream, &it, &need);
+  if (!msg.empty()) return report(msg.find("too large") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, msg);
+  if (iterations) *iterations = it;
+  return EIK_OK;
+}
+
 void* eik_stream(const eik_solver* h) { return (h && h->dev) ? h->dev->stream() : nullptr; }
 
 const char* eik_last_error(const eik_solver* h) { return h ? h->err.c_str() : "null handle"; }

@@ -15,6 +15,9 @@
 
 #include "setup.hpp"
 
+struct CUstream_st;
+typedef struct CUstream_st* cudaStream_t;
+
 namespace eikgb {
 
 struct SolveStats {
@@ -83,5 +86,13 @@ class DeviceSolve {
 // root_quot); 3 / 4: single-triangle blocks through the 2D sweep / check kernel
 // (7 inputs -> 3 outputs).  Host arrays.
 std::string selftest_device(int which, const float* in, float* out, int n);
+
+// Allocation-free 3D solve: the layout and every solver buffer live in a fixed
+// 32 MiB array of the library's device image (no cudaMalloc / cudaFree).  Runs on
+// `stream` (a cudaStream_t, may be null), one host round trip per outer
+// iteration.  Fails with a message when the mesh needs more scratch than the array
+// holds (bytes_needed reports the requirement).
+std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int max_iters, float* out_host,
+                            cudaStream_t stream, int* iterations, size_t* bytes_needed);
 
 }  // namespace eikgb

@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1333,6 +1334,197 @@ std::string selftest_device(int which, const float* in, float* out, int n) {
   cudaFree(din);
   cudaFree(dout);
   if (e != cudaSuccess) return std::string("self-test kernel: ") + cudaGetErrorString(e);
+  return "";
+}
+
+}  // namespace eikgb
+
+// ===========================================================================
+// Allocation-free 3D solve (eik_solve3d_noalloc).
+//
+// Some callers cannot call cudaMalloc: code that runs while another component
+// captures the stream into a CUDA graph, real-time or embedded hosts that reserve
+// all device memory at start-up, and plugins whose host application owns the
+// device memory pool.  This path keeps every device buffer of one solve (the
+// block layout and the solver state) in one fixed array in the library's device
+// image instead of allocating.  The array is kNoAllocScratchBytes (32 MiB) on
+// every GPU that loads the library, for the life of the process.
+// ===========================================================================
+static __device__ __align__(256) unsigned char g_noalloc_scratch[32u << 20];
+
+namespace eikgb {
+
+constexpr size_t kNoAllocScratchBytes = sizeof(g_noalloc_scratch);
+
+namespace {
+
+// End of an outer iteration without a CUDA graph (the host reads the control
+// block between iterations instead of a conditional node).
+__global__ void k_close3d_noalloc(DevArgs a) {
+  if (threadIdx.x != 0) return;
+  Ctl* c = a.ctl;
+  c->iter += 1;
+  c->nact = c->nnext;
+  c->nnext = 0;
+  c->nnew = 0;
+  c->work_a = c->work_b = c->work_c = c->work_d = 0;
+  c->done_c = c->done_d = 0;
+  c->conv_fail = 0;
+}
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_base[64] = {};
+
+// Device address of the scratch array on the current device, looked up once per
+// device with that device current.
+std::string noalloc_base(void** out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return "device index out of range";
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_base[dev] = p;
+  }
+  *out = g_noalloc_base[dev];
+  return "";
+}
+
+// carve `n` elements of T from the scratch cursor (256-byte aligned)
+template <typename T>
+T* carve_scratch(unsigned char* base, size_t& off, size_t n) {
+  off = (off + 255) & ~(size_t)255;
+  T* p = reinterpret_cast<T*>(base + off);
+  off += sizeof(T) * (n ? n : 1);
+  return p;
+}
+
+}  // namespace
+
+std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int max_iters, float* out_host,
+                            cudaStream_t st, int* iterations, size_t* bytes_needed) {
+  const int ncoef = 6;
+  // byte budget of the layout and the state
+  size_t need = 0;
+  {
+    unsigned char* z = nullptr;
+    carve_scratch<BlockDesc>(z, need, L.nb);
+    carve_scratch<float>(z, need, L.coef.size());
+    carve_scratch<uint16_t>(z, need, L.lv.size());
+    carve_scratch<int>(z, need, L.halo_ids.size());
+    carve_scratch<int>(z, need, L.nbr_off.size());
+    carve_scratch<int>(z, need, L.nbr.size());
+    for (int k = 0; k < 2; ++k) carve_scratch<int>(z, need, L.nv);          // vblock, perm
+    for (int k = 0; k < 3; ++k) carve_scratch<float>(z, need, L.nv);        // Ta, Tb, out
+    for (int k = 0; k < 6; ++k) carve_scratch<int>(z, need, L.nb);          // conv, stamps, lists
+    carve_scratch<unsigned char>(z, need, L.nb);                            // visited
+    carve_scratch<Ctl>(z, need, 1);
+  }
+  if (bytes_needed) *bytes_needed = need;
+  if (need > kNoAllocScratchBytes)
+    return "mesh too large for the allocation-free path: needs " + std::to_string(need >> 20) +
+           " MiB of scratch, the fixed array holds " + std::to_string(kNoAllocScratchBytes >> 20) + " MiB";
+  const int max_slots_pad = (L.max_slots + 3) & ~3;
+  const int max_local = std::max(L.max_local, 1), max_owned = std::max(L.max_owned, 1);
+  const size_t smem = smem_bytes(ncoef, max_slots_pad, max_local, max_owned);
+  int dev = 0, maxsm = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (smem + 64 > (size_t)maxsm) return "block too large for shared memory; use fewer vertices per block";
+  void* basev = nullptr;
+  std::string e = noalloc_base(&basev);
+  if (!e.empty()) return e;
+  unsigned char* base = static_cast<unsigned char*>(basev);
+  size_t off = 0;
+  DevArgs a{};
+  BlockDesc* blocks = carve_scratch<BlockDesc>(base, off, L.nb);
+  float* coef = carve_scratch<float>(base, off, L.coef.size());
+  uint16_t* lv = carve_scratch<uint16_t>(base, off, L.lv.size());
+  int* halo = carve_scratch<int>(base, off, L.halo_ids.size());
+  int* nbr_off = carve_scratch<int>(base, off, L.nbr_off.size());
+  int* nbr = carve_scratch<int>(base, off, L.nbr.size());
+  int* vblock = carve_scratch<int>(base, off, L.nv);
+  int* perm = carve_scratch<int>(base, off, L.nv);
+  float* Ta = carve_scratch<float>(base, off, L.nv);
+  float* Tb = carve_scratch<float>(base, off, L.nv);
+  float* out = carve_scratch<float>(base, off, L.nv);
+  int* conv = carve_scratch<int>(base, off, L.nb);
+  int* stampA = carve_scratch<int>(base, off, L.nb);
+  int* stampC = carve_scratch<int>(base, off, L.nb);
+  int* list0 = carve_scratch<int>(base, off, L.nb);
+  int* list1 = carve_scratch<int>(base, off, L.nb);
+  int* list_new = carve_scratch<int>(base, off, L.nb);
+  unsigned char* visited = carve_scratch<unsigned char>(base, off, L.nb);
+  Ctl* ctl = carve_scratch<Ctl>(base, off, 1);
+
+  // inputs into the scratch array; everything that must start at zero is cleared
+  // here because the array keeps the previous call's contents
+  std::vector<int> vb(L.nv, 0);
+  for (int b = 0; b < L.nb; ++b)
+    for (int k = 0; k < L.blocks[b].nowned; ++k) vb[L.blocks[b].vbase + k] = b;
+  std::vector<float> init(L.nv, kLarge3D);
+  std::vector<char> act(L.nb, 0);
+  for (int s : seeds) {
+    init[L.perm[s]] = 0.0f;
+    act[vb[L.perm[s]]] = 1;
+  }
+  std::vector<int> alist;
+  for (int b = 0; b < L.nb; ++b)
+    if (act[b]) alist.push_back(b);
+  CK(cudaMemcpyAsync(blocks, L.blocks.data(), sizeof(BlockDesc) * L.nb, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(lv, L.lv.data(), sizeof(uint16_t) * L.lv.size(), cudaMemcpyHostToDevice, st));
+  if (!L.halo_ids.empty())
+    CK(cudaMemcpyAsync(halo, L.halo_ids.data(), sizeof(int) * L.halo_ids.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(nbr_off, L.nbr_off.data(), sizeof(int) * L.nbr_off.size(), cudaMemcpyHostToDevice, st));
+  if (!L.nbr.empty()) CK(cudaMemcpyAsync(nbr, L.nbr.data(), sizeof(int) * L.nbr.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(vblock, vb.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(perm, L.perm.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(Ta, init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(Tb, init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(conv, 0, sizeof(int) * L.nb, st));
+  CK(cudaMemsetAsync(stampA, 0, sizeof(int) * L.nb, st));
+  CK(cudaMemsetAsync(stampC, 0, sizeof(int) * L.nb, st));
+  CK(cudaMemsetAsync(visited, 0, L.nb, st));
+  if (!alist.empty()) CK(cudaMemcpyAsync(list0, alist.data(), sizeof(int) * alist.size(), cudaMemcpyHostToDevice, st));
+  Ctl c{};
+  c.max_iters = max_iters;
+  c.nact = (int)alist.size();
+  CK(cudaMemcpyAsync(ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+
+  a.blocks = blocks; a.coef = coef; a.lv = reinterpret_cast<const uint2*>(lv); a.halo = halo; a.nbr_off = nbr_off;
+  a.nbr = nbr; a.vblock = vblock; a.nb = L.nb; a.nv = L.nv; a.Ta = Ta; a.Tb = Tb; a.Tinit = Ta; a.prev = Tb;
+  a.conv = conv; a.stampA = stampA; a.stampC = stampC; a.visited = visited; a.list0 = list0; a.list1 = list1;
+  a.list_new = list_new; a.ctl = ctl; a.hist = nullptr; a.hist_cap = 0; a.ktime = nullptr; a.ktime_cap = 0;
+  a.fim_sweeps = 2; a.max_slots_pad = max_slots_pad; a.max_local = max_local; a.max_owned = max_owned;
+  CK(cudaFuncSetAttribute((const void*)k_visit3d<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CK(cudaFuncSetAttribute((const void*)k_visit3d<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_visit3d<false>, 256, smem));
+  if (occ < 1) return "visit kernel cannot be resident";
+  const int grid = std::min(occ * nsm, std::max(L.nb, 1));
+  int iters = 0;
+  for (;;) {
+    Ctl h{};
+    CK(cudaMemcpyAsync(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    iters = h.iter;
+    if (h.error) return "device reported error flags " + std::to_string(h.error);
+    if (h.nact == 0 || h.iter >= max_iters) break;
+    k_visit3d<false><<<grid, 256, smem, st>>>(a);
+    k_commit3d<<<nsm * 4, 256, 0, st>>>(a);
+    k_visit3d<true><<<grid, 256, smem, st>>>(a);
+    k_close3d_noalloc<<<1, 32, 0, st>>>(a);
+    CK(cudaGetLastError());
+  }
+  k_gather_result<<<std::max(1, std::min(1024, (L.nv + 255) / 256)), 256, 0, st>>>(Ta, visited, vblock, perm, L.nv,
+                                                                                   3, out);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out_host, out, sizeof(float) * L.nv, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (iterations) *iterations = iters;
   return "";
 }
 
