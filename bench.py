@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-sample-iters", type=int, default=0, help="0 = choose automatically")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--launch", default="graph", choices=["graph", "direct"],
+                   help="graph: one CUDA-graph launch per solve; direct: kernel by kernel (for ncu)")
     return p.parse_args()
 
 
@@ -196,6 +198,7 @@ def main():
     e.maxVertsPerBlock_ = 64
     e.maxIterations_ = MAX_ITERS
     e.keepHistory_ = 0
+    e.directLaunch_ = 1 if args.launch == "direct" else 0
     t0 = time.perf_counter()
     e.solveEikonal()  # partition, layout, upload, graph build, first solve
     setup_s = time.perf_counter() - t0
@@ -286,7 +289,8 @@ def main():
         "config": {"workload": WORKLOAD, "blocks": st0["num_blocks"], "iterations_per_solve": iters[0],
                    "vertex_updates_per_solve": upd // args.steps, "max_iterations": MAX_ITERS,
                    "l2": "flushed before every timed solve (512 MB write, outside the timed events)",
-                   "partition": "recursive coordinate bisection", "parallelism": f"replicas x{world}"},
+                   "partition": "recursive coordinate bisection", "parallelism": f"replicas x{world}",
+                   "launch": args.launch},
         "solves_per_s": world * args.steps / (total_ms * 1e-3),
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
         "setup_s": setup_s,

@@ -49,6 +49,10 @@ typedef struct eik_options {
   int verbose;             /* verbose_ (0) */
   int keep_history;        /* 1 (default): keep every iteration for eik_get_iteration */
   int fim_sweeps;          /* sweeps per active-block visit; -1 = reference (3D 2, 2D 7) */
+  int direct_launch;       /* 0 (default): a solve is one CUDA-graph launch; 1: the same kernels
+                              launched one by one with a host check per iteration, for profilers
+                              that cannot see kernels inside conditional graphs */
+  int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/512/1024); 0 = default */
 } eik_options;
 
 typedef struct eik_stats {

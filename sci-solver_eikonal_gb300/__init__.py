@@ -33,7 +33,7 @@ class EikOptions(ctypes.Structure):
         ("square_block_length", ctypes.c_int), ("square_block_width", ctypes.c_int),
         ("square_block_depth", ctypes.c_int),
         ("max_iterations", ctypes.c_int), ("verbose", ctypes.c_int), ("keep_history", ctypes.c_int),
-        ("fim_sweeps", ctypes.c_int),
+        ("fim_sweeps", ctypes.c_int), ("direct_launch", ctypes.c_int), ("threads_per_block", ctypes.c_int),
     ]
 
 
@@ -148,6 +148,7 @@ class Eikonal:
         "squareBlockLength_": "square_block_length", "squareBlockWidth_": "square_block_width",
         "squareBlockDepth_": "square_block_depth", "maxIterations_": "max_iterations",
         "verbose_": "verbose", "keepHistory_": "keep_history", "fimSweeps_": "fim_sweeps",
+        "directLaunch_": "direct_launch", "threadsPerBlock_": "threads_per_block",
     }
 
     def __init__(self, isTriMesh, fname="../src/test/test_data/sphere_74verts.ply", verbose=False):

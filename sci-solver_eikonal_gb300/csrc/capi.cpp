@@ -153,6 +153,8 @@ void eik_default_options(eik_options* o) {
   o->verbose = 0;
   o->keep_history = 1;
   o->fim_sweeps = -1;
+  o->direct_launch = 0;
+  o->threads_per_block = 0;
 }
 
 int eik_create(int is_tri_mesh, eik_solver** out) {
@@ -172,6 +174,9 @@ int eik_set_options(eik_solver* h, const eik_options* o) {
   if (o->max_verts_per_block <= 0) return fail(h, EIK_ERR_ARG, "max_verts_per_block must be positive");
   if (o->max_iterations < 0) return fail(h, EIK_ERR_ARG, "max_iterations must be >= 0");
   if (o->speed_type != EIK_SPEED_ONE) return fail(h, EIK_ERR_ARG, "only speed type ONE is supported");
+  if (o->threads_per_block != 0 && o->threads_per_block != 128 && o->threads_per_block != 256 &&
+      o->threads_per_block != 512 && o->threads_per_block != 1024)
+    return fail(h, EIK_ERR_ARG, "threads_per_block must be 0, 128, 256, 512 or 1024");
   h->opt = *o;
   return EIK_OK;
 }
@@ -296,6 +301,8 @@ int eik_solve(eik_solver* h) {
   so.fim_sweeps = h->opt.fim_sweeps;
   so.keep_history = h->opt.keep_history != 0;
   so.history_cap = h->opt.max_iterations;
+  so.direct_launch = h->opt.direct_launch != 0;
+  if (h->opt.threads_per_block > 0) so.threads = h->opt.threads_per_block;
   e = h->dev->solve(so);
   if (!e.empty()) {
     h->solved = false;

@@ -43,7 +43,8 @@ struct SolveOptions {
   int fim_sweeps = -1;       // -1: reference value (3D: 2, 2D: 7)
   bool keep_history = false; // per-iteration snapshots (getResultAtIteration)
   int history_cap = 0;       // snapshots kept when keep_history
-  int threads = 256;         // CTA size of the visit kernels
+  int threads = 0;           // CTA size of the 3D visit kernels (0: from the largest block)
+  bool direct_launch = false; // launch the loop body kernel by kernel (for profilers)
 };
 
 class DeviceSolve {

@@ -55,7 +55,7 @@ struct Ctl {
   int done_c, done_d;
   int conv_fail;  // 2D: a vertex failed the all-vertex test this iteration
   int error;
-  int pad_;
+  int stop;       // set when the outer loop must end (read by the direct-launch loop)
   unsigned long long updates, fim_visits, chk_visits, slot_visits, halo_visits, owned_visits;
   unsigned long long fim_slots, fim_halo, fim_owned;  // per-visit inputs of the sweep kernel only
 };
@@ -90,6 +90,7 @@ struct DevArgs {
   int fim_sweeps;
   int max_slots_pad, max_local, max_owned;
   cudaGraphConditionalHandle cond;
+  int use_cond;  // 1 inside the CUDA graph, 0 for direct launches
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -226,10 +227,11 @@ __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd
 //           kCheck = true  -> run_check_neghbor (1 sweep, flags only)
 // ===========================================================================
 template <bool kCheck>
-__global__ void __launch_bounds__(256) k_visit3d(DevArgs a) {
+__global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
+  __shared__ volatile int s_moved;  // check visits: some owned vertex drops by >= EPS
   const Smem s0 = carve(sm, a, 6);
   const int tid = threadIdx.x, NT = blockDim.x;
   const Ctl* ctl = a.ctl;
@@ -268,10 +270,15 @@ __global__ void __launch_bounds__(256) k_visit3d(DevArgs a) {
       for (int k = 0; k < 4; ++k) s.h0[4 * j + k] = (id[k] < nown) ? 0.0f : s.vt[id[k]];
       s.m0[j] = 0;
     }
+    if (tid == 0) s_moved = 0;
     __syncthreads();
     int myconv = 1;
     for (int sw = 0; sw < nsweeps; ++sw) {
       for (int j = tid; j < ns; j += NT) {
+        // A check only decides whether the block stays converged; one candidate
+        // that lowers an owned vertex by EPS or more decides it (the minimum can
+        // only be lower), so the remaining slots are skipped.
+        if (kCheck && s_moved) break;
         const uint2 l = s.lv[j];
         const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
         bool own[4];
@@ -309,19 +316,29 @@ __global__ void __launch_bounds__(256) k_visit3d(DevArgs a) {
           nw[1] = fminf(TB, tet_update(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC));
           nw[2] = fminf(TC, tet_update(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD));
         }
-        unsigned m = 0;
+        if (kCheck) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          if (own[k]) {
-            if (nw[k] < T[k]) atomicMin(&s.vnew[id[k]], fkey(nw[k]));
-          } else {
-            s.h1[4 * j + k] = nw[k];
-            m |= (nw[k] != T[k] ? 1u : 0u) << k;
+          for (int k = 0; k < 4; ++k)
+            if (own[k] && !((T[k] - nw[k]) <= kEps3DLe)) s_moved = 1;  // (double)(old - c) >= 1e-5
+        } else {
+          unsigned m = 0;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (own[k]) {
+              if (nw[k] < T[k]) atomicMin(&s.vnew[id[k]], fkey(nw[k]));
+            } else {
+              s.h1[4 * j + k] = nw[k];
+              m |= (nw[k] != T[k] ? 1u : 0u) << k;
+            }
           }
+          s.m1[j] = (unsigned char)m;
         }
-        s.m1[j] = (unsigned char)m;
       }
       __syncthreads();
+      if (kCheck) {
+        myconv = s_moved ? 0 : 1;
+        break;
+      }
       const bool last = (sw == nsweeps - 1);
       for (int k = tid; k < nown; k += NT) {
         const float nv = fval(s.vnew[k]);
@@ -751,7 +768,8 @@ __device__ void finish_iteration(const DevArgs& a, bool all_vertices_converged) 
   c->done_c = c->done_d = 0;
   c->conv_fail = 0;
   const bool go = c->nact > 0 && c->iter < c->max_iters && !all_vertices_converged && c->error == 0;
-  cudaGraphSetConditional(a.cond, go ? 1u : 0u);
+  c->stop = go ? 0 : 1;
+  if (a.use_cond) cudaGraphSetConditional(a.cond, go ? 1u : 0u);
 }
 
 // last-CTA detection without any waiting: every CTA bumps the counter once
@@ -907,6 +925,13 @@ struct DeviceSolve::Impl {
   int grid_visit = 0, grid_aux = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int max_slots_pad = 0, max_local = 0, max_owned = 0;
+  struct Launch {
+    void* func;
+    int grid, block;
+    size_t smem;
+    int extra;  // second kernel argument (k_snapshot's dimension), unused otherwise
+  };
+  std::vector<Launch> body;  // the loop body, in graph order
 
   void free_all() {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
@@ -1042,7 +1067,14 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   const Layout& L = *L_;
   cudaStream_t st = (cudaStream_t)stream_;
   const int sweeps = (opt.fim_sweeps > 0) ? opt.fim_sweeps : (L.dim == 3 ? 2 : 7);
-  const int threads = (opt.threads == 128 || opt.threads == 256) ? opt.threads : 256;
+  // CTA size of the 3D visit kernels: one thread per element slot of the largest
+  // block (one tet-update group per thread per sweep) measured fastest on the
+  // 65^3 workload; explicit 128/256/512/1024 overrides it
+  int auto_threads = 256;
+  while (auto_threads < P.max_slots_pad && auto_threads < 1024) auto_threads *= 2;
+  const int threads = (opt.threads == 128 || opt.threads == 256 || opt.threads == 512 || opt.threads == 1024)
+                          ? opt.threads
+                          : auto_threads;
   const int hcap = opt.keep_history ? std::max(0, opt.history_cap) : 0;
   if (hcap > 0 && hcap != P.hist_cap) {
     if (P.hist) cudaFree(P.hist);
@@ -1097,6 +1129,7 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     a.ktime = P.ktime; a.ktime_cap = P.ktime_cap;
     a.fim_sweeps = sweeps; a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local;
     a.max_owned = P.max_owned;
+    a.use_cond = 1;
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
     int dev = 0, nsm = 0;
@@ -1142,7 +1175,9 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     CK(cudaGraphAddNode(&n_while, P.graph, &n_start, nullptr, 1, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     cudaGraphNode_t prevn = nullptr, n;
+    P.body.clear();
     auto add = [&](void* f, int grid, int block, size_t sm, void** params) -> std::string {
+      P.body.push_back(Impl::Launch{f, grid, block, sm, (f == (void*)k_snapshot) ? L.dim : 0});
       cudaKernelNodeParams q{};
       q.func = f; q.gridDim = dim3(grid); q.blockDim = dim3(block); q.sharedMemBytes = (unsigned)sm;
       q.kernelParams = params;
@@ -1172,7 +1207,25 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     P.g_histcap = hcap;
   }
   CK(cudaEventRecord(P.ev0, st));
-  CK(cudaGraphLaunch(P.exec, st));
+  if (!opt.direct_launch) {
+    CK(cudaGraphLaunch(P.exec, st));
+  } else {
+    // the graph's kernels launched one by one, the host reading the control block
+    // between iterations (profilers cannot see kernels inside conditional graphs)
+    DevArgs d = P.args;
+    d.use_cond = 0;
+    for (;;) {
+      Ctl h{};
+      CK(cudaMemcpyAsync(&h, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      if (h.stop || h.error || h.nact <= 0 || h.iter >= opt.max_iterations) break;
+      for (const Impl::Launch& l : P.body) {
+        void* args[2] = {&d, (void*)&l.extra};
+        CK(cudaLaunchKernel(l.func, dim3(l.grid), dim3(l.block), args, l.smem, st));
+      }
+      CK(cudaGetLastError());
+    }
+  }
   CK(cudaEventRecord(P.ev1, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());

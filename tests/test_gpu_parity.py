@@ -289,6 +289,28 @@ def test_resolve_after_speed_change_matches_fresh_handle(need_gpu, eik, mg):
     assert bits_equal(g.getFinalResult(), f.getFinalResult())
 
 
+def test_direct_launch_matches_graph_launch(need_gpu, eik, mg):
+    """The kernel-by-kernel mode (for profilers) computes exactly what the single
+    graph launch computes, in 3D and 2D."""
+    xyz, tets, sp, seed = cube(mg, 17)
+    a = solve3d(eik, xyz, tets, sp, [seed])
+    b = solve3d(eik, xyz, tets, sp, [seed], directLaunch_=1)
+    assert a.numIterations() == b.numIterations()
+    assert bits_equal(a.getFinalResult(), b.getFinalResult())
+    assert a.stats()["vertex_updates"] == b.stats()["vertex_updates"]
+    xyz2, f2 = mg.icosphere(4)
+    res = []
+    for direct in (0, 1):
+        e = eik.Eikonal(True)
+        e.set_mesh(xyz2, f2)
+        e.initSpeedMtxMultipliers(mg.batch_speed(xyz2, f2))
+        e.maxVertsPerBlock_ = 32
+        e.directLaunch_ = direct
+        e.solveEikonal()
+        res.append((e.numIterations(), e.getFinalResult()))
+    assert res[0][0] == res[1][0] and bits_equal(res[0][1], res[1][1])
+
+
 def test_write_vtk(need_gpu, eik, golden, tmp_path):
     e = eik.Eikonal(False)
     e.set_mesh(golden["sphere334_xyz"], golden["sphere334_tets"])
