@@ -188,6 +188,41 @@ int eik_solve3d_noalloc(const float* xyz, int nv, const int* tets, int nt, const
                         const int* seeds, int nseeds, int max_verts_per_block, int max_iterations, float* out_times,
                         void* stream, int* iterations, char* errbuf, int errlen);
 
+/* ---- Batched solves --------------------------------------------------------
+ * No counterpart in the reference, which solves one mesh per Eikonal object
+ * (src/Eikonal.cu:139-279 solveEikonal).  A batch packs the solves of several
+ * handles of the same dimension (each with its own mesh, speeds, seeds, initial
+ * values, partition and max_iterations, set through the calls above) into one
+ * device-resident layout and runs them in ONE device loop: every outer iteration
+ * visits the active blocks of all unfinished instances from a single work list,
+ * and each instance stops on its own rule (active list empty, its iteration cap,
+ * 2D all-vertex test).  Every instance's result equals, bit for bit, the result
+ * of eik_solve on its handle alone.  Launch shape (threads_per_block,
+ * direct_launch, fim_sweeps) comes from the first handle's options.
+ *
+ * The packed layout is rebuilt when a handle's mesh, partition inputs or speeds
+ * changed since the last eik_batch_solve; seeds and initial values are re-read on
+ * every call.  The handles must outlive the batch. */
+typedef struct eik_batch eik_batch;
+int eik_batch_create(eik_solver* const* solvers, int n, eik_batch** out);
+void eik_batch_destroy(eik_batch* b);
+int eik_batch_solve(eik_batch* b);
+int eik_batch_num_instances(const eik_batch* b);
+/* vertices of instance i (= eik_num_vertices of its handle) */
+int eik_batch_num_vertices(const eik_batch* b, int i);
+/* outer iterations instance i ran in the last eik_batch_solve */
+int eik_batch_num_iterations(const eik_batch* b, int i);
+/* result of instance i in its handle's vertex order; nv must equal its vertex count */
+int eik_batch_get_result(eik_batch* b, int i, float* out, int nv);
+/* all instances' results, instance after instance (n = total vertices) */
+int eik_batch_get_results(eik_batch* b, float* out, long long n);
+/* the same into device memory (n floats, current device) */
+int eik_batch_get_results_device(eik_batch* b, float* out_dev, long long n);
+/* whole-batch statistics of the last eik_batch_solve (iterations = longest instance) */
+int eik_batch_get_stats(const eik_batch* b, eik_stats* s);
+void* eik_batch_stream(const eik_batch* b);
+const char* eik_batch_last_error(const eik_batch* b);
+
 /* The CUDA stream (cudaStream_t) the handle's solves and copies run on, or null
  * before the first solve.  Lets callers order their own work or time with events. */
 void* eik_stream(const eik_solver* h);

@@ -91,6 +91,18 @@ SIGNATURES = {
     "eik_solve3d_noalloc": (ctypes.c_int, [_FP, ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_longlong, _IP,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _FP, _P, _IP, ctypes.c_char_p,
                                            ctypes.c_int]),
+    "eik_batch_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(_P)]),
+    "eik_batch_destroy": (None, [_P]),
+    "eik_batch_solve": (ctypes.c_int, [_P]),
+    "eik_batch_num_instances": (ctypes.c_int, [_P]),
+    "eik_batch_num_vertices": (ctypes.c_int, [_P, ctypes.c_int]),
+    "eik_batch_num_iterations": (ctypes.c_int, [_P, ctypes.c_int]),
+    "eik_batch_get_result": (ctypes.c_int, [_P, ctypes.c_int, _FP, ctypes.c_int]),
+    "eik_batch_get_results": (ctypes.c_int, [_P, _FP, ctypes.c_longlong]),
+    "eik_batch_get_results_device": (ctypes.c_int, [_P, _P, ctypes.c_longlong]),
+    "eik_batch_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(EikStats)]),
+    "eik_batch_stream": (_P, [_P]),
+    "eik_batch_last_error": (ctypes.c_char_p, [_P]),
     "eik_last_error": (ctypes.c_char_p, [_P]),
     "eik_version": (ctypes.c_char_p, []),
 }
@@ -315,6 +327,76 @@ class Eikonal:
         print("--------|------------------------------------------" + f"  Converged to: {rms[-1]:.4f}")
         print("        |1   5    10   15   20   25   30   35")
         print("                   Iteration")
+
+
+class EikonalBatch:
+    """Several Eikonal solves of one dimension in one device loop (eik_batch_*).
+
+    Built from configured Eikonal objects (mesh, speeds, seeds, options); every
+    solveEikonal() re-reads their seeds and initial values.  Each instance's result
+    equals what solveEikonal() on its object alone gives.
+    """
+
+    def __init__(self, solvers):
+        self._lib = lib()
+        self._solvers = list(solvers)
+        if not self._solvers:
+            raise ValueError("empty batch")
+        for e in self._solvers:
+            if not e._mesh_loaded:
+                e.initializeMesh()
+        arr = (_P * len(self._solvers))(*[e._h for e in self._solvers])
+        h = _P()
+        rc = self._lib.eik_batch_create(arr, len(self._solvers), ctypes.byref(h))
+        if rc:
+            raise EikonalError(rc, "eik_batch_create failed: " + self._solvers[0]._lib.eik_last_error(
+                self._solvers[0]._h).decode())
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.eik_batch_destroy(h)
+            self._h = None
+
+    def __len__(self):
+        return len(self._solvers)
+
+    def _check(self, rc):
+        if rc:
+            raise EikonalError(rc, self._lib.eik_batch_last_error(self._h).decode())
+
+    def solveEikonal(self):
+        for e in self._solvers:
+            e._push_options()
+        self._check(self._lib.eik_batch_solve(self._h))
+
+    def numIterations(self, i):
+        return self._lib.eik_batch_num_iterations(self._h, int(i))
+
+    def getFinalResult(self, i):
+        out = np.empty(self._lib.eik_batch_num_vertices(self._h, int(i)), dtype=np.float32)
+        self._check(self._lib.eik_batch_get_result(self._h, int(i), _fptr(out), out.size))
+        return out
+
+    def getFinalResults(self):
+        """All instances' results, split per instance."""
+        sizes = [self._lib.eik_batch_num_vertices(self._h, i) for i in range(len(self))]
+        out = np.empty(int(sum(sizes)), dtype=np.float32)
+        self._check(self._lib.eik_batch_get_results(self._h, _fptr(out), out.size))
+        return np.split(out, np.cumsum(sizes)[:-1])
+
+    def getResultsDevice(self, dev_ptr, n):
+        self._check(self._lib.eik_batch_get_results_device(self._h, ctypes.c_void_p(dev_ptr), int(n)))
+
+    def stream(self):
+        p = self._lib.eik_batch_stream(self._h)
+        return p or 0
+
+    def stats(self):
+        s = EikStats()
+        self._check(self._lib.eik_batch_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
 
 
 def selftest_local_update(which, inputs):

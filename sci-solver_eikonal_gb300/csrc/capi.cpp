@@ -136,6 +136,64 @@ int host_prepare(eik_solver* h, bool* new_layout_out) {
   return EIK_OK;
 }
 
+// Seeds and initial values as the reference derives them (src/Eikonal.cu:143-159,
+// 186-202): vertices the user's initial values set to 0, else the explicit seed
+// list, else vertex 0.  3D ignores initial values like the reference.
+int resolve_seeds(eik_solver* h, std::vector<int>& seeds, const float** init) {
+  seeds.clear();
+  *init = nullptr;
+  if (h->user_initial) {
+    for (int v = 0; v < h->nv; ++v)
+      if (h->init_vals[v] == 0.) seeds.push_back(v);
+    if (h->dim == 2) *init = h->init_vals.data();
+  } else if (h->user_seeds) {
+    seeds = h->seeds;
+  } else {
+    seeds.push_back(0);
+  }
+  for (int s : seeds)
+    if (s >= h->nv) return fail(h, EIK_ERR_ARG, "seed out of range");
+  return EIK_OK;
+}
+
+SolveOptions solve_options(const eik_options& o) {
+  SolveOptions so;
+  so.max_iterations = o.max_iterations;
+  so.fim_sweeps = o.fim_sweeps;
+  so.keep_history = o.keep_history != 0;
+  so.history_cap = o.max_iterations;
+  so.direct_launch = o.direct_launch != 0;
+  if (o.threads_per_block > 0) so.threads = o.threads_per_block;
+  return so;
+}
+
+void fill_stats(eik_stats& s, const SolveStats& st, const Layout& L, float setup_ms) {
+  s.iterations = st.iterations;
+  s.num_blocks = L.nb;
+  s.vertex_updates = st.vertex_updates;
+  s.fim_visits = st.fim_visits;
+  s.check_visits = st.check_visits;
+  s.slot_visits = st.slot_visits;
+  s.halo_visits = st.halo_visits;
+  s.owned_visits = st.owned_visits;
+  s.solve_ms = st.solve_ms;
+  s.setup_ms = setup_ms;
+  s.max_slots_per_block = L.max_slots;
+  s.max_local_vertices = L.max_local;
+  s.total_slots = L.total_slots;
+  s.mean_slots_per_block = L.mean_slots_per_block;
+  s.mean_halo_per_block = L.mean_halo_per_block;
+  s.device_error = st.error;
+  s.fim_kernel_ms = st.fim_kernel_ms;
+  s.check_kernel_ms = st.check_kernel_ms;
+  s.fim_launches = st.fim_launches;
+  s.check_launches = st.check_launches;
+  s.fim_slots = st.fim_slots;
+  s.fim_halo = st.fim_halo;
+  s.fim_owned = st.fim_owned;
+  s.h2d_bytes = st.h2d_bytes;
+}
+
 }  // namespace
 
 extern "C" {
@@ -267,22 +325,12 @@ int eik_solve(eik_solver* h) {
   if (!h) return EIK_ERR_ARG;
   if (h->nv == 0) return fail(h, EIK_ERR_STATE, "no mesh: call eik_set_mesh or eik_load_mesh first");
   const auto t0 = std::chrono::steady_clock::now();
-  // seeds (src/Eikonal.cu:143-159, 186-202)
   std::vector<int> seeds;
   const float* init = nullptr;
-  if (h->user_initial) {
-    for (int v = 0; v < h->nv; ++v)
-      if (h->init_vals[v] == 0.) seeds.push_back(v);
-    init = h->init_vals.data();
-  } else if (h->user_seeds) {
-    seeds = h->seeds;
-  } else {
-    seeds.push_back(0);
-  }
-  for (int s : seeds)
-    if (s >= h->nv) return fail(h, EIK_ERR_ARG, "seed out of range");
+  int rc = resolve_seeds(h, seeds, &init);
+  if (rc) return rc;
   bool new_layout = false;
-  int rc = host_prepare(h, &new_layout);
+  rc = host_prepare(h, &new_layout);
   if (rc) return rc;
   if (!h->dev) h->dev.reset(new DeviceSolve);
   if (new_layout || !h->uploaded) {
@@ -293,17 +341,10 @@ int eik_solve(eik_solver* h) {
     }
     h->uploaded = true;
   }
-  std::string e = h->dev->set_seeds(seeds, (h->dim == 2) ? init : nullptr);
+  std::string e = h->dev->set_seeds(seeds, init);
   if (!e.empty()) return fail(h, EIK_ERR_ARG, e);
   const auto t1 = std::chrono::steady_clock::now();
-  SolveOptions so;
-  so.max_iterations = h->opt.max_iterations;
-  so.fim_sweeps = h->opt.fim_sweeps;
-  so.keep_history = h->opt.keep_history != 0;
-  so.history_cap = h->opt.max_iterations;
-  so.direct_launch = h->opt.direct_launch != 0;
-  if (h->opt.threads_per_block > 0) so.threads = h->opt.threads_per_block;
-  e = h->dev->solve(so);
+  e = h->dev->solve(solve_options(h->opt));
   if (!e.empty()) {
     h->solved = false;
     return fail(h, h->dev->stats().error ? EIK_ERR_DEVICE : EIK_ERR_CUDA, e);
@@ -311,30 +352,7 @@ int eik_solve(eik_solver* h) {
   h->solved = true;
   const SolveStats& st = h->dev->stats();
   eik_stats& s = h->stats;
-  s.iterations = st.iterations;
-  s.num_blocks = h->nb;
-  s.vertex_updates = st.vertex_updates;
-  s.fim_visits = st.fim_visits;
-  s.check_visits = st.check_visits;
-  s.slot_visits = st.slot_visits;
-  s.halo_visits = st.halo_visits;
-  s.owned_visits = st.owned_visits;
-  s.solve_ms = st.solve_ms;
-  s.setup_ms = std::chrono::duration<float, std::milli>(t1 - t0).count();
-  s.max_slots_per_block = h->layout.max_slots;
-  s.max_local_vertices = h->layout.max_local;
-  s.total_slots = h->layout.total_slots;
-  s.mean_slots_per_block = h->layout.mean_slots_per_block;
-  s.mean_halo_per_block = h->layout.mean_halo_per_block;
-  s.device_error = st.error;
-  s.fim_kernel_ms = st.fim_kernel_ms;
-  s.check_kernel_ms = st.check_kernel_ms;
-  s.fim_launches = st.fim_launches;
-  s.check_launches = st.check_launches;
-  s.fim_slots = st.fim_slots;
-  s.fim_halo = st.fim_halo;
-  s.fim_owned = st.fim_owned;
-  s.h2d_bytes = st.h2d_bytes;
+  fill_stats(s, st, h->layout, std::chrono::duration<float, std::milli>(t1 - t0).count());
   if (h->opt.verbose) {
     std::printf("Eikonal GB300: %d blocks, %d iterations, %.3f ms solve, %.3f ms setup\n", h->nb, st.iterations,
                 st.solve_ms, s.setup_ms);
@@ -477,6 +495,156 @@ int eik_solve3d_noalloc(const float* xyz, int nv, const int* tets, int nt, const
   if (iterations) *iterations = it;
   return EIK_OK;
 }
+
+// ---- batches ----------------------------------------------------------------
+
+struct eik_batch {
+  std::vector<eik_solver*> solvers;
+  std::vector<std::string> keys;  // per handle: layout identity at pack time
+  Layout layout;
+  std::unique_ptr<DeviceSolve> dev;
+  bool packed = false, solved = false, have_host = false;
+  std::vector<float> host_result;
+  std::vector<int> iters;
+  eik_stats stats{};
+  std::string err;
+};
+
+namespace {
+
+int bfail(eik_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+std::string layout_identity(const eik_solver* h) {
+  return std::to_string(h->lay_mesh) + "/" + h->lay_key + "/" + std::to_string(h->lay_speed);
+}
+
+}  // namespace
+
+int eik_batch_create(eik_solver* const* solvers, int n, eik_batch** out) {
+  if (!out || !solvers || n <= 0) return EIK_ERR_ARG;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!solvers[i]) return EIK_ERR_ARG;
+    if (solvers[i]->dim != solvers[0]->dim) return fail(solvers[i], EIK_ERR_ARG, "batch mixes 2D and 3D handles");
+  }
+  eik_batch* b = new eik_batch;
+  b->solvers.assign(solvers, solvers + n);
+  *out = b;
+  return EIK_OK;
+}
+
+void eik_batch_destroy(eik_batch* b) { delete b; }
+
+int eik_batch_solve(eik_batch* b) {
+  if (!b) return EIK_ERR_ARG;
+  const auto t0 = std::chrono::steady_clock::now();
+  const int n = (int)b->solvers.size();
+  std::vector<std::vector<int>> seeds(n);
+  std::vector<const float*> init(n, nullptr);
+  bool repack = !b->packed || (int)b->keys.size() != n;
+  b->keys.resize(n);
+  for (int i = 0; i < n; ++i) {
+    eik_solver* h = b->solvers[i];
+    if (h->nv == 0) return bfail(b, EIK_ERR_STATE, "instance " + std::to_string(i) + ": no mesh");
+    int rc = resolve_seeds(h, seeds[i], &init[i]);
+    if (rc) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
+    bool nl = false;
+    rc = host_prepare(h, &nl);
+    if (rc) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
+    const std::string key = layout_identity(h);
+    if (key != b->keys[i]) repack = true;
+    b->keys[i] = key;
+  }
+  if (repack) {
+    b->packed = false;
+    std::vector<const Layout*> parts(n);
+    for (int i = 0; i < n; ++i) parts[i] = &b->solvers[i]->layout;
+    std::string e = concat_layouts(parts, b->layout);
+    if (!e.empty()) return bfail(b, EIK_ERR_ARG, e);
+    if (!b->dev) b->dev.reset(new DeviceSolve);
+    e = b->dev->upload(b->layout);
+    if (!e.empty()) return bfail(b, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+    b->packed = true;
+  }
+  std::string e = b->dev->set_seeds_multi(seeds, init);
+  if (!e.empty()) return bfail(b, EIK_ERR_ARG, e);
+  const auto t1 = std::chrono::steady_clock::now();
+  SolveOptions so = solve_options(b->solvers[0]->opt);
+  so.keep_history = false;
+  so.inst_max_iterations.resize(n);
+  for (int i = 0; i < n; ++i) so.inst_max_iterations[i] = b->solvers[i]->opt.max_iterations;
+  b->solved = false;
+  b->have_host = false;
+  e = b->dev->solve(so);
+  if (!e.empty()) return bfail(b, b->dev->stats().error ? EIK_ERR_DEVICE : EIK_ERR_CUDA, e);
+  b->solved = true;
+  b->iters = b->dev->stats().inst_iters;
+  fill_stats(b->stats, b->dev->stats(), b->layout, std::chrono::duration<float, std::milli>(t1 - t0).count());
+  return EIK_OK;
+}
+
+int eik_batch_num_instances(const eik_batch* b) { return b ? (int)b->solvers.size() : 0; }
+
+int eik_batch_num_vertices(const eik_batch* b, int i) {
+  if (!b || i < 0 || i >= (int)b->solvers.size()) return 0;
+  return b->solvers[i]->nv;
+}
+
+int eik_batch_num_iterations(const eik_batch* b, int i) {
+  if (!b || !b->solved || i < 0 || i >= (int)b->iters.size()) return 0;
+  return b->iters[i];
+}
+
+int eik_batch_get_results(eik_batch* b, float* out, long long n) {
+  if (!b || !out) return EIK_ERR_ARG;
+  if (!b->solved) return bfail(b, EIK_ERR_STATE, "no batch solve yet");
+  if (n != b->layout.nv) return bfail(b, EIK_ERR_ARG, "size mismatch");
+  if (!b->have_host) {
+    b->host_result.resize(b->layout.nv);
+    std::string e = b->dev->result(b->host_result.data());
+    if (!e.empty()) return bfail(b, EIK_ERR_CUDA, e);
+    b->have_host = true;
+  }
+  std::memcpy(out, b->host_result.data(), sizeof(float) * (size_t)n);
+  return EIK_OK;
+}
+
+int eik_batch_get_result(eik_batch* b, int i, float* out, int nv) {
+  if (!b || !out || i < 0 || i >= (int)b->solvers.size()) return EIK_ERR_ARG;
+  if (!b->solved) return bfail(b, EIK_ERR_STATE, "no batch solve yet");
+  const int v0 = b->layout.inst_vbeg[i], cnt = b->layout.inst_vbeg[i + 1] - v0;
+  if (nv != cnt) return bfail(b, EIK_ERR_ARG, "size mismatch");
+  if (!b->have_host) {
+    b->host_result.resize(b->layout.nv);
+    std::string e = b->dev->result(b->host_result.data());
+    if (!e.empty()) return bfail(b, EIK_ERR_CUDA, e);
+    b->have_host = true;
+  }
+  std::memcpy(out, b->host_result.data() + v0, sizeof(float) * (size_t)cnt);
+  return EIK_OK;
+}
+
+int eik_batch_get_results_device(eik_batch* b, float* out_dev, long long n) {
+  if (!b || !out_dev) return EIK_ERR_ARG;
+  if (!b->solved) return bfail(b, EIK_ERR_STATE, "no batch solve yet");
+  if (n != b->layout.nv) return bfail(b, EIK_ERR_ARG, "size mismatch");
+  std::string e = b->dev->result_device(out_dev);
+  if (!e.empty()) return bfail(b, EIK_ERR_CUDA, e);
+  return EIK_OK;
+}
+
+int eik_batch_get_stats(const eik_batch* b, eik_stats* s) {
+  if (!b || !s) return EIK_ERR_ARG;
+  *s = b->stats;
+  return EIK_OK;
+}
+
+void* eik_batch_stream(const eik_batch* b) { return (b && b->dev) ? b->dev->stream() : nullptr; }
+
+const char* eik_batch_last_error(const eik_batch* b) { return b ? b->err.c_str() : "null handle"; }
 
 void* eik_stream(const eik_solver* h) { return (h && h->dev) ? h->dev->stream() : nullptr; }
 

@@ -36,6 +36,7 @@ struct SolveStats {
   float check_kernel_ms = 0.0f;  // same for the neighbour-check kernel
   int fim_launches = 0, check_launches = 0;
   long long h2d_bytes = 0;       // host-to-device bytes the last solve copied (initial state)
+  std::vector<int> inst_iters;   // outer iterations run by every instance
 };
 
 struct SolveOptions {
@@ -45,6 +46,7 @@ struct SolveOptions {
   int history_cap = 0;       // snapshots kept when keep_history
   int threads = 0;           // CTA size of the 3D visit kernels (0: from the largest block)
   bool direct_launch = false; // launch the loop body kernel by kernel (for profilers)
+  std::vector<int> inst_max_iterations;  // per instance; empty: max_iterations for all
 };
 
 class DeviceSolve {
@@ -61,6 +63,9 @@ class DeviceSolve {
   // Seeds are original vertex ids.  init_vals (2D only, may be null) are the
   // vertex values the reference's all-vertex convergence test starts from.
   std::string set_seeds(const std::vector<int>& seeds_orig, const float* init_vals);
+  // Several instances (a layout from concat_layouts): per instance its seeds
+  // (vertex ids of that instance) and optional initial values.
+  std::string set_seeds_multi(const std::vector<std::vector<int>>& seeds, const std::vector<const float*>& init_vals);
   // Runs the solve to completion on the solver's stream.
   std::string solve(const SolveOptions& opt);
   // Final travel times in original vertex order.

@@ -91,6 +91,16 @@ struct DevArgs {
   int max_slots_pad, max_local, max_owned;
   cudaGraphConditionalHandle cond;
   int use_cond;  // 1 inside the CUDA graph, 0 for direct launches
+  // independent instances (a single solve is one): per block its instance, per
+  // instance finished flag, iterations run, blocks queued for the next iteration,
+  // and (2D) a vertex that failed the all-vertex test this iteration
+  const int* blk_inst;
+  int* inst_done;
+  int* inst_iters;
+  int* inst_nnext;
+  const int* inst_maxit;  // iteration cap of every instance
+  int* inst_fail;
+  int ninst;
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -251,6 +261,10 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
     const int item = s_item;
     if (item >= count) break;
     const int b = list[item];
+    if (a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
+      __syncthreads();
+      continue;
+    }
     const BlockDesc bd = a.blocks[b];
     Smem s = s0;
     const bool ok = load_block(a, bd, 6, s, &bar, parity, a.Ta);
@@ -364,7 +378,10 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
         if (!allc) a.stampA[b] = stamp;
         atomicAdd(&a.ctl->fim_visits, 1ull);
       } else {
-        if (!allc) nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+        if (!allc) {
+          nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+          atomicAdd(&a.inst_nnext[a.blk_inst[b]], 1);
+        }
         atomicAdd(&a.ctl->chk_visits, 1ull);
       }
       atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
@@ -414,6 +431,10 @@ __global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
     const int item = s_item;
     if (item >= count) break;
     const int b = (item < nact) ? act[item] : a.list_new[item - nact];
+    if (a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
+      __syncthreads();
+      continue;
+    }
     const BlockDesc bd = a.blocks[b];
     Smem s = s0;
     const bool ok = load_block(a, bd, 4, s, &bar, parity, Tsrc);
@@ -515,6 +536,7 @@ __global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
       } else {
         if (!allc) {
           nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+          atomicAdd(&a.inst_nnext[a.blk_inst[b]], 1);
           a.stampA[b] = stamp + 1;  // member of the next iteration's active list
         }
         atomicAdd(&a.ctl->chk_visits, 1ull);
@@ -579,6 +601,10 @@ __global__ void __launch_bounds__(1024) k_visit2d_slot(DevArgs a) {
     const int item = s_item;
     if (item >= count) break;
     const int b = (item < nact) ? act[item] : a.list_new[item - nact];
+    if (a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
+      __syncthreads();
+      continue;
+    }
     const BlockDesc bd = a.blocks[b];
     const bool ok = load_block(a, bd, 4, sv, &bar, parity, Tsrc);
     if (!ok) {
@@ -684,6 +710,7 @@ __global__ void __launch_bounds__(1024) k_visit2d_slot(DevArgs a) {
       } else {
         if (!allc) {
           nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+          atomicAdd(&a.inst_nnext[a.blk_inst[b]], 1);
           a.stampA[b] = stamp + 1;
         }
         atomicAdd(&a.ctl->chk_visits, 1ull);
@@ -721,6 +748,7 @@ __global__ void k_commit3d(DevArgs a) {
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= count) break;
     const int b = act[item];
+    if (a.inst_done[a.blk_inst[b]]) continue;
     const BlockDesc bd = a.blocks[b];
     for (int k = lane; k < bd.nowned; k += 32) a.Ta[bd.vbase + k] = a.Tb[bd.vbase + k];
     if (lane == 0) a.visited[b] = 1;
@@ -732,6 +760,7 @@ __global__ void k_commit3d(DevArgs a) {
       }
     } else if (lane == 0) {
       nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+      atomicAdd(&a.inst_nnext[a.blk_inst[b]], 1);
     }
   }
 }
@@ -748,7 +777,7 @@ __global__ void k_activate2d(DevArgs a) {
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= count) break;
     const int b = act[item];
-    if (!a.conv[b]) continue;
+    if (a.inst_done[a.blk_inst[b]] || !a.conv[b]) continue;
     for (int e = a.nbr_off[b] + lane; e < a.nbr_off[b + 1]; e += 32) {
       const int nb = a.nbr[e];
       if (a.stampA[nb] != stamp && atomicExch(&a.stampC[nb], stamp) != stamp)
@@ -757,19 +786,38 @@ __global__ void k_activate2d(DevArgs a) {
   }
 }
 
-// End of an outer iteration (run by the last CTA of the iteration's last kernel).
-__device__ void finish_iteration(const DevArgs& a, bool all_vertices_converged) {
+// End of an outer iteration, run by all threads of one CTA: every running
+// instance counts the iteration and stops when its next active list is empty, its
+// iteration cap is reached, or (2D) every vertex passed the all-vertex test
+// (the loop conditions of meshFIM3dEikonal.cu:411-417 / meshFIM2d_eikonal.cu:683-690,
+// 813-815); the loop goes on while any instance runs.
+__device__ void finish_iteration_cta(const DevArgs& a, bool vertex_test) {
   Ctl* c = a.ctl;
-  c->iter += 1;
-  c->nact = c->nnext;
-  c->nnext = 0;
-  c->nnew = 0;
-  c->work_a = c->work_b = c->work_c = c->work_d = 0;
-  c->done_c = c->done_d = 0;
-  c->conv_fail = 0;
-  const bool go = c->nact > 0 && c->iter < c->max_iters && !all_vertices_converged && c->error == 0;
-  c->stop = go ? 0 : 1;
-  if (a.use_cond) cudaGraphSetConditional(a.cond, go ? 1u : 0u);
+  const int it = c->iter + 1;
+  int any = 0;
+  for (int i = threadIdx.x; i < a.ninst; i += blockDim.x) {
+    if (!a.inst_done[i]) {
+      a.inst_iters[i] = it;
+      const bool stop = a.inst_nnext[i] == 0 || it >= a.inst_maxit[i] || (vertex_test && a.inst_fail[i] == 0);
+      if (stop) a.inst_done[i] = 1;
+      else any = 1;
+    }
+    a.inst_nnext[i] = 0;
+    a.inst_fail[i] = 0;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) {
+    c->iter = it;
+    c->nact = c->nnext;
+    c->nnext = 0;
+    c->nnew = 0;
+    c->work_a = c->work_b = c->work_c = c->work_d = 0;
+    c->done_c = c->done_d = 0;
+    c->conv_fail = 0;
+    const bool go = any && c->error == 0;
+    c->stop = go ? 0 : 1;
+    if (a.use_cond) cudaGraphSetConditional(a.cond, go ? 1u : 0u);
+  }
 }
 
 // last-CTA detection without any waiting: every CTA bumps the counter once
@@ -787,29 +835,21 @@ __device__ __forceinline__ bool last_cta(int* counter) {
 
 // 2D all-vertex convergence test (meshFIM2d_eikonal.cu:804-815) + iteration close
 __global__ void k_vertex_test2d(DevArgs a) {
-  int fail = 0;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x) {
+    const int inst = a.blk_inst[a.vblock[v]];
+    if (a.inst_done[inst]) continue;
     const float cur = a.Ta[v];
     float diff = a.prev[v] - cur;
     if (diff < 0.0f) diff = -diff;
     const bool ok = (diff <= kEps2D) && (cur < kLarge2DDev);
-    fail |= ok ? 0 : 1;
+    if (!ok && a.inst_fail[inst] == 0) atomicOr(&a.inst_fail[inst], 1);
     a.prev[v] = cur;
   }
-  fail = __syncthreads_or(fail);
-  if (threadIdx.x == 0 && fail) atomicOr(&a.ctl->conv_fail, 1);
-  if (last_cta(&a.ctl->done_d)) {
-    if (threadIdx.x == 0) {
-      const bool allc = (atomicAdd(&a.ctl->conv_fail, 0) == 0);
-      finish_iteration(a, allc);
-    }
-  }
+  if (last_cta(&a.ctl->done_d)) finish_iteration_cta(a, true);
 }
 
 // 3D close: a tiny single-CTA kernel after the check visits.
-__global__ void k_close3d(DevArgs a) {
-  if (threadIdx.x == 0) finish_iteration(a, false);
-}
+__global__ void k_close3d(DevArgs a) { finish_iteration_cta(a, false); }
 
 // start of a solve: set the while-condition from the initial active list
 __global__ void k_start(DevArgs a) {
@@ -909,10 +949,17 @@ struct DeviceSolve::Impl {
   unsigned long long* ktime = nullptr;
   int ktime_cap = 0;
   float* out_tmp = nullptr;
+  int* blk_inst = nullptr;
+  int* inst_done = nullptr;
+  int* inst_iters = nullptr;
+  int* inst_nnext = nullptr;
+  int* inst_fail = nullptr;
+  int* inst_maxit = nullptr;
+  int ninst = 1;
   size_t coef_n = 0;
   // host staging for the initial state
   std::vector<float> h_init, h_prev;
-  std::vector<int> h_stampA, h_act, h_vblock;
+  std::vector<int> h_stampA, h_act, h_vblock, h_done, h_maxit;
   std::vector<unsigned long long> h_ktime;
   // graph
   cudaGraph_t graph = nullptr;
@@ -935,13 +982,16 @@ struct DeviceSolve::Impl {
 
   void free_all() {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
-                  stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp};
+                  stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
+                  blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit};
     for (void* p : ps)
       if (p) cudaFree(p);
     blocks = nullptr; coef = nullptr; lv = nullptr; halo = nullptr; nbr_off = nullptr; nbr = nullptr;
     vblock = nullptr; perm = nullptr; Ta = nullptr; Tb = nullptr; Tinit = nullptr; prev = nullptr;
     conv = nullptr; stampA = nullptr; stampC = nullptr; visited = nullptr; list0 = nullptr;
     list1 = nullptr; list_new = nullptr; ctl = nullptr; hist = nullptr; ktime = nullptr; out_tmp = nullptr;
+    blk_inst = nullptr; inst_done = nullptr; inst_iters = nullptr; inst_nnext = nullptr; inst_fail = nullptr;
+    inst_maxit = nullptr;
     hist_cap = 0;
     ktime_cap = 0;
     drop_graph();
@@ -994,6 +1044,10 @@ std::string DeviceSolve::upload(const Layout& L) {
     if (!(e = dev_alloc(*t, (size_t)L.nb)).empty()) return e;
   if (!(e = dev_alloc(P.visited, (size_t)L.nb)).empty()) return e;
   if (!(e = dev_alloc(P.ctl, 1)).empty()) return e;
+  P.ninst = std::max(L.ninst, 1);
+  if (!(e = dev_alloc(P.blk_inst, (size_t)L.nb)).empty()) return e;
+  for (int** t : {&P.inst_done, &P.inst_iters, &P.inst_nnext, &P.inst_fail, &P.inst_maxit})
+    if (!(e = dev_alloc(*t, (size_t)P.ninst)).empty()) return e;
   cudaStream_t st = (cudaStream_t)stream_;
   CK(cudaMemcpyAsync(P.blocks, L.blocks.data(), sizeof(BlockDesc) * L.nb, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(P.coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice, st));
@@ -1009,6 +1063,9 @@ std::string DeviceSolve::upload(const Layout& L) {
     for (int k = 0; k < L.blocks[b].nowned; ++k) vb[L.blocks[b].vbase + k] = b;
   CK(cudaMemcpyAsync(P.vblock, vb.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(P.perm, L.perm.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  std::vector<int> bi(L.blk_inst);
+  if ((int)bi.size() != L.nb) bi.assign(L.nb, 0);
+  CK(cudaMemcpyAsync(P.blk_inst, bi.data(), sizeof(int) * L.nb, cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));
   P.coef_n = L.coef.size();
   P.max_slots_pad = (L.max_slots + 3) & ~3;
@@ -1034,27 +1091,42 @@ std::string DeviceSolve::upload_coef(const Layout& L) {
 }
 
 std::string DeviceSolve::set_seeds(const std::vector<int>& seeds, const float* init_vals) {
+  return set_seeds_multi(std::vector<std::vector<int>>(1, seeds), std::vector<const float*>(1, init_vals));
+}
+
+std::string DeviceSolve::set_seeds_multi(const std::vector<std::vector<int>>& seeds,
+                                         const std::vector<const float*>& init_vals) {
   Impl& P = *p_;
   if (!L_) return "no layout uploaded";
   const Layout& L = *L_;
+  const int ninst = std::max(L.ninst, 1);
+  if ((int)seeds.size() != ninst) return "one seed list per instance expected";
   const float large = (L.dim == 3) ? kLarge3D : kLarge2D;
   P.h_init.assign(L.nv, large);
+  P.h_prev.assign(L.nv, large);
   std::vector<char> act(L.nb, 0);
-  for (int s : seeds) {
-    if (s < 0 || s >= L.nv) return "seed vertex out of range";
-    P.h_init[L.perm[s]] = 0.0f;
-    act[P.h_vblock[L.perm[s]]] = 1;
+  P.h_done.assign(ninst, 1);
+  for (int i = 0; i < ninst; ++i) {
+    const int v0 = (L.ninst > 1) ? L.inst_vbeg[i] : 0;
+    const int nvi = (L.ninst > 1) ? L.inst_vbeg[i + 1] - v0 : L.nv;
+    for (int s : seeds[i]) {
+      if (s < 0 || s >= nvi) return "seed vertex out of range";
+      const int r = L.perm[v0 + s];
+      P.h_init[r] = 0.0f;
+      act[P.h_vblock[r]] = 1;
+      P.h_done[i] = 0;
+    }
+    // the reference's TriMesh::vertT: user values, or 0 at seeds and LARGENUM elsewhere
+    const float* iv = (i < (int)init_vals.size()) ? init_vals[i] : nullptr;
+    if (iv) {
+      for (int v = 0; v < nvi; ++v) P.h_prev[L.perm[v0 + v]] = iv[v];
+    } else {
+      for (int s : seeds[i]) P.h_prev[L.perm[v0 + s]] = 0.0f;
+    }
   }
   P.h_act.clear();
   for (int b = 0; b < L.nb; ++b)
     if (act[b]) P.h_act.push_back(b);
-  // the reference's TriMesh::vertT: user values, or 0 at seeds and LARGENUM elsewhere
-  P.h_prev.assign(L.nv, large);
-  if (init_vals) {
-    for (int v = 0; v < L.nv; ++v) P.h_prev[L.perm[v]] = init_vals[v];
-  } else {
-    for (int s : seeds) P.h_prev[L.perm[s]] = 0.0f;
-  }
   P.h_stampA.assign(L.nb, 0);
   if (L.dim == 2)
     for (int b : P.h_act) P.h_stampA[b] = 1;
@@ -1075,6 +1147,11 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   const int threads = (opt.threads == 128 || opt.threads == 256 || opt.threads == 512 || opt.threads == 1024)
                           ? opt.threads
                           : auto_threads;
+  // per-instance iteration caps (one cap for all when not given)
+  std::vector<int> cap(P.ninst, opt.max_iterations);
+  if ((int)opt.inst_max_iterations.size() == P.ninst) cap = opt.inst_max_iterations;
+  int max_iters = 0;
+  for (int m : cap) max_iters = std::max(max_iters, m);
   const int hcap = opt.keep_history ? std::max(0, opt.history_cap) : 0;
   if (hcap > 0 && hcap != P.hist_cap) {
     if (P.hist) cudaFree(P.hist);
@@ -1083,10 +1160,10 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     P.hist_cap = hcap;
     P.drop_graph();
   }
-  if (opt.max_iterations + 1 > P.ktime_cap) {
+  if (max_iters + 1 > P.ktime_cap) {
     if (P.ktime) cudaFree(P.ktime);
     P.ktime = nullptr;
-    P.ktime_cap = opt.max_iterations + 1;
+    P.ktime_cap = max_iters + 1;
     CK(cudaMalloc((void**)&P.ktime, sizeof(unsigned long long) * 4 * (size_t)P.ktime_cap));
     P.drop_graph();
   }
@@ -1107,12 +1184,23 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   CK(cudaMemsetAsync(P.stampC, 0, sizeof(int) * L.nb, st));
   CK(cudaMemsetAsync(P.visited, 0, L.nb, st));
   CK(cudaMemsetAsync(P.conv, 0, sizeof(int) * L.nb, st));
+  {
+    std::vector<int> done(P.h_done);
+    for (int i = 0; i < P.ninst; ++i)
+      if (cap[i] <= 0) done[i] = 1;
+    P.h_maxit = cap;
+    CK(cudaMemcpyAsync(P.inst_done, done.data(), sizeof(int) * P.ninst, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(P.inst_maxit, P.h_maxit.data(), sizeof(int) * P.ninst, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(P.inst_iters, 0, sizeof(int) * P.ninst, st));
+    CK(cudaMemsetAsync(P.inst_nnext, 0, sizeof(int) * P.ninst, st));
+    CK(cudaMemsetAsync(P.inst_fail, 0, sizeof(int) * P.ninst, st));
+  }
   if (!P.h_act.empty())
     CK(cudaMemcpyAsync(P.list0, P.h_act.data(), sizeof(int) * P.h_act.size(), cudaMemcpyHostToDevice, st));
   stats_.h2d_bytes = (long long)sizeof(unsigned long long) * P.h_ktime.size() + 4ll * sizeof(float) * L.nv +
                      (long long)sizeof(int) * L.nb + (long long)sizeof(int) * P.h_act.size() + (long long)sizeof(Ctl);
   Ctl c{};
-  c.max_iters = opt.max_iterations;
+  c.max_iters = max_iters;
   c.nact = (int)P.h_act.size();
   CK(cudaMemcpyAsync(P.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st));
 
@@ -1130,6 +1218,8 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     a.fim_sweeps = sweeps; a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local;
     a.max_owned = P.max_owned;
     a.use_cond = 1;
+    a.blk_inst = P.blk_inst; a.inst_done = P.inst_done; a.inst_iters = P.inst_iters;
+    a.inst_nnext = P.inst_nnext; a.inst_fail = P.inst_fail; a.ninst = P.ninst; a.inst_maxit = P.inst_maxit;
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
     int dev = 0, nsm = 0;
@@ -1192,7 +1282,7 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     if (L.dim == 3) {
       if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
       if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-      if (!(e = add((void*)k_close3d, 1, 32, 0, args_ptr)).empty()) return e;
+      if (!(e = add((void*)k_close3d, 1, 256, 0, args_ptr)).empty()) return e;
     } else {
       if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
       if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
@@ -1218,7 +1308,7 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
       Ctl h{};
       CK(cudaMemcpyAsync(&h, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      if (h.stop || h.error || h.nact <= 0 || h.iter >= opt.max_iterations) break;
+      if (h.stop || h.error || h.nact <= 0 || h.iter >= max_iters) break;
       for (const Impl::Launch& l : P.body) {
         void* args[2] = {&d, (void*)&l.extra};
         CK(cudaLaunchKernel(l.func, dim3(l.grid), dim3(l.block), args, l.smem, st));
@@ -1241,6 +1331,8 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   stats_.halo_visits = (long long)out.halo_visits;
   stats_.owned_visits = (long long)out.owned_visits;
   stats_.error = out.error;
+  stats_.inst_iters.assign(P.ninst, 0);
+  CK(cudaMemcpy(stats_.inst_iters.data(), P.inst_iters, sizeof(int) * P.ninst, cudaMemcpyDeviceToHost));
   stats_.fim_slots = (long long)out.fim_slots;
   stats_.fim_halo = (long long)out.fim_halo;
   stats_.fim_owned = (long long)out.fim_owned;
@@ -1312,6 +1404,9 @@ std::string DeviceSolve::visit_once(bool check, const float* T_host, float* out_
   a.vblock = P.vblock; a.nb = L.nb; a.nv = L.nv; a.Ta = P.Ta; a.Tb = P.Tb; a.Tinit = P.Tinit; a.prev = P.prev;
   a.conv = P.conv; a.stampA = P.stampA; a.stampC = P.stampC; a.visited = P.visited; a.list0 = P.list0;
   a.list1 = P.list1; a.list_new = P.list_new; a.ctl = P.ctl; a.fim_sweeps = (L.dim == 3) ? 2 : 7;
+  a.blk_inst = P.blk_inst; a.inst_done = P.inst_done; a.inst_iters = P.inst_iters;
+  a.inst_nnext = P.inst_nnext; a.inst_fail = P.inst_fail; a.ninst = P.ninst;
+  CK(cudaMemsetAsync(P.inst_done, 0, sizeof(int) * P.ninst, st));
   a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local; a.max_owned = P.max_owned;
   int dev = 0, nsm = 0;
   CK(cudaGetDevice(&dev));
@@ -1473,6 +1568,8 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
     for (int k = 0; k < 6; ++k) carve_scratch<int>(z, need, L.nb);          // conv, stamps, lists
     carve_scratch<unsigned char>(z, need, L.nb);                            // visited
     carve_scratch<Ctl>(z, need, 1);
+    carve_scratch<int>(z, need, L.nb);                                      // block -> instance
+    carve_scratch<int>(z, need, 4);                                         // instance control
   }
   if (bytes_needed) *bytes_needed = need;
   if (need > kNoAllocScratchBytes)
@@ -1511,6 +1608,8 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
   int* list_new = carve_scratch<int>(base, off, L.nb);
   unsigned char* visited = carve_scratch<unsigned char>(base, off, L.nb);
   Ctl* ctl = carve_scratch<Ctl>(base, off, 1);
+  int* blk_inst = carve_scratch<int>(base, off, L.nb);
+  int* inst_ctl = carve_scratch<int>(base, off, 4);
 
   // inputs into the scratch array; everything that must start at zero is cleared
   // here because the array keeps the previous call's contents
@@ -1541,6 +1640,8 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
   CK(cudaMemsetAsync(stampA, 0, sizeof(int) * L.nb, st));
   CK(cudaMemsetAsync(stampC, 0, sizeof(int) * L.nb, st));
   CK(cudaMemsetAsync(visited, 0, L.nb, st));
+  CK(cudaMemsetAsync(blk_inst, 0, sizeof(int) * L.nb, st));
+  CK(cudaMemsetAsync(inst_ctl, 0, sizeof(int) * 4, st));
   if (!alist.empty()) CK(cudaMemcpyAsync(list0, alist.data(), sizeof(int) * alist.size(), cudaMemcpyHostToDevice, st));
   Ctl c{};
   c.max_iters = max_iters;
@@ -1552,6 +1653,8 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
   a.conv = conv; a.stampA = stampA; a.stampC = stampC; a.visited = visited; a.list0 = list0; a.list1 = list1;
   a.list_new = list_new; a.ctl = ctl; a.hist = nullptr; a.hist_cap = 0; a.ktime = nullptr; a.ktime_cap = 0;
   a.fim_sweeps = 2; a.max_slots_pad = max_slots_pad; a.max_local = max_local; a.max_owned = max_owned;
+  a.blk_inst = blk_inst; a.inst_done = inst_ctl; a.inst_iters = inst_ctl + 1; a.inst_nnext = inst_ctl + 2;
+  a.inst_fail = inst_ctl + 3; a.ninst = 1;
   CK(cudaFuncSetAttribute((const void*)k_visit3d<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   CK(cudaFuncSetAttribute((const void*)k_visit3d<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 0;

@@ -365,6 +365,13 @@ void renumber(int nv, const int* labels, int nb, Layout& L, std::vector<int>& vb
   }
 }
 
+void single_instance(Layout& L) {
+  L.ninst = 1;
+  L.blk_inst.assign(L.nb, 0);
+  L.inst_bbeg = {0, L.nb};
+  L.inst_vbeg = {0, L.nv};
+}
+
 void finish_stats(Layout& L) {
   L.max_slots = L.max_local = L.max_owned = L.max_halo = 0;
   double s = 0, h = 0;
@@ -490,6 +497,7 @@ std::string build_layout3d(int nv, const float* xyz, int nt, const int* tets, co
   }
   refresh_gram3d(xyz, tets, M, L);
   finish_stats(L);
+  single_instance(L);
   return "";
 }
 
@@ -622,6 +630,7 @@ std::string build_layout2d(int nv, const float* xyz, const TriPrep& P, const flo
   }
   refresh_speed2d(P, speed_inv, L);
   finish_stats(L);
+  single_instance(L);
   return "";
 }
 
@@ -641,6 +650,48 @@ void refresh_speed2d(const TriPrep& P, const float* speed_inv, Layout& L) {
       base[3 * np + j] = F;
     }
   }
+}
+
+std::string concat_layouts(const std::vector<const Layout*>& parts, Layout& out) {
+  out = Layout();
+  if (parts.empty()) return "no instances";
+  const int dim = parts[0]->dim;
+  out.dim = dim;
+  out.inst_bbeg.push_back(0);
+  out.inst_vbeg.push_back(0);
+  for (const Layout* p : parts) {
+    if (p->dim != dim) return "instances of different dimension";
+    const int boff = out.nb, voff = out.nv, soff = out.total_slots, hoff = (int)out.halo_ids.size();
+    const int noff = (int)out.nbr.size();
+    for (int v : p->perm) out.perm.push_back(v + voff);
+    for (int v : p->iperm) out.iperm.push_back(v + voff);
+    for (BlockDesc d : p->blocks) {
+      d.slot_begin += soff;
+      d.vbase += voff;
+      d.halo_begin += hoff;
+      out.blocks.push_back(d);
+    }
+    out.coef.insert(out.coef.end(), p->coef.begin(), p->coef.end());
+    out.lv.insert(out.lv.end(), p->lv.begin(), p->lv.end());
+    for (int e : p->slot_elem) out.slot_elem.push_back(e);
+    for (int h : p->halo_ids) out.halo_ids.push_back(h + voff);
+    if (out.nbr_off.empty()) out.nbr_off.push_back(0);
+    for (int b = 0; b < p->nb; ++b) out.nbr_off.push_back(p->nbr_off[b + 1] + noff);
+    for (int n : p->nbr) out.nbr.push_back(n + boff);
+    out.nb += p->nb;
+    out.nv += p->nv;
+    out.ne += p->ne;
+    out.total_slots += p->total_slots;
+    out.inst_bbeg.push_back(out.nb);
+    out.inst_vbeg.push_back(out.nv);
+  }
+  out.ninst = (int)parts.size();
+  // instance of every block from the block ranges
+  out.blk_inst.assign(out.nb, 0);
+  for (int i = 0; i < out.ninst; ++i)
+    for (int b = out.inst_bbeg[i]; b < out.inst_bbeg[i + 1]; ++b) out.blk_inst[b] = i;
+  finish_stats(out);
+  return "";
 }
 
 }  // namespace eikgb

@@ -100,7 +100,17 @@ struct Layout {
   std::vector<int> halo_ids;      // renumbered ids of halo vertices, per block
   std::vector<int> nbr_off, nbr;  // block neighbour graph (sorted)
   double mean_slots_per_block = 0, mean_halo_per_block = 0;
+  // independent solves packed together (a single mesh is one instance): blocks and
+  // renumbered vertices of instance i are [inst_bbeg[i], inst_bbeg[i+1]) and
+  // [inst_vbeg[i], inst_vbeg[i+1]); original vertex ids are per instance
+  int ninst = 1;
+  std::vector<int> blk_inst;      // instance of every block
+  std::vector<int> inst_bbeg, inst_vbeg;
 };
+
+// One layout holding several independent meshes (same dimension), instance by
+// instance; the neighbour graph never crosses instances.
+std::string concat_layouts(const std::vector<const Layout*>& parts, Layout& out);
 
 // 3D layout; gram terms computed from xyz and per-tet metrics.
 std::string build_layout3d(int nv, const float* xyz, int nt, const int* tets, const float* M,

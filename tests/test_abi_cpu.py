@@ -167,3 +167,20 @@ def test_file_readers_match_arrays(eik, golden, tmp_path):
     fc, oc, vc, wc = c.triPrep()
     fd, od, vd, wd = d.triPrep()
     assert np.array_equal(fc, fd) and np.array_equal(oc, od) and np.array_equal(wc, wd)
+
+
+def test_batch_rejects_mixed_dimensions_and_empty(eik, mg):
+    xyz, faces = mg.icosphere(1)
+    a = eik.Eikonal(True)
+    a.set_mesh(xyz, faces)
+    xyz3, tets = mg.kuhn_cube(5, 0.2, seed=1)
+    c = eik.Eikonal(False)
+    c.set_mesh(xyz3, tets)
+    with pytest.raises(eik.EikonalError):
+        eik.EikonalBatch([a, c])
+    with pytest.raises(ValueError):
+        eik.EikonalBatch([])
+    b = eik.EikonalBatch([a, a])
+    assert len(b) == 2 and b.numIterations(0) == 0
+    with pytest.raises(eik.EikonalError):
+        b.getFinalResult(0)  # nothing solved yet

@@ -1,0 +1,106 @@
+"""Batched solves (eik_batch_*): every instance of a batch must equal, bit for bit,
+the solve of its handle alone, with the same iteration count.  The batch has no
+counterpart in the reference (src/Eikonal.cu solves one mesh per object); the
+standalone solve it is held to is the one the other GPU tests pin against the
+reference's own kernels."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def _cube_solver(eik, mg, n, seed, seeds, vpb=64, max_iters=100):
+    xyz, tets = mg.kuhn_cube(n, 0.2, seed=seed)
+    speed = mg.log_uniform_speeds(tets.shape[0], seed=seed + 100)
+    e = eik.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.initSpeedMtxMultipliers((1.0 / speed.astype(np.float64) ** 2).astype(np.float32))
+    e.setSeeds(list(seeds))
+    e.maxVertsPerBlock_ = vpb
+    e.maxIterations_ = max_iters
+    return e
+
+
+def _sphere_solver(eik, mg, level, seeds, vpb=32, max_iters=100):
+    xyz, faces = mg.icosphere(level)
+    e = eik.Eikonal(True)
+    e.set_mesh(xyz, faces)
+    e.initSpeedMtxMultipliers(mg.batch_speed(xyz, faces))
+    e.setSeeds(list(seeds))
+    e.maxVertsPerBlock_ = vpb
+    e.maxIterations_ = max_iters
+    return e
+
+
+def _alone(e):
+    e.solveEikonal()
+    return e.getFinalResult(), e.numIterations()
+
+
+def test_batch3d_equals_standalone(need_gpu, eik, mg):
+    rng = np.random.default_rng(11)
+    specs = [(9, 1), (13, 2), (7, 3), (17, 4), (11, 5)]
+    solvers = []
+    for n, sd in specs:
+        seeds = rng.choice(n ** 3, size=int(rng.integers(1, 4)), replace=False)
+        solvers.append(_cube_solver(eik, mg, n, sd, seeds))
+    want = [_alone(e) for e in solvers]
+    b = eik.EikonalBatch(solvers)
+    b.solveEikonal()
+    for i, (res, it) in enumerate(want):
+        assert b.numIterations(i) == it, (i, b.numIterations(i), it)
+        assert bits_equal(b.getFinalResult(i), res), i
+    got = b.getFinalResults()
+    for i, (res, _) in enumerate(want):
+        assert bits_equal(got[i], res), i
+    st = b.stats()
+    assert st["iterations"] == max(it for _, it in want)
+
+
+def test_batch2d_equals_standalone(need_gpu, eik, mg):
+    rng = np.random.default_rng(12)
+    levels = [1, 3, 2, 4, 2, 1]
+    solvers = []
+    for lv in levels:
+        nv = 10 * 4 ** lv + 2
+        seeds = rng.choice(nv, size=int(rng.integers(1, 9)), replace=False)
+        solvers.append(_sphere_solver(eik, mg, lv, seeds))
+    want = [_alone(e) for e in solvers]
+    b = eik.EikonalBatch(solvers)
+    b.solveEikonal()
+    for i, (res, it) in enumerate(want):
+        assert b.numIterations(i) == it, (i, b.numIterations(i), it)
+        assert bits_equal(b.getFinalResult(i), res), i
+
+
+def test_batch_per_instance_iteration_caps(need_gpu, eik, mg):
+    caps = [3, 100, 1, 7]
+    solvers = [_cube_solver(eik, mg, 13, 20 + i, [mg.center_vertex(13)], max_iters=c) for i, c in enumerate(caps)]
+    want = [_alone(e) for e in solvers]
+    assert [it for _, it in want][0] == 3
+    b = eik.EikonalBatch(solvers)
+    b.solveEikonal()
+    for i, (res, it) in enumerate(want):
+        assert b.numIterations(i) == it
+        assert bits_equal(b.getFinalResult(i), res), i
+
+
+def test_batch_resolve_with_new_seeds_and_repeated_handle(need_gpu, eik, mg):
+    a = _sphere_solver(eik, mg, 3, [0])
+    c = _sphere_solver(eik, mg, 2, [5, 17])
+    b = eik.EikonalBatch([a, c, a])  # the same handle twice: two identical instances
+    b.solveEikonal()
+    r0 = b.getFinalResults()
+    assert bits_equal(r0[0], r0[2])
+    # new seeds are picked up without a repack; a speed change forces one
+    a.setSeeds([100, 200])
+    c.initSpeedMtxMultipliers(mg.batch_speed(*mg.icosphere(2)) * np.float32(1.5))
+    b.solveEikonal()
+    got = b.getFinalResults()
+    wa, _ = _alone(a)
+    wc, _ = _alone(c)
+    assert bits_equal(got[0], wa) and bits_equal(got[2], wa)
+    assert bits_equal(got[1], wc)
+    assert not bits_equal(got[0], r0[0])
