@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-sample-iters", type=int, default=0, help="0 = choose automatically")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="c3d", choices=["c3d", "batch"],
+                   help="c3d: the 65^3 tet solve (headline); batch: 256 icospheres, batched vs plain")
+    p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--launch", default="graph", choices=["graph", "direct"],
                    help="graph: one CUDA-graph launch per solve; direct: kernel by kernel (for ncu)")
     return p.parse_args()
@@ -179,6 +182,105 @@ def partition_host(E, xyz, tets, metric):
     return e.getPartition()
 
 
+BATCH_WORKLOAD = ("batching: 256 unit icospheres, subdivision level U{2..6} (162-40,962 verts; seed 3), "
+                  "1-8 random seeds each (seed 4), per-triangle speed 1 + 0.5 sin(3x) cos(2y) sin(z)")
+
+
+def bench_batch(args, E, torch, world, local):
+    """Batched vs plain (one solve at a time) on the icosphere batch.  Block size
+    and CTA size from the autotuner; plain solves use the same partitions, so the
+    batched results must equal them bit for bit (checked)."""
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    tune = importlib.import_module("sci-solver_eikonal_gb300.autotune")
+    work = mg.batch_workload(args.batch_count)
+    solvers = []
+    for xyz, faces, speed, seeds in work:
+        e = E.Eikonal(True)
+        e.set_mesh(xyz, faces)
+        e.initSpeedMtxMultipliers(speed)
+        e.setSeeds(seeds)
+        e.maxIterations_ = MAX_ITERS
+        solvers.append(e)
+    nv_total = sum(w[0].shape[0] for w in work)
+    t0 = time.perf_counter()
+    tuned, batch = tune.tune_batch(solvers, reps=2)
+    tune_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(batch.stream())
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # batched: device-resident (events around the solve on the batch's stream)
+    for _ in range(args.warmup):
+        batch.solveEikonal()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    times, upd, iters = [], 0, []
+    for _ in range(args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        batch.solveEikonal()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+        st = batch.stats()
+        upd += st["vertex_updates"]
+        iters.append(st["iterations"])
+    barrier()
+    clocks = sampler.stop()
+    batched_ms = statistics.median(times)
+    n = len(solvers)
+    # batched end to end: seeds in, solve, every travel time out
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        for e, w in zip(solvers, work):
+            e.setSeeds(w[3])
+        batch.solveEikonal()
+        res = batch.getFinalResults()
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t)
+    # plain: the same solves one at a time (same partitions, each its own handle)
+    plain_ms, plain_upd, plain_wall = [], 0, []
+    mismatch = 0
+    for k, e in enumerate(solvers):
+        e.solveEikonal()  # upload + graph build
+        t = time.perf_counter()
+        e.solveEikonal()
+        r = e.getFinalResult()
+        plain_wall.append(time.perf_counter() - t)
+        plain_ms.append(e.stats()["solve_ms"])
+        plain_upd += e.stats()["vertex_updates"]
+        if not np.array_equal(r.view(np.uint32), res[k].view(np.uint32)):
+            mismatch += 1
+    plain_total_ms = sum(plain_ms)
+    lat = sorted(times)
+    return {
+        "metric": METRIC, "value": n / (batched_ms * 1e-3), "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD, "instances": n, "vertices": nv_total,
+                   "verts_per_block": tuned.verts_per_block, "threads_per_block": tuned.threads_per_block,
+                   "iterations_per_step": iters[0], "l2": "inputs resident; results 11 MB",
+                   "autotune_s": round(tune_s, 2), "autotune": tuned.table},
+        "vertex_updates_per_s": (upd / args.steps) / (batched_ms * 1e-3),
+        "plain": {"solves_per_s": n / (plain_total_ms * 1e-3), "ms_total": plain_total_ms,
+                  "vertex_updates_per_s": plain_upd / (plain_total_ms * 1e-3),
+                  "e2e_solves_per_s": n / sum(plain_wall)},
+        "batched_over_plain": (n / (batched_ms * 1e-3)) / (n / (plain_total_ms * 1e-3)),
+        "bitwise_mismatches_vs_plain": mismatch,
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+        "e2e": {"value": n / statistics.median(e2e), "unit": "solves/s",
+                "h2d_bytes_per_step": int(batch.stats()["h2d_bytes"]), "d2h_bytes_per_step": 4 * nv_total},
+        "clocks": clocks,
+        "gpu_launches": int(1 + 4 * sum(iters)),
+    }
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -190,6 +292,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     E = importlib.import_module("sci-solver_eikonal_gb300")
+    if args.workload == "batch":
+        res = bench_batch(args, E, torch, world, local)
+        if rank == 0:
+            print(json.dumps(res), flush=True)
+        return 0
     xyz, tets, metric, seed = build_workload()
     e = E.Eikonal(False)
     e.set_mesh(xyz, tets)

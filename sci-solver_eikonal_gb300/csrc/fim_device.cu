@@ -852,6 +852,31 @@ __global__ void k_vertex_test2d(DevArgs a) {
 __global__ void k_close3d(DevArgs a) { finish_iteration_cta(a, false); }
 
 // start of a solve: set the while-condition from the initial active list
+// initial travel times: LARGENUM everywhere (prev too unless the caller's initial
+// values were copied in) ...
+__global__ void k_init_state(float* Ta, float* Tb, float* Tinit, float* prev, int nv, float large) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    Ta[v] = large;
+    Tb[v] = large;
+    Tinit[v] = large;
+    if (prev) prev[v] = large;
+  }
+}
+
+// ... then 0 at the seed vertices, and the starting blocks marked active (2D)
+__global__ void k_seed_state(const int* ids, int n, float* Ta, float* Tb, float* Tinit, float* prev,
+                             const int* act, int nact, int* stampA) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int v = ids[i];
+    Ta[v] = 0.0f;
+    Tb[v] = 0.0f;
+    Tinit[v] = 0.0f;
+    if (prev) prev[v] = 0.0f;
+  }
+  if (stampA)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nact; i += gridDim.x * blockDim.x) stampA[act[i]] = 1;
+}
+
 __global__ void k_start(DevArgs a) {
   if (threadIdx.x == 0) {
     const Ctl* c = a.ctl;
@@ -958,8 +983,10 @@ struct DeviceSolve::Impl {
   int ninst = 1;
   size_t coef_n = 0;
   // host staging for the initial state
-  std::vector<float> h_init, h_prev;
-  std::vector<int> h_stampA, h_act, h_vblock, h_done, h_maxit;
+  std::vector<float> h_prev;  // caller's initial values (renumbered), empty when none
+  std::vector<int> h_seed_ids, h_act, h_vblock, h_done, h_maxit;
+  int* seed_ids = nullptr;
+  size_t seed_cap = 0;
   std::vector<unsigned long long> h_ktime;
   // graph
   cudaGraph_t graph = nullptr;
@@ -983,9 +1010,11 @@ struct DeviceSolve::Impl {
   void free_all() {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
-                  blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit};
+                  blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids};
     for (void* p : ps)
       if (p) cudaFree(p);
+    seed_ids = nullptr;
+    seed_cap = 0;
     blocks = nullptr; coef = nullptr; lv = nullptr; halo = nullptr; nbr_off = nullptr; nbr = nullptr;
     vblock = nullptr; perm = nullptr; Ta = nullptr; Tb = nullptr; Tinit = nullptr; prev = nullptr;
     conv = nullptr; stampA = nullptr; stampC = nullptr; visited = nullptr; list0 = nullptr;
@@ -1102,8 +1131,11 @@ std::string DeviceSolve::set_seeds_multi(const std::vector<std::vector<int>>& se
   const int ninst = std::max(L.ninst, 1);
   if ((int)seeds.size() != ninst) return "one seed list per instance expected";
   const float large = (L.dim == 3) ? kLarge3D : kLarge2D;
-  P.h_init.assign(L.nv, large);
-  P.h_prev.assign(L.nv, large);
+  bool any_user = false;
+  for (int i = 0; i < ninst && i < (int)init_vals.size(); ++i) any_user = any_user || init_vals[i] != nullptr;
+  P.h_prev.clear();
+  if (any_user) P.h_prev.assign(L.nv, large);
+  P.h_seed_ids.clear();
   std::vector<char> act(L.nb, 0);
   P.h_done.assign(ninst, 1);
   for (int i = 0; i < ninst; ++i) {
@@ -1112,7 +1144,7 @@ std::string DeviceSolve::set_seeds_multi(const std::vector<std::vector<int>>& se
     for (int s : seeds[i]) {
       if (s < 0 || s >= nvi) return "seed vertex out of range";
       const int r = L.perm[v0 + s];
-      P.h_init[r] = 0.0f;
+      P.h_seed_ids.push_back(r);
       act[P.h_vblock[r]] = 1;
       P.h_done[i] = 0;
     }
@@ -1120,16 +1152,13 @@ std::string DeviceSolve::set_seeds_multi(const std::vector<std::vector<int>>& se
     const float* iv = (i < (int)init_vals.size()) ? init_vals[i] : nullptr;
     if (iv) {
       for (int v = 0; v < nvi; ++v) P.h_prev[L.perm[v0 + v]] = iv[v];
-    } else {
+    } else if (any_user) {
       for (int s : seeds[i]) P.h_prev[L.perm[v0 + s]] = 0.0f;
     }
   }
   P.h_act.clear();
   for (int b = 0; b < L.nb; ++b)
     if (act[b]) P.h_act.push_back(b);
-  P.h_stampA.assign(L.nb, 0);
-  if (L.dim == 2)
-    for (int b : P.h_act) P.h_stampA[b] = 1;
   return "";
 }
 
@@ -1176,11 +1205,34 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
                        cudaMemcpyHostToDevice, st));
   }
   // initial state
-  CK(cudaMemcpyAsync(P.Ta, P.h_init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.Tb, P.h_init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.Tinit, P.h_init.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.prev, P.h_prev.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.stampA, P.h_stampA.data(), sizeof(int) * L.nb, cudaMemcpyHostToDevice, st));
+  // initial state built on the device: only the seed ids, the starting blocks and
+  // (when given) the caller's initial values cross from the host
+  if (P.h_seed_ids.size() > P.seed_cap) {
+    if (P.seed_ids) cudaFree(P.seed_ids);
+    P.seed_ids = nullptr;
+    P.seed_cap = std::max<size_t>(P.h_seed_ids.size(), 64);
+    CK(cudaMalloc((void**)&P.seed_ids, sizeof(int) * P.seed_cap));
+  }
+  const float large = (L.dim == 3) ? kLarge3D : kLarge2D;
+  const bool user_prev = !P.h_prev.empty();
+  const int nseed = (int)P.h_seed_ids.size();
+  if (nseed > 0)
+    CK(cudaMemcpyAsync(P.seed_ids, P.h_seed_ids.data(), sizeof(int) * nseed, cudaMemcpyHostToDevice, st));
+  k_init_state<<<std::max(1, std::min(4096, (L.nv + 255) / 256)), 256, 0, st>>>(
+      P.Ta, P.Tb, P.Tinit, user_prev ? nullptr : P.prev, L.nv, large);
+  if (user_prev) CK(cudaMemcpyAsync(P.prev, P.h_prev.data(), sizeof(float) * L.nv, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(P.stampA, 0, sizeof(int) * L.nb, st));
+  if (!P.h_act.empty())
+    CK(cudaMemcpyAsync(P.list0, P.h_act.data(), sizeof(int) * P.h_act.size(), cudaMemcpyHostToDevice, st));
+  {
+    const int nact = (int)P.h_act.size();
+    const int n = std::max(nseed, nact);
+    if (n > 0)
+      k_seed_state<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, st>>>(
+          P.seed_ids, nseed, P.Ta, P.Tb, P.Tinit, user_prev ? nullptr : P.prev, P.list0, nact,
+          (L.dim == 2) ? P.stampA : nullptr);
+    CK(cudaGetLastError());
+  }
   CK(cudaMemsetAsync(P.stampC, 0, sizeof(int) * L.nb, st));
   CK(cudaMemsetAsync(P.visited, 0, L.nb, st));
   CK(cudaMemsetAsync(P.conv, 0, sizeof(int) * L.nb, st));
@@ -1195,10 +1247,9 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     CK(cudaMemsetAsync(P.inst_nnext, 0, sizeof(int) * P.ninst, st));
     CK(cudaMemsetAsync(P.inst_fail, 0, sizeof(int) * P.ninst, st));
   }
-  if (!P.h_act.empty())
-    CK(cudaMemcpyAsync(P.list0, P.h_act.data(), sizeof(int) * P.h_act.size(), cudaMemcpyHostToDevice, st));
-  stats_.h2d_bytes = (long long)sizeof(unsigned long long) * P.h_ktime.size() + 4ll * sizeof(float) * L.nv +
-                     (long long)sizeof(int) * L.nb + (long long)sizeof(int) * P.h_act.size() + (long long)sizeof(Ctl);
+  stats_.h2d_bytes = (long long)sizeof(unsigned long long) * P.h_ktime.size() +
+                     (long long)sizeof(float) * P.h_prev.size() + (long long)sizeof(int) * nseed +
+                     (long long)sizeof(int) * P.h_act.size() + 2ll * sizeof(int) * P.ninst + (long long)sizeof(Ctl);
   Ctl c{};
   c.max_iters = max_iters;
   c.nact = (int)P.h_act.size();

@@ -7,6 +7,8 @@
                         1,572,864 tets); interior vertices jittered by U(-0.2h, 0.2h)^3
   log_uniform_speeds    per-element speed exp(U(ln lo, ln hi))
   icosphere(level)      unit icosahedron subdivided `level` times (10*4^L + 2 vertices)
+  batch_workload(256)   the batching workload: icospheres of levels U{2..6}, 1-8
+                        seeds each, per-triangle speed 1 + 0.5 sin(3x) cos(2y) sin(z)
   sliver_cube / anisotropic_metrics   the precision workload (49^3 cube with
                         10% sliver tets and per-tet SPD metrics R diag(1,a,b) R^T)
 
@@ -69,7 +71,18 @@ def log_uniform_speeds(count, lo=0.5, hi=2.0, seed=2):
     return np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.float32)
 
 
+_ICO_CACHE = {}
+
+
 def icosphere(level):
+    """Unit icosphere: (10*4^level + 2) x 3 float32 vertices, 20*4^level x 3 int32 faces."""
+    if level not in _ICO_CACHE:
+        _ICO_CACHE[level] = _icosphere(level)
+    v, f = _ICO_CACHE[level]
+    return v.copy(), f.copy()
+
+
+def _icosphere(level):
     t = (1.0 + 5.0 ** 0.5) / 2.0
     v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
          (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
@@ -103,6 +116,22 @@ def batch_speed(xyz, faces):
     """Per-triangle speed 1 + 0.5 sin(3x) cos(2y) sin(z) at the centroid."""
     c = xyz[faces].mean(axis=1).astype(np.float64)
     return (1.0 + 0.5 * np.sin(3 * c[:, 0]) * np.cos(2 * c[:, 1]) * np.sin(c[:, 2])).astype(np.float32)
+
+
+def batch_workload(count=256, level_seed=3, seed_seed=4, lo=2, hi=6):
+    """Independent 2D solves of uneven size: per instance (xyz, faces, speeds, seeds)
+    with the icosphere level drawn uniformly from {lo..hi} (PCG64 seed level_seed),
+    1-8 distinct seed vertices (PCG64 seed seed_seed) and batch_speed speeds."""
+    rl = np.random.Generator(np.random.PCG64(level_seed))
+    rs = np.random.Generator(np.random.PCG64(seed_seed))
+    levels = rl.integers(lo, hi + 1, size=count)
+    out = []
+    for lv in levels:
+        xyz, faces = icosphere(int(lv))
+        k = int(rs.integers(1, 9))
+        seeds = np.sort(rs.choice(xyz.shape[0], size=k, replace=False)).astype(np.int32)
+        out.append((xyz, faces, batch_speed(xyz, faces), seeds))
+    return out
 
 
 def random_rotations(count, rng):
