@@ -223,6 +223,59 @@ int eik_batch_get_stats(const eik_batch* b, eik_stats* s);
 void* eik_batch_stream(const eik_batch* b);
 const char* eik_batch_last_error(const eik_batch* b);
 
+/* ---- Request server -----------------------------------------------------------
+ * No counterpart in the reference.  A server keeps a pool of meshes resident on
+ * the device and solves requests (a pool mesh, seed vertices, a global speed
+ * scale) as they arrive, with continuous batching: requests that arrive while
+ * others run are admitted between outer iterations as instance slots free up, and
+ * all admitted requests advance together in one device loop per dimension (one
+ * worker thread and CUDA stream for the 2D pool meshes, one for the 3D ones).
+ *
+ * Memory: at eik_server_start the pool meshes are laid out as slots, each a
+ * resident copy of one mesh's block layout and solver state (device_bytes per
+ * slot, reported by eik_server_mesh_info).  A mesh added with slots = 0 gets
+ * floor(share / device_bytes) slots (at least 1, at most 64), share being the
+ * HBM budget divided evenly among such meshes.  A request is admitted when a
+ * slot of its mesh is free (and, with max_inflight > 0, fewer than max_inflight
+ * requests run); it waits in arrival order otherwise.
+ *
+ * Speed scale s: 2D face speeds are multiplied by s; 3D metric entries by
+ * fl32(1 / s^2).  Each request's result equals, bit for bit, eik_solve on its
+ * mesh handle with those scaled speeds / metric and the request's seeds, and is
+ * independent of what else runs.  max_inflight = 1 gives one-at-a-time solving. */
+typedef struct eik_server eik_server;
+typedef struct {
+  long long id;       /* from eik_server_submit */
+  int mesh;           /* pool mesh id */
+  int iterations;     /* outer iterations the solve ran */
+  int status;         /* EIK_OK, or the error that ended the server */
+  double submit_s;    /* seconds since the server was created */
+  double admit_s;
+  double done_s;      /* results on the host */
+} eik_completion;
+typedef struct {
+  long long submitted, completed, queued, running;
+  long long device_bytes;  /* slots of both arenas (layouts + state) */
+  int slots_2d, slots_3d;
+  long long device_loops;  /* launches of the serving loop */
+} eik_server_stats;
+int eik_server_create(long long hbm_budget_bytes, int max_inflight, int keep_results, eik_server** out);
+/* Adds the handle's mesh, speeds, partition options and max_iterations to the pool
+ * (the host layout is built now); slots = 0 sizes it from the budget. */
+int eik_server_add_mesh(eik_server* s, eik_solver* h, int slots, int* mesh_id);
+int eik_server_mesh_info(const eik_server* s, int mesh_id, int* nv, int* slots, long long* device_bytes);
+int eik_server_start(eik_server* s);
+int eik_server_submit(eik_server* s, int mesh_id, const int* seeds, int nseeds, float speed_scale, long long* id);
+/* Completed requests since the last call (waits up to wait_ms for the first). */
+int eik_server_poll(eik_server* s, eik_completion* out, int max, int wait_ms, int* n);
+/* Travel times of a completed request (keep_results = 1); releases them. */
+int eik_server_result(eik_server* s, long long id, float* out, int nv);
+/* Waits until nothing is queued or running (timeout_ms < 0: no limit). */
+int eik_server_drain(eik_server* s, int timeout_ms);
+int eik_server_get_stats(eik_server* s, eik_server_stats* out);
+void eik_server_destroy(eik_server* s);
+const char* eik_server_last_error(const eik_server* s);
+
 /* The CUDA stream (cudaStream_t) the handle's solves and copies run on, or null
  * before the first solve.  Lets callers order their own work or time with events. */
 void* eik_stream(const eik_solver* h);

@@ -63,6 +63,18 @@ _IP = ctypes.POINTER(ctypes.c_int)
 _UP = ctypes.POINTER(ctypes.c_ubyte)
 
 # name: (restype, argtypes) — every symbol declared in include/eikonal_gb300.h
+class EikCompletion(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_longlong), ("mesh", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("status", ctypes.c_int), ("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("done_s", ctypes.c_double)]
+
+
+class EikServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong), ("queued", ctypes.c_longlong),
+                ("running", ctypes.c_longlong), ("device_bytes", ctypes.c_longlong), ("slots_2d", ctypes.c_int),
+                ("slots_3d", ctypes.c_int), ("device_loops", ctypes.c_longlong)]
+
+
 SIGNATURES = {
     "eik_default_options": (None, [ctypes.POINTER(EikOptions)]),
     "eik_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
@@ -103,6 +115,20 @@ SIGNATURES = {
     "eik_batch_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(EikStats)]),
     "eik_batch_stream": (_P, [_P]),
     "eik_batch_last_error": (ctypes.c_char_p, [_P]),
+    "eik_server_create": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "eik_server_add_mesh": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "eik_server_mesh_info": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)]),
+    "eik_server_start": (ctypes.c_int, [_P]),
+    "eik_server_submit": (ctypes.c_int, [_P, ctypes.c_int, _IP, ctypes.c_int, ctypes.c_float,
+                                         ctypes.POINTER(ctypes.c_longlong)]),
+    "eik_server_poll": (ctypes.c_int, [_P, ctypes.POINTER(EikCompletion), ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int)]),
+    "eik_server_result": (ctypes.c_int, [_P, ctypes.c_longlong, _FP, ctypes.c_int]),
+    "eik_server_drain": (ctypes.c_int, [_P, ctypes.c_int]),
+    "eik_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(EikServerStats)]),
+    "eik_server_destroy": (None, [_P]),
+    "eik_server_last_error": (ctypes.c_char_p, [_P]),
     "eik_last_error": (ctypes.c_char_p, [_P]),
     "eik_version": (ctypes.c_char_p, []),
 }
@@ -397,6 +423,87 @@ class EikonalBatch:
         s = EikStats()
         self._check(self._lib.eik_batch_get_stats(self._h, ctypes.byref(s)))
         return s.as_dict()
+
+
+class EikonalServer:
+    """Request server over resident pool meshes (eik_server_*).
+
+    add_mesh() takes configured Eikonal objects (mesh, speeds, block options);
+    start() lays the pool out in HBM and starts the device loops; submit() queues a
+    request (mesh id, seeds, speed scale) and returns its id; poll() returns
+    completions as dicts; result() the travel times of a completed request when
+    keep_results is set.  max_inflight=1 solves one request at a time.
+    """
+
+    def __init__(self, hbm_budget_bytes=8 << 30, max_inflight=0, keep_results=False):
+        self._lib = lib()
+        h = _P()
+        rc = self._lib.eik_server_create(int(hbm_budget_bytes), int(max_inflight), 1 if keep_results else 0,
+                                         ctypes.byref(h))
+        if rc:
+            raise EikonalError(rc, "eik_server_create failed")
+        self._h = h
+        self._nv = []
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.eik_server_destroy(h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc:
+            raise EikonalError(rc, self._lib.eik_server_last_error(self._h).decode())
+
+    def add_mesh(self, solver, slots=0):
+        if not solver._mesh_loaded:
+            solver.initializeMesh()
+        solver._push_options()
+        mid = ctypes.c_int()
+        self._check(self._lib.eik_server_add_mesh(self._h, solver._h, int(slots), ctypes.byref(mid)))
+        self._nv.append(solver.numVertices())
+        return mid.value
+
+    def mesh_info(self, mesh_id):
+        nv, slots, nbytes = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        self._check(self._lib.eik_server_mesh_info(self._h, int(mesh_id), ctypes.byref(nv), ctypes.byref(slots),
+                                                   ctypes.byref(nbytes)))
+        return {"vertices": nv.value, "slots": slots.value, "device_bytes": nbytes.value}
+
+    def start(self):
+        self._check(self._lib.eik_server_start(self._h))
+
+    def submit(self, mesh_id, seeds, speed_scale=1.0):
+        sd = np.ascontiguousarray(seeds, dtype=np.int32).ravel()
+        rid = ctypes.c_longlong()
+        self._check(self._lib.eik_server_submit(self._h, int(mesh_id), _iptr(sd), sd.size, float(speed_scale),
+                                                ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, max_items=1024, wait_ms=0):
+        buf = (EikCompletion * max_items)()
+        n = ctypes.c_int()
+        rc = self._lib.eik_server_poll(self._h, buf, max_items, int(wait_ms), ctypes.byref(n))
+        out = [{f: getattr(buf[i], f) for f, _ in EikCompletion._fields_} for i in range(n.value)]
+        if rc and not out:
+            self._check(rc)
+        return out
+
+    def result(self, request_id, mesh_id):
+        out = np.empty(self._nv[mesh_id], dtype=np.float32)
+        self._check(self._lib.eik_server_result(self._h, int(request_id), _fptr(out), out.size))
+        return out
+
+    def drain(self, timeout_ms=-1):
+        self._check(self._lib.eik_server_drain(self._h, int(timeout_ms)))
+
+    def stats(self):
+        s = EikServerStats()
+        self._check(self._lib.eik_server_get_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in EikServerStats._fields_}
 
 
 def selftest_local_update(which, inputs):

@@ -25,9 +25,9 @@ HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wext
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "-Xcompiler",
               "-ffp-contract=off"]
 
-HOST_SRC = ["setup.cpp", "mesh_io.cpp", "capi.cpp"]
+HOST_SRC = ["setup.cpp", "mesh_io.cpp", "capi.cpp", "serve.cpp"]
 CUDA_SRC = ["fim_device.cu"]
-HEADERS = ["setup.hpp", "mesh_io.hpp", "device.hpp", "local_update.cuh"]
+HEADERS = ["setup.hpp", "mesh_io.hpp", "device.hpp", "local_update.cuh", "solver_access.hpp"]
 
 
 def _newer(target, deps):
@@ -64,7 +64,7 @@ def build(force=False, verbose=False):
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout + r.stderr)
     if force or jobs or not _newer(LIB, objs):
-        _run([NVCC, "-shared", *ARCH, "--cudart", "static", "-o", LIB, *objs])
+        _run([NVCC, "-shared", *ARCH, "--cudart", "static", "-o", LIB, *objs, "-lpthread"])
     return LIB
 
 

@@ -13,6 +13,7 @@
 #include "device.hpp"
 #include "mesh_io.hpp"
 #include "setup.hpp"
+#include "solver_access.hpp"
 
 using namespace eikgb;
 
@@ -495,6 +496,42 @@ int eik_solve3d_noalloc(const float* xyz, int nv, const int* tets, int nt, const
   if (iterations) *iterations = it;
   return EIK_OK;
 }
+
+}  // extern "C"
+
+// ---- request server support ---------------------------------------------------
+
+int eikgb::snapshot_for_server(eik_solver* h, MeshSnapshot& out, std::string& err) {
+  if (!h) return EIK_ERR_ARG;
+  if (h->nv == 0) {
+    err = "no mesh: call eik_set_mesh or eik_load_mesh first";
+    return EIK_ERR_STATE;
+  }
+  bool nl = false;
+  int rc = host_prepare(h, &nl);
+  if (rc) {
+    err = h->err;
+    return rc;
+  }
+  out.dim = h->dim;
+  out.nv = h->nv;
+  out.ne = h->ne;
+  out.layout = h->layout;
+  out.xyz = h->xyz;
+  out.max_iterations = h->opt.max_iterations;
+  out.fim_sweeps = h->opt.fim_sweeps;
+  out.threads = h->opt.threads_per_block;
+  if (h->dim == 3) {
+    out.elems = h->elems;
+    tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), out.M6);
+  } else {
+    out.speed.assign(h->ne, 1.0f);
+    if (h->speeds_set && (int)h->speeds.size() == h->ne) out.speed = h->speeds;
+  }
+  return EIK_OK;
+}
+
+extern "C" {
 
 // ---- batches ----------------------------------------------------------------
 

@@ -49,6 +49,31 @@ struct SolveOptions {
   std::vector<int> inst_max_iterations;  // per instance; empty: max_iterations for all
 };
 
+// Coefficient inputs of one pool mesh for the serving path (original vertex and
+// element order, host arrays; copied to the device by serve_setup).
+struct ServeSource {
+  int dim = 3;
+  const float* xyz = nullptr;  // 3D: 3 per vertex
+  int nv = 0;
+  const int* tets = nullptr;   // 3D: 4 per tet (0-based)
+  int nt = 0;
+  const float* M6 = nullptr;   // 3D: 6 metric entries per tet (tet_metrics)
+  const float* speed = nullptr;  // 2D: speed per real face
+  int nf = 0;
+};
+
+// One request started on instance `inst`: 3D metric entries are multiplied by
+// coef_scale, 2D face speeds by coef_scale; seeds are vertex ids of the instance.
+struct Admission {
+  int inst = 0;
+  float coef_scale = 1.0f;
+  int max_iterations = 100;
+  std::vector<int> seeds;
+};
+
+// Device bytes one instance of this layout occupies (layout arrays + state).
+size_t device_footprint(const Layout& L);
+
 class DeviceSolve {
  public:
   DeviceSolve();
@@ -75,6 +100,24 @@ class DeviceSolve {
   // One visit of every block with the 2D kernel on the given vertex values
   // (renumbered order); sweep visit or neighbour check.  For self-tests.
   std::string visit_once(bool check, const float* T_host, float* out_host);
+  // ---- serving: a resident arena of instances admitted one by one ----------
+  // serve_setup makes every instance of the uploaded (concatenated) layout idle,
+  // uploads the coefficient sources of the pool meshes and builds the serving
+  // loop.  serve_admit starts instances (fresh state, request-scaled
+  // coefficients, seeds); serve_run runs the device loop until some instance
+  // finishes, the pending flag is raised or nothing runs; serve_poll reads which
+  // instances are done; serve_fetch + serve_sync copy results to pinned memory.
+  std::string serve_setup(const std::vector<ServeSource>& meshes, const std::vector<int>& inst_mesh, int sweeps,
+                          int threads);
+  std::string serve_admit(const std::vector<Admission>& adm);
+  std::string serve_run();
+  std::string serve_poll(std::vector<int>& done, std::vector<int>& iters);
+  std::string serve_fetch(int inst);
+  std::string serve_sync();
+  const float* serve_host_result(int inst) const;  // valid after serve_sync
+  volatile int* serve_pending() const;             // host side of the pending flag
+  // Makes the device this object was created on current in the calling thread.
+  void bind_thread() const;
   const SolveStats& stats() const { return stats_; }
   const Layout* layout() const { return L_; }
   void* stream() const { return stream_; }

@@ -101,6 +101,10 @@ struct DevArgs {
   const int* inst_maxit;  // iteration cap of every instance
   int* inst_fail;
   int ninst;
+  // serving: the loop also ends after an iteration in which some instance
+  // finished, or once the host raised *pending (requests waiting for admission)
+  int serve;
+  const volatile int* pending;
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -794,18 +798,24 @@ __global__ void k_activate2d(DevArgs a) {
 __device__ void finish_iteration_cta(const DevArgs& a, bool vertex_test) {
   Ctl* c = a.ctl;
   const int it = c->iter + 1;
-  int any = 0;
+  int any = 0, fin = 0;
   for (int i = threadIdx.x; i < a.ninst; i += blockDim.x) {
     if (!a.inst_done[i]) {
-      a.inst_iters[i] = it;
-      const bool stop = a.inst_nnext[i] == 0 || it >= a.inst_maxit[i] || (vertex_test && a.inst_fail[i] == 0);
-      if (stop) a.inst_done[i] = 1;
-      else any = 1;
+      const int own = a.inst_iters[i] + 1;  // iterations of this instance since it started
+      a.inst_iters[i] = own;
+      const bool stop = a.inst_nnext[i] == 0 || own >= a.inst_maxit[i] || (vertex_test && a.inst_fail[i] == 0);
+      if (stop) {
+        a.inst_done[i] = 1;
+        fin = 1;
+      } else {
+        any = 1;
+      }
     }
     a.inst_nnext[i] = 0;
     a.inst_fail[i] = 0;
   }
   any = __syncthreads_or(any);
+  fin = __syncthreads_or(fin);
   if (threadIdx.x == 0) {
     c->iter = it;
     c->nact = c->nnext;
@@ -814,7 +824,8 @@ __device__ void finish_iteration_cta(const DevArgs& a, bool vertex_test) {
     c->work_a = c->work_b = c->work_c = c->work_d = 0;
     c->done_c = c->done_d = 0;
     c->conv_fail = 0;
-    const bool go = any && c->error == 0;
+    bool go = any && c->error == 0;
+    if (a.serve && (fin || *a.pending != 0)) go = false;
     c->stop = go ? 0 : 1;
     if (a.use_cond) cudaGraphSetConditional(a.cond, go ? 1u : 0u);
   }
@@ -903,6 +914,133 @@ __global__ void k_gather_result(const float* Ta, const unsigned char* visited, c
 }
 __global__ void k_gather_hist(const float* h, const int* perm, int nv, float* out) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) out[v] = h[perm[v]];
+}
+
+// ---------------------------------------------------------------------------
+// Serving: instances of a resident arena are admitted between device loops.
+// ---------------------------------------------------------------------------
+
+// Drops entries of finished instances from the active list of the coming
+// iteration (one CTA; list order does not affect results).
+__global__ void k_compact_active(DevArgs a) {
+  __shared__ int s_n;
+  Ctl* c = a.ctl;
+  int* act = act_list(a, c->iter);
+  const int n = c->nact;
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int b = act[i];
+    if (!a.inst_done[a.blk_inst[b]]) a.list_new[atomicAdd(&s_n, 1)] = b;
+  }
+  __syncthreads();
+  const int m = s_n;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) act[i] = a.list_new[i];
+  if (threadIdx.x == 0) c->nact = m;
+}
+
+// Fresh state for one instance: vertices [v0, v0+nv), blocks [b0, b0+nb).
+__global__ void k_admit_state(DevArgs a, int v0, int nv, int b0, int nb, float large) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+    a.Ta[v0 + i] = large;
+    a.Tb[v0 + i] = large;
+    const_cast<float*>(a.Tinit)[v0 + i] = large;
+    a.prev[v0 + i] = large;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += stride) {
+    a.conv[b0 + i] = 0;
+    a.stampA[b0 + i] = 0;
+    a.stampC[b0 + i] = 0;
+    a.visited[b0 + i] = 0;
+  }
+}
+
+// Per-slot metric terms of one 3D instance from its mesh and the request's metric
+// factor k (metric entries multiplied by k, then the six products u^T M w of
+// tet_gram, every operation rounded separately in the host build's order).
+__device__ __forceinline__ float uMw_rn(const float* u, const float* m, const float* w) {
+  const float x = __fadd_rn(__fadd_rn(__fmul_rn(u[0], m[0]), __fmul_rn(u[1], m[1])), __fmul_rn(u[2], m[2]));
+  const float y = __fadd_rn(__fadd_rn(__fmul_rn(u[0], m[1]), __fmul_rn(u[1], m[3])), __fmul_rn(u[2], m[4]));
+  const float z = __fadd_rn(__fadd_rn(__fmul_rn(u[0], m[2]), __fmul_rn(u[1], m[4])), __fmul_rn(u[2], m[5]));
+  return __fadd_rn(__fadd_rn(__fmul_rn(x, w[0]), __fmul_rn(y, w[1])), __fmul_rn(z, w[2]));
+}
+
+__global__ void k_admit_coef3d(const BlockDesc* blocks, int nb, float* coef, const int* slot_elem, const float* xyz,
+                               const int* tets, const float* M6, float k) {
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    const BlockDesc d = blocks[b];
+    for (int j = threadIdx.x; j < d.nslots; j += blockDim.x) {
+      const int t = slot_elem[d.slot_begin + j];
+      float P[4][3], m[6];
+      for (int q = 0; q < 4; ++q) {
+        const int v = tets[4 * (size_t)t + q];
+        for (int c = 0; c < 3; ++c) P[q][c] = xyz[3 * (size_t)v + c];
+      }
+      for (int q = 0; q < 6; ++q) m[q] = __fmul_rn(M6[6 * (size_t)t + q], k);
+      float AC[3], AD[3], BC[3], CD[3], BD[3];
+      for (int c = 0; c < 3; ++c) {
+        AC[c] = __fsub_rn(P[2][c], P[0][c]);
+        AD[c] = __fsub_rn(P[3][c], P[0][c]);
+        BC[c] = __fsub_rn(P[2][c], P[1][c]);
+        CD[c] = __fsub_rn(P[3][c], P[2][c]);
+        BD[c] = __fsub_rn(P[3][c], P[1][c]);
+      }
+      float* base = coef + 6 * (size_t)d.slot_begin + j;
+      const size_t np = (size_t)d.nslots_pad;
+      base[0 * np] = uMw_rn(AC, m, BC);
+      base[1 * np] = uMw_rn(BC, m, CD);
+      base[2 * np] = uMw_rn(AC, m, CD);
+      base[3 * np] = uMw_rn(AD, m, BD);
+      base[4 * np] = uMw_rn(AC, m, AD);
+      base[5 * np] = uMw_rn(BC, m, BD);
+    }
+  }
+}
+
+// Inverse speed column of one 2D instance: 1 / (speed * s) per real face, 1 on
+// the virtual faces of obtuse corners (as the host layout sets them).
+__global__ void k_admit_coef2d(const BlockDesc* blocks, int nb, float* coef, const int* slot_elem, const float* speed,
+                               float s) {
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    const BlockDesc d = blocks[b];
+    for (int j = threadIdx.x; j < d.nslots; j += blockDim.x) {
+      const int e = slot_elem[d.slot_begin + j];
+      const float F = (e >= 0) ? __fdiv_rn(1.0f, __fmul_rn(speed[e], s)) : 1.0f;
+      coef[4 * (size_t)d.slot_begin + 3 * (size_t)d.nslots_pad + j] = F;
+    }
+  }
+}
+
+// Seeds of one admitted instance (renumbered ids) and its starting blocks appended
+// to the active list of the coming iteration; the instance starts running.
+__global__ void k_admit_seeds(DevArgs a, int inst, const int* seed_ids, int nseeds, const int* seed_blocks, int nsb,
+                              int maxit, int dim) {
+  __shared__ int s_base;
+  Ctl* c = a.ctl;
+  for (int i = threadIdx.x; i < nseeds; i += blockDim.x) {
+    const int v = seed_ids[i];
+    a.Ta[v] = 0.0f;
+    a.Tb[v] = 0.0f;
+    const_cast<float*>(a.Tinit)[v] = 0.0f;
+    a.prev[v] = 0.0f;
+  }
+  if (threadIdx.x == 0) {
+    s_base = c->nact;
+    c->nact += nsb;
+    a.inst_done[inst] = 0;
+    a.inst_iters[inst] = 0;
+    a.inst_nnext[inst] = 0;
+    a.inst_fail[inst] = 0;
+    const_cast<int*>(a.inst_maxit)[inst] = maxit;
+  }
+  __syncthreads();
+  int* act = act_list(a, c->iter);
+  for (int i = threadIdx.x; i < nsb; i += blockDim.x) {
+    const int b = seed_blocks[i];
+    act[s_base + i] = b;
+    if (dim == 2) a.stampA[b] = c->iter + 1;
+  }
 }
 
 // element-wise evaluation of the device local updates (self-test entry points)
@@ -995,6 +1133,34 @@ struct DeviceSolve::Impl {
   int g_sweeps = -1, g_threads = -1;
   bool g_hist = false;
   int g_histcap = -1;
+  int g_serve = -1;
+  int device = 0;  // the device current when the object was created
+  // serving: host flag (mapped pinned memory) that ends the device loop early
+  int* pending_host = nullptr;
+  const volatile int* pending_dev = nullptr;
+  struct Source {
+    float* xyz = nullptr;
+    int* tets = nullptr;
+    float* M6 = nullptr;
+    float* speed = nullptr;
+  };
+  std::vector<Source> src;         // per pool mesh
+  std::vector<int> inst_mesh;      // pool mesh of every instance
+  int* slot_elem = nullptr;        // element id per slot (instance-local)
+  float* host_res = nullptr;       // pinned: results of finished instances
+  void free_serve() {
+    for (Source& x : src) {
+      if (x.xyz) cudaFree(x.xyz);
+      if (x.tets) cudaFree(x.tets);
+      if (x.M6) cudaFree(x.M6);
+      if (x.speed) cudaFree(x.speed);
+    }
+    src.clear();
+    if (slot_elem) cudaFree(slot_elem);
+    slot_elem = nullptr;
+    if (host_res) cudaFreeHost(host_res);
+    host_res = nullptr;
+  }
   size_t smem = 0;
   int grid_visit = 0, grid_aux = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1025,16 +1191,119 @@ struct DeviceSolve::Impl {
     ktime_cap = 0;
     drop_graph();
   }
+  std::string build_graph(const Layout& L, int sweeps, int threads, int hcap, bool serve);
   void drop_graph() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     exec = nullptr;
     graph = nullptr;
     g_sweeps = g_threads = g_histcap = -1;
+    g_serve = -1;
   }
 };
 
+std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int threads, int hcap, bool serve) {
+  Impl& P = *this;
+  const bool want_hist = hcap > 0;
+  {
+    P.drop_graph();
+    DevArgs& a = P.args;
+    a = DevArgs{};
+    a.blocks = P.blocks; a.coef = P.coef; a.lv = P.lv; a.halo = P.halo; a.nbr_off = P.nbr_off; a.nbr = P.nbr;
+    a.vblock = P.vblock; a.nb = L.nb; a.nv = L.nv; a.Ta = P.Ta; a.Tb = P.Tb; a.Tinit = P.Tinit; a.prev = P.prev;
+    a.conv = P.conv; a.stampA = P.stampA; a.stampC = P.stampC; a.visited = P.visited; a.list0 = P.list0;
+    a.list1 = P.list1; a.list_new = P.list_new; a.ctl = P.ctl; a.hist = P.hist; a.hist_cap = hcap;
+    a.ktime = P.ktime; a.ktime_cap = P.ktime_cap;
+    a.fim_sweeps = sweeps; a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local;
+    a.max_owned = P.max_owned;
+    a.use_cond = 1;
+    a.blk_inst = P.blk_inst; a.inst_done = P.inst_done; a.inst_iters = P.inst_iters;
+    a.inst_nnext = P.inst_nnext; a.inst_fail = P.inst_fail; a.ninst = P.ninst; a.inst_maxit = P.inst_maxit;
+    a.serve = serve ? 1 : 0;
+    a.pending = P.pending_dev;
+    if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
+    CK(cudaGraphCreate(&P.graph, 0));
+    CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    // 2D blocks of up to 1024 slots use the thread-per-slot kernel (bitwise equal
+    // to the reference); larger 2D blocks fall back to the slot-loop kernel
+    const bool slot2d = (L.dim == 2) && P.max_slots_pad <= 1024;
+    int vthreads = threads;
+    size_t vsmem = P.smem;
+    void* kv_fim;
+    void* kv_chk;
+    if (L.dim == 3) {
+      kv_fim = (void*)k_visit3d<false>;
+      kv_chk = (void*)k_visit3d<true>;
+    } else if (slot2d) {
+      vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
+      vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
+      kv_fim = (sweeps == 7) ? (void*)k_visit2d_slot<false, 7> : (void*)k_visit2d_slot<false, 0>;
+      kv_chk = (void*)k_visit2d_slot<true, 1>;
+    } else {
+      kv_fim = (void*)k_visit2d<false>;
+      kv_chk = (void*)k_visit2d<true>;
+    }
+    for (void* k : {kv_fim, kv_chk})
+      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, vthreads, vsmem));
+    if (occ < 1) return "visit kernel cannot be resident (shared memory / registers)";
+    P.grid_visit = std::min(occ * nsm, std::max(L.nb, 1));
+    P.grid_aux = nsm * 4;
+    // start node
+    void* args_ptr[] = {&P.args};
+    cudaGraphNode_t n_start, n_while;
+    cudaKernelNodeParams kp{};
+    kp.func = (void*)k_start; kp.gridDim = dim3(1); kp.blockDim = dim3(32); kp.kernelParams = args_ptr;
+    CK(cudaGraphAddKernelNode(&n_start, P.graph, nullptr, 0, &kp));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = a.cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    CK(cudaGraphAddNode(&n_while, P.graph, &n_start, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaGraphNode_t prevn = nullptr, n;
+    P.body.clear();
+    auto add = [&](void* f, int grid, int block, size_t sm, void** params) -> std::string {
+      P.body.push_back(Impl::Launch{f, grid, block, sm, (f == (void*)k_snapshot) ? L.dim : 0});
+      cudaKernelNodeParams q{};
+      q.func = f; q.gridDim = dim3(grid); q.blockDim = dim3(block); q.sharedMemBytes = (unsigned)sm;
+      q.kernelParams = params;
+      CK(cudaGraphAddKernelNode(&n, body, prevn ? &prevn : nullptr, prevn ? 1 : 0, &q));
+      prevn = n;
+      return "";
+    };
+    static int dim3v = 3, dim2v = 2;
+    void* snap_args[] = {&P.args, (L.dim == 3) ? (void*)&dim3v : (void*)&dim2v};
+    std::string e;
+    if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
+    if (L.dim == 3) {
+      if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
+      if (!(e = add((void*)k_close3d, 1, 256, 0, args_ptr)).empty()) return e;
+    } else {
+      if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
+      if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+    }
+    if (want_hist)
+      if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
+    CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
+    P.g_sweeps = sweeps;
+    P.g_threads = threads;
+    P.g_hist = want_hist;
+    P.g_histcap = hcap;
+    P.g_serve = serve ? 1 : 0;
+  }
+  return "";
+}
+
 DeviceSolve::DeviceSolve() : p_(new Impl) {
+  cudaGetDevice(&p_->device);
   cudaStream_t s;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess) stream_ = s;
   cudaEventCreate(&p_->ev0);
@@ -1043,6 +1312,8 @@ DeviceSolve::DeviceSolve() : p_(new Impl) {
 
 DeviceSolve::~DeviceSolve() {
   p_->free_all();
+  p_->free_serve();
+  if (p_->pending_host) cudaFreeHost(p_->pending_host);
   if (p_->ev0) cudaEventDestroy(p_->ev0);
   if (p_->ev1) cudaEventDestroy(p_->ev1);
   if (stream_) cudaStreamDestroy((cudaStream_t)stream_);
@@ -1257,95 +1528,10 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
 
   // (re)build the graph when the launch shape changes
   const bool want_hist = hcap > 0;
-  if (!P.exec || P.g_sweeps != sweeps || P.g_threads != threads || P.g_hist != want_hist || P.g_histcap != hcap) {
-    P.drop_graph();
-    DevArgs& a = P.args;
-    a = DevArgs{};
-    a.blocks = P.blocks; a.coef = P.coef; a.lv = P.lv; a.halo = P.halo; a.nbr_off = P.nbr_off; a.nbr = P.nbr;
-    a.vblock = P.vblock; a.nb = L.nb; a.nv = L.nv; a.Ta = P.Ta; a.Tb = P.Tb; a.Tinit = P.Tinit; a.prev = P.prev;
-    a.conv = P.conv; a.stampA = P.stampA; a.stampC = P.stampC; a.visited = P.visited; a.list0 = P.list0;
-    a.list1 = P.list1; a.list_new = P.list_new; a.ctl = P.ctl; a.hist = P.hist; a.hist_cap = hcap;
-    a.ktime = P.ktime; a.ktime_cap = P.ktime_cap;
-    a.fim_sweeps = sweeps; a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local;
-    a.max_owned = P.max_owned;
-    a.use_cond = 1;
-    a.blk_inst = P.blk_inst; a.inst_done = P.inst_done; a.inst_iters = P.inst_iters;
-    a.inst_nnext = P.inst_nnext; a.inst_fail = P.inst_fail; a.ninst = P.ninst; a.inst_maxit = P.inst_maxit;
-    CK(cudaGraphCreate(&P.graph, 0));
-    CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
-    int dev = 0, nsm = 0;
-    CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    // 2D blocks of up to 1024 slots use the thread-per-slot kernel (bitwise equal
-    // to the reference); larger 2D blocks fall back to the slot-loop kernel
-    const bool slot2d = (L.dim == 2) && P.max_slots_pad <= 1024;
-    int vthreads = threads;
-    size_t vsmem = P.smem;
-    void* kv_fim;
-    void* kv_chk;
-    if (L.dim == 3) {
-      kv_fim = (void*)k_visit3d<false>;
-      kv_chk = (void*)k_visit3d<true>;
-    } else if (slot2d) {
-      vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
-      vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
-      kv_fim = (sweeps == 7) ? (void*)k_visit2d_slot<false, 7> : (void*)k_visit2d_slot<false, 0>;
-      kv_chk = (void*)k_visit2d_slot<true, 1>;
-    } else {
-      kv_fim = (void*)k_visit2d<false>;
-      kv_chk = (void*)k_visit2d<true>;
-    }
-    for (void* k : {kv_fim, kv_chk})
-      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
-    int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, vthreads, vsmem));
-    if (occ < 1) return "visit kernel cannot be resident (shared memory / registers)";
-    P.grid_visit = std::min(occ * nsm, std::max(L.nb, 1));
-    P.grid_aux = nsm * 4;
-    // start node
-    void* args_ptr[] = {&P.args};
-    cudaGraphNode_t n_start, n_while;
-    cudaKernelNodeParams kp{};
-    kp.func = (void*)k_start; kp.gridDim = dim3(1); kp.blockDim = dim3(32); kp.kernelParams = args_ptr;
-    CK(cudaGraphAddKernelNode(&n_start, P.graph, nullptr, 0, &kp));
-    cudaGraphNodeParams cp{};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = a.cond;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    CK(cudaGraphAddNode(&n_while, P.graph, &n_start, nullptr, 1, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    cudaGraphNode_t prevn = nullptr, n;
-    P.body.clear();
-    auto add = [&](void* f, int grid, int block, size_t sm, void** params) -> std::string {
-      P.body.push_back(Impl::Launch{f, grid, block, sm, (f == (void*)k_snapshot) ? L.dim : 0});
-      cudaKernelNodeParams q{};
-      q.func = f; q.gridDim = dim3(grid); q.blockDim = dim3(block); q.sharedMemBytes = (unsigned)sm;
-      q.kernelParams = params;
-      CK(cudaGraphAddKernelNode(&n, body, prevn ? &prevn : nullptr, prevn ? 1 : 0, &q));
-      prevn = n;
-      return "";
-    };
-    static int dim3v = 3, dim2v = 2;
-    void* snap_args[] = {&P.args, (L.dim == 3) ? (void*)&dim3v : (void*)&dim2v};
-    std::string e;
-    if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-    if (L.dim == 3) {
-      if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-      if (!(e = add((void*)k_close3d, 1, 256, 0, args_ptr)).empty()) return e;
-    } else {
-      if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-      if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-    }
-    if (want_hist)
-      if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
-    CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
-    P.g_sweeps = sweeps;
-    P.g_threads = threads;
-    P.g_hist = want_hist;
-    P.g_histcap = hcap;
+  if (!P.exec || P.g_sweeps != sweeps || P.g_threads != threads || P.g_hist != want_hist || P.g_histcap != hcap ||
+      P.g_serve != 0) {
+    std::string e = P.build_graph(L, sweeps, threads, hcap, false);
+    if (!e.empty()) return e;
   }
   CK(cudaEventRecord(P.ev0, st));
   if (!opt.direct_launch) {
@@ -1513,6 +1699,190 @@ std::string selftest_tri_blocks(const float* in, int n, bool check, float* out) 
   if (!e.empty()) return e;
   return ds.visit_once(check, T.data(), out);
 }
+
+size_t device_footprint(const Layout& L) {
+  const size_t nv = (size_t)L.nv, nb = (size_t)L.nb;
+  return nb * sizeof(BlockDesc) + L.coef.size() * sizeof(float) + (size_t)L.total_slots * (sizeof(uint2) + sizeof(int)) +
+         L.halo_ids.size() * sizeof(int) + (L.nbr_off.size() + L.nbr.size()) * sizeof(int) +
+         nv * (2 * sizeof(int) + 5 * sizeof(float)) + nb * (7 * sizeof(int) + 1) + 5 * sizeof(int);
+}
+
+std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, const std::vector<int>& inst_mesh,
+                                     int sweeps, int threads) {
+  Impl& P = *p_;
+  if (!L_) return "no layout uploaded";
+  const Layout& L = *L_;
+  if ((int)inst_mesh.size() != P.ninst) return "one pool mesh per instance expected";
+  for (int m : inst_mesh)
+    if (m < 0 || m >= (int)meshes.size()) return "pool mesh id out of range";
+  cudaStream_t st = (cudaStream_t)stream_;
+  P.free_serve();
+  P.src.resize(meshes.size());
+  for (size_t m = 0; m < meshes.size(); ++m) {
+    const ServeSource& x = meshes[m];
+    Impl::Source& d = P.src[m];
+    std::string e;
+    if (x.dim != L.dim) return "pool mesh of another dimension";
+    if (x.dim == 3) {
+      if (!(e = dev_alloc(d.xyz, 3 * (size_t)x.nv)).empty()) return e;
+      if (!(e = dev_alloc(d.tets, 4 * (size_t)x.nt)).empty()) return e;
+      if (!(e = dev_alloc(d.M6, 6 * (size_t)x.nt)).empty()) return e;
+      CK(cudaMemcpyAsync(d.xyz, x.xyz, sizeof(float) * 3 * x.nv, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.tets, x.tets, sizeof(int) * 4 * (size_t)x.nt, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d.M6, x.M6, sizeof(float) * 6 * (size_t)x.nt, cudaMemcpyHostToDevice, st));
+    } else {
+      if (!(e = dev_alloc(d.speed, (size_t)std::max(x.nf, 1))).empty()) return e;
+      CK(cudaMemcpyAsync(d.speed, x.speed, sizeof(float) * x.nf, cudaMemcpyHostToDevice, st));
+    }
+  }
+  P.inst_mesh = inst_mesh;
+  {
+    std::string e;
+    if (!(e = dev_alloc(P.slot_elem, (size_t)std::max(L.total_slots, 1))).empty()) return e;
+  }
+  CK(cudaMemcpyAsync(P.slot_elem, L.slot_elem.data(), sizeof(int) * L.slot_elem.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaHostAlloc((void**)&P.host_res, sizeof(float) * std::max(L.nv, 1), cudaHostAllocDefault));
+  if (!P.pending_host) {
+    CK(cudaHostAlloc((void**)&P.pending_host, sizeof(int), cudaHostAllocMapped));
+    void* d = nullptr;
+    CK(cudaHostGetDevicePointer(&d, P.pending_host, 0));
+    P.pending_dev = (const volatile int*)d;
+  }
+  *(volatile int*)P.pending_host = 0;
+  // every instance idle, every vertex at LARGENUM
+  std::vector<int> ones(P.ninst, 1);
+  CK(cudaMemcpyAsync(P.inst_done, ones.data(), sizeof(int) * P.ninst, cudaMemcpyHostToDevice, st));
+  for (int* t : {P.inst_iters, P.inst_nnext, P.inst_fail, P.inst_maxit})
+    CK(cudaMemsetAsync(t, 0, sizeof(int) * P.ninst, st));
+  for (int* t : {P.conv, P.stampA, P.stampC}) CK(cudaMemsetAsync(t, 0, sizeof(int) * L.nb, st));
+  CK(cudaMemsetAsync(P.visited, 0, L.nb, st));
+  k_init_state<<<std::max(1, std::min(4096, (L.nv + 255) / 256)), 256, 0, st>>>(
+      P.Ta, P.Tb, P.Tinit, P.prev, L.nv, (L.dim == 3) ? kLarge3D : kLarge2D);
+  CK(cudaGetLastError());
+  Ctl c{};
+  c.max_iters = 1 << 30;
+  CK(cudaMemcpyAsync(P.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+  int auto_threads = 256;
+  while (auto_threads < P.max_slots_pad && auto_threads < 1024) auto_threads *= 2;
+  const int th = (threads == 128 || threads == 256 || threads == 512 || threads == 1024) ? threads : auto_threads;
+  const int sw = (sweeps > 0) ? sweeps : (L.dim == 3 ? 2 : 7);
+  std::string e = P.build_graph(L, sw, th, 0, true);
+  if (!e.empty()) return e;
+  CK(cudaStreamSynchronize(st));
+  return "";
+}
+
+std::string DeviceSolve::serve_admit(const std::vector<Admission>& adm) {
+  Impl& P = *p_;
+  if (!L_ || P.g_serve != 1) return "serving not set up";
+  const Layout& L = *L_;
+  if (adm.empty()) return "";
+  cudaStream_t st = (cudaStream_t)stream_;
+  // stage every admission's seed ids (renumbered) and starting blocks in one copy
+  std::vector<int> stage;
+  std::vector<int> off(adm.size()), nsd(adm.size()), boff(adm.size()), nbk(adm.size());
+  for (size_t q = 0; q < adm.size(); ++q) {
+    const Admission& x = adm[q];
+    if (x.inst < 0 || x.inst >= P.ninst) return "instance out of range";
+    const int v0 = L.inst_vbeg[x.inst], nvi = L.inst_vbeg[x.inst + 1] - v0;
+    off[q] = (int)stage.size();
+    for (int sd : x.seeds) {
+      if (sd < 0 || sd >= nvi) return "seed vertex out of range";
+      stage.push_back(L.perm[v0 + sd]);
+    }
+    nsd[q] = (int)stage.size() - off[q];
+    boff[q] = (int)stage.size();
+    for (int i = off[q]; i < off[q] + nsd[q]; ++i) {
+      const int b = P.h_vblock[stage[i]];
+      bool seen = false;
+      for (int j = boff[q]; j < (int)stage.size(); ++j) seen = seen || stage[j] == b;
+      if (!seen) stage.push_back(b);
+    }
+    nbk[q] = (int)stage.size() - boff[q];
+  }
+  if (stage.size() > P.seed_cap) {
+    if (P.seed_ids) cudaFree(P.seed_ids);
+    P.seed_ids = nullptr;
+    P.seed_cap = std::max<size_t>(stage.size(), 1024);
+    CK(cudaMalloc((void**)&P.seed_ids, sizeof(int) * P.seed_cap));
+  }
+  CK(cudaMemcpyAsync(P.seed_ids, stage.data(), sizeof(int) * stage.size(), cudaMemcpyHostToDevice, st));
+  // list entries of instances that finished since the last loop leave the list
+  k_compact_active<<<1, 1024, 0, st>>>(P.args);
+  const float large = (L.dim == 3) ? kLarge3D : kLarge2D;
+  for (size_t q = 0; q < adm.size(); ++q) {
+    const Admission& x = adm[q];
+    const int i = x.inst;
+    const int v0 = L.inst_vbeg[i], nvi = L.inst_vbeg[i + 1] - v0;
+    const int b0 = L.inst_bbeg[i], nbi = L.inst_bbeg[i + 1] - b0;
+    k_admit_state<<<std::max(1, std::min(2048, (std::max(nvi, nbi) + 255) / 256)), 256, 0, st>>>(
+        P.args, v0, nvi, b0, nbi, large);
+    const Impl::Source& src = P.src[P.inst_mesh[i]];
+    const int g = std::max(1, std::min(nbi, 4096));
+    if (L.dim == 3)
+      k_admit_coef3d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.xyz, src.tets, src.M6,
+                                        x.coef_scale);
+    else
+      k_admit_coef2d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.speed, x.coef_scale);
+    k_admit_seeds<<<1, 256, 0, st>>>(P.args, i, P.seed_ids + off[q], nsd[q], P.seed_ids + boff[q], nbk[q],
+                                     x.max_iterations, L.dim);
+  }
+  CK(cudaGetLastError());
+  return "";
+}
+
+std::string DeviceSolve::serve_run() {
+  Impl& P = *p_;
+  if (!L_ || P.g_serve != 1) return "serving not set up";
+  cudaStream_t st = (cudaStream_t)stream_;
+  CK(cudaGraphLaunch(P.exec, st));
+  CK(cudaStreamSynchronize(st));
+  Ctl out{};
+  CK(cudaMemcpy(&out, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  stats_.iterations = out.iter;
+  stats_.error = out.error;
+  if (out.error) return "device reported error flags " + std::to_string(out.error);
+  return "";
+}
+
+std::string DeviceSolve::serve_poll(std::vector<int>& done, std::vector<int>& iters) {
+  Impl& P = *p_;
+  cudaStream_t st = (cudaStream_t)stream_;
+  done.resize(P.ninst);
+  iters.resize(P.ninst);
+  CK(cudaMemcpyAsync(done.data(), P.inst_done, sizeof(int) * P.ninst, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(iters.data(), P.inst_iters, sizeof(int) * P.ninst, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return "";
+}
+
+std::string DeviceSolve::serve_fetch(int inst) {
+  Impl& P = *p_;
+  if (!L_ || inst < 0 || inst >= P.ninst || !P.host_res) return "instance out of range";
+  const Layout& L = *L_;
+  cudaStream_t st = (cudaStream_t)stream_;
+  const int v0 = L.inst_vbeg[inst], nvi = L.inst_vbeg[inst + 1] - v0;
+  k_gather_result<<<std::max(1, std::min(1024, (nvi + 255) / 256)), 256, 0, st>>>(
+      P.Ta, P.visited, P.vblock, P.perm + v0, nvi, L.dim, P.out_tmp + v0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(P.host_res + v0, P.out_tmp + v0, sizeof(float) * nvi, cudaMemcpyDeviceToHost, st));
+  return "";
+}
+
+std::string DeviceSolve::serve_sync() {
+  CK(cudaStreamSynchronize((cudaStream_t)stream_));
+  return "";
+}
+
+const float* DeviceSolve::serve_host_result(int inst) const {
+  const Impl& P = *p_;
+  if (!L_ || !P.host_res || inst < 0 || inst >= P.ninst) return nullptr;
+  return P.host_res + L_->inst_vbeg[inst];
+}
+
+volatile int* DeviceSolve::serve_pending() const { return (volatile int*)p_->pending_host; }
+
+void DeviceSolve::bind_thread() const { cudaSetDevice(p_->device); }
 
 std::string selftest_device(int which, const float* in, float* out, int n) {
   if (which == 3 || which == 4) return selftest_tri_blocks(in, n, which == 4, out);

@@ -184,3 +184,19 @@ def test_batch_rejects_mixed_dimensions_and_empty(eik, mg):
     assert len(b) == 2 and b.numIterations(0) == 0
     with pytest.raises(eik.EikonalError):
         b.getFinalResult(0)  # nothing solved yet
+
+
+def test_server_host_side_and_no_gpu_failure(eik, mg):
+    xyz, faces = mg.icosphere(2)
+    a = eik.Eikonal(True)
+    a.set_mesh(xyz, faces)
+    srv = eik.EikonalServer(hbm_budget_bytes=1 << 26)
+    mid = srv.add_mesh(a)
+    info = srv.mesh_info(mid)
+    assert info["vertices"] == xyz.shape[0] and info["device_bytes"] > 4 * xyz.shape[0]
+    with pytest.raises(eik.EikonalError):
+        srv.submit(mid, [0], 1.0)  # not started
+    if not gpu_available():
+        with pytest.raises(eik.EikonalError):
+            srv.start()  # no device: fails loudly, no CPU fallback
+    srv.close()
