@@ -52,8 +52,11 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-sample-iters", type=int, default=0, help="0 = choose automatically")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="c3d", choices=["c3d", "batch"],
-                   help="c3d: the 65^3 tet solve (headline); batch: 256 icospheres, batched vs plain")
+    p.add_argument("--workload", default="c3d", choices=["c3d", "batch", "serve"],
+                   help="c3d: the 65^3 tet solve (headline); batch: 256 icospheres, batched vs plain; "
+                        "serve: Poisson request stream over a resident mesh pool")
+    p.add_argument("--serve-rates", default="50,200,500,1000,2000")
+    p.add_argument("--serve-budget-gb", type=float, default=16.0)
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--launch", default="graph", choices=["graph", "direct"],
                    help="graph: one CUDA-graph launch per solve; direct: kernel by kernel (for ncu)")
@@ -281,6 +284,112 @@ def bench_batch(args, E, torch, world, local):
     }
 
 
+SERVE_WORKLOAD = ("serving: resident pool of icospheres L5, L6, L7 and L6 with other speeds (2D) and jittered "
+                  "Kuhn cubes 33^3, 49^3, 65^3, 97^3 (3D); Poisson arrivals (seed 7), each request a uniform "
+                  "pool mesh, 1-16 random seeds and a global speed scale U[0.5, 2]")
+
+
+def serve_pool(E, mg):
+    """The eight pool meshes as configured handles."""
+    pool = []
+    for lv, phase in ((5, 0.0), (6, 0.0), (7, 0.0), (6, 1.0)):
+        xyz, faces = mg.icosphere(lv)
+        c = xyz[faces].mean(axis=1).astype(np.float64)
+        sp = (1.0 + 0.5 * np.sin(3 * c[:, 0] + phase) * np.cos(2 * c[:, 1]) * np.sin(c[:, 2])).astype(np.float32)
+        e = E.Eikonal(True)
+        e.set_mesh(xyz, faces)
+        e.initSpeedMtxMultipliers(sp)
+        e.maxVertsPerBlock_ = 64
+        e.maxIterations_ = 1000
+        pool.append((e, xyz.shape[0]))
+    for k, n in enumerate((33, 49, 65, 97)):
+        xyz, tets = mg.kuhn_cube(n, 0.2, seed=20 + k)
+        v = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=30 + k)
+        e = E.Eikonal(False)
+        e.set_mesh(xyz, tets)
+        e.initSpeedMtxMultipliers((1.0 / (v.astype(np.float64) ** 2)).astype(np.float32))
+        e.maxVertsPerBlock_ = 64
+        e.maxIterations_ = 1000
+        pool.append((e, xyz.shape[0]))
+    return pool
+
+
+def serve_stream(srv, ids, sizes, rate, count, rng):
+    """Submits `count` Poisson arrivals at `rate`/s, waits for all, returns the
+    completion records."""
+    gaps = rng.exponential(1.0 / rate, size=count)
+    reqs = []
+    for _ in range(count):
+        m = int(rng.integers(len(ids)))
+        seeds = rng.choice(sizes[m], size=int(rng.integers(1, 17)), replace=False).astype(np.int32)
+        reqs.append((m, seeds, float(rng.uniform(0.5, 2.0))))
+    t0 = time.perf_counter()
+    due = t0
+    for (m, seeds, s), g in zip(reqs, gaps):
+        due += g
+        while True:
+            now = time.perf_counter()
+            if now >= due:
+                break
+            time.sleep(min(due - now, 0.001))
+        srv.submit(ids[m], seeds, s)
+    srv.drain()
+    out = []
+    while True:
+        got = srv.poll(max_items=4096)
+        if not got:
+            break
+        out += got
+    return out
+
+
+def bench_serve(args, E, torch):
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    pool = serve_pool(E, mg)
+    sizes = [n for _, n in pool]
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    res = {"metric": METRIC, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "steps": args.steps, "warmup": args.warmup,
+           "config": {"workload": SERVE_WORKLOAD, "rates_per_s": rates, "hbm_budget_gb": args.serve_budget_gb}}
+    modes = {}
+    for mode, inflight in (("served", 0), ("plain", 1)):
+        srv = E.EikonalServer(hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)), max_inflight=inflight)
+        t0 = time.perf_counter()
+        ids = [srv.add_mesh(e) for e, _ in pool]
+        srv.start()
+        setup_s = time.perf_counter() - t0
+        info = [srv.mesh_info(i) for i in ids]
+        rng = np.random.Generator(np.random.PCG64(7))
+        # warm-up: one request per pool mesh
+        for i in ids:
+            srv.submit(i, [0], 1.0)
+        srv.drain()
+        srv.poll(max_items=4096)
+        per_rate = []
+        for rate in rates:
+            count = int(min(300, max(100, 2 * rate)))
+            comp = serve_stream(srv, ids, sizes, rate, count, rng)
+            lat = sorted(1e3 * (c["done_s"] - c["submit_s"]) for c in comp)
+            span = max(c["done_s"] for c in comp) - min(c["submit_s"] for c in comp)
+            per_rate.append({"rate_per_s": rate, "requests": len(comp), "solves_per_s": len(comp) / span,
+                             "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                             "errors": sum(1 for c in comp if c["status"] != 0)})
+        st = srv.stats()
+        srv.close()
+        modes[mode] = {"per_rate": per_rate, "setup_s": round(setup_s, 2), "device_bytes": st["device_bytes"],
+                       "slots": [x["slots"] for x in info], "device_loops": st["device_loops"]}
+    top = modes["served"]["per_rate"][-1]
+    res["value"] = top["solves_per_s"]
+    res["ms_per_step"] = 1e3 / top["solves_per_s"]
+    res["latency_ms"] = {"p50": top["p50_ms"], "p99": top["p99_ms"]}
+    res["served"] = modes["served"]
+    res["plain"] = modes["plain"]
+    res["served_over_plain"] = top["solves_per_s"] / modes["plain"]["per_rate"][-1]["solves_per_s"]
+    res["e2e"] = {"value": top["solves_per_s"], "unit": "solves/s", "note": "requests submitted from the host, "
+                  "travel times copied back to pinned host memory before completion"}
+    return res
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -294,6 +403,11 @@ def main():
     E = importlib.import_module("sci-solver_eikonal_gb300")
     if args.workload == "batch":
         res = bench_batch(args, E, torch, world, local)
+        if rank == 0:
+            print(json.dumps(res), flush=True)
+        return 0
+    if args.workload == "serve":
+        res = bench_serve(args, E, torch)
         if rank == 0:
             print(json.dumps(res), flush=True)
         return 0

@@ -6,6 +6,7 @@
 //                src/core3d/cuda/tetgen.cu:1993-...)
 //   write_vtk    ASCII VTK unstructured grids with a "traveltime" point field
 //                (meshFIM2d_eikonal.cu:74-109, meshFIM3dEikonal.cu:116-151)
+#include <algorithm>
 #include "mesh_io.hpp"
 
 #include <cstdint>
@@ -158,6 +159,13 @@ std::string read_ply(const std::string& path, std::vector<float>& xyz, std::vect
       faces.push_back(poly[k]);
       faces.push_back(poly[k + 1]);
     }
+  }
+  // Corner indices counted from 1 (min 1, max nvert, as in some test fixtures of
+  // the reference) are read as 1-based, like the element indices of tet meshes.
+  if (!faces.empty()) {
+    const auto mm = std::minmax_element(faces.begin(), faces.end());
+    if (*mm.first == 1 && *mm.second == nvert)
+      for (int& v : faces) v -= 1;
   }
   for (int v : faces)
     if (v < 0 || v >= nvert) return "PLY face index out of range: " + path;
