@@ -52,9 +52,10 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-sample-iters", type=int, default=0, help="0 = choose automatically")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="c3d", choices=["c3d", "batch", "serve"],
+    p.add_argument("--workload", default="c3d", choices=["c3d", "batch", "serve", "prec"],
                    help="c3d: the 65^3 tet solve (headline); batch: 256 icospheres, batched vs plain; "
-                        "serve: Poisson request stream over a resident mesh pool")
+                        "serve: Poisson request stream over a resident mesh pool; "
+                        "prec: sliver + anisotropic 49^3 mesh, FP32 vs mixed FP32/FP64 vs an FP64 run")
     p.add_argument("--serve-rates", default="50,200,500,1000,2000")
     p.add_argument("--serve-budget-gb", type=float, default=16.0)
     p.add_argument("--batch-count", type=int, default=256)
@@ -390,6 +391,69 @@ def bench_serve(args, E, torch):
     return res
 
 
+PREC_WORKLOAD = ("precision: 49^3 jittered Kuhn cube with sliver tets (min dihedral < 5 deg, vertices moved "
+                 "toward opposite faces, seed 5), per-tet metric R diag(1, a, b) R^T with a, b log-uniform in "
+                 "[1, 100] (seed 6), 4 random seeds (seed 9), 64 verts/block")
+
+
+def bench_prec(args, E, torch):
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    from oracle import oracle as O  # the FP64 run of the same scheme (error reference)
+    t0 = time.perf_counter()
+    xyz, tets, sl = mg.sliver_cube(49, 0.10, seed=5)
+    M6 = mg.anisotropic_metrics(tets.shape[0], seed=6)
+    seeds = np.random.Generator(np.random.PCG64(9)).choice(xyz.shape[0], 4, replace=False).astype(np.int32)
+    gen_s = time.perf_counter() - t0
+    runs = {}
+    for name, prec in (("fp32", 0), ("mixed", 1)):
+        e = E.Eikonal(False)
+        e.set_mesh(xyz, tets)
+        e.initSpeedMtxMultipliers(M6.ravel())
+        e.setSeeds(seeds)
+        e.maxIterations_ = 1000
+        e.keepHistory_ = 0
+        e.precisionMode_ = prec
+        e.solveEikonal()
+        for _ in range(args.warmup):
+            e.solveEikonal()
+        ms = []
+        for _ in range(args.steps):
+            e.solveEikonal()
+            ms.append(e.stats()["solve_ms"])
+        st = e.stats()
+        runs[name] = {"e": e, "ms": statistics.median(ms), "stats": st, "result": e.getFinalResult()}
+    lab, nb = runs["fp32"]["e"].getPartition()
+    t1 = time.perf_counter()
+    r64 = O.solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], M6.ravel()), lab, nb, seeds,
+                    max_iters=1000, precision=64, nthreads=O.num_threads())
+    t64 = time.perf_counter() - t1
+    ref = r64["result"].astype(np.float64)
+
+    def err(r):
+        rel = np.abs(r.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-6)
+        return {"max": float(rel.max()), "p99": float(np.percentile(rel, 99)), "mean": float(rel.mean()),
+                "vertices_above_1e-5": int((rel > 1e-5).sum())}
+
+    out = {"metric": METRIC, "unit": "vertex-updates/s", "n_gpus": 1, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "steps": args.steps, "warmup": args.warmup,
+           "config": {"workload": PREC_WORKLOAD, "vertices": int(xyz.shape[0]), "tets": int(tets.shape[0]),
+                      "sliver_fraction": float(sl.mean()), "mesh_generation_s": round(gen_s, 1),
+                      "kappa_threshold": 1e4}}
+    for name in ("fp32", "mixed"):
+        r = runs[name]
+        st = r["stats"]
+        out[name] = {"solve_ms": r["ms"], "iterations": st["iterations"],
+                     "vertex_updates_per_s": st["vertex_updates"] / (r["ms"] * 1e-3),
+                     "error_vs_fp64": err(r["result"]), "flagged_tets": st["flagged_tets"],
+                     "residual_max_rel": st["residual_max_rel"], "residual_vertices": st["residual_vertices"]}
+    out["value"] = out["mixed"]["vertex_updates_per_s"]
+    out["ms_per_step"] = runs["mixed"]["ms"]
+    out["fp64_oracle"] = {"seconds": t64, "iterations": r64["iterations"], "threads": O.num_threads()}
+    out["e2e"] = None
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -405,6 +469,10 @@ def main():
         res = bench_batch(args, E, torch, world, local)
         if rank == 0:
             print(json.dumps(res), flush=True)
+        return 0
+    if args.workload == "prec":
+        res = bench_prec(args, E, torch)
+        print(json.dumps(res), flush=True)
         return 0
     if args.workload == "serve":
         res = bench_serve(args, E, torch)

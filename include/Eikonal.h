@@ -18,7 +18,8 @@
 //   * the reference's internal pointers (triMesh_, tetMesh_, FIMPtr2d_, FIMPtr3d_)
 //     have no counterpart; setMesh() takes vertex / element arrays instead;
 //   * keepHistory_ (default true) can be cleared to skip the per-iteration
-//     snapshots: iteration_values_ then holds the final result only.
+//     snapshots: iteration_values_ then holds the final result only;
+//   * precisionMode_ / precisionKappa_ select the mixed FP32/FP64 mode.
 #ifndef EIKONAL_GB300_CPP_H
 #define EIKONAL_GB300_CPP_H
 
@@ -49,6 +50,8 @@ class Eikonal {
     squareBlockDepth_ = o.square_block_depth;
     maxIterations_ = o.max_iterations;
     keepHistory_ = o.keep_history != 0;
+    precisionMode_ = o.precision;
+    precisionKappa_ = o.precision_kappa;
     if (eik_create(isTriMesh ? 1 : 0, &h_) != EIK_OK) throw std::runtime_error("eik_create failed");
   }
   virtual ~Eikonal() { eik_destroy(h_); }
@@ -166,6 +169,10 @@ class Eikonal {
   bool isTriMesh_;
   std::vector<float> speedMtxMultipliers_;
   bool keepHistory_;
+  // precision mode (not in the reference): 1 = FP64 local updates on tets whose
+  // metric edge Gram condition number exceeds precisionKappa_, FP64 residual check
+  int precisionMode_;
+  float precisionKappa_;
 
  private:
   void check(int rc) const {
@@ -188,6 +195,8 @@ class Eikonal {
     o.max_iterations = maxIterations_;
     o.verbose = verbose_ ? 1 : 0;
     o.keep_history = keepHistory_ ? 1 : 0;
+    o.precision = precisionMode_;
+    o.precision_kappa = precisionKappa_;
     check(eik_set_options(h_, &o));
   }
   eik_solver* h_ = nullptr;

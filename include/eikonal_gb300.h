@@ -53,6 +53,12 @@ typedef struct eik_options {
                               launched one by one with a host check per iteration, for profilers
                               that cannot see kernels inside conditional graphs */
   int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/512/1024); 0 = default */
+  int precision;           /* 0 (default): the reference's FP32 arithmetic, bit for bit.  1 (3D):
+                              tets whose metric edge Gram matrix has condition number above
+                              precision_kappa (slivers, strong anisotropy) run their local
+                              updates in FP64 from FP64 metric edge products; every other tet
+                              stays FP32.  An FP64 residual check runs after the solve. */
+  float precision_kappa;   /* flagging threshold on ||G||_F ||G^-1||_F (1e4) */
 } eik_options;
 
 typedef struct eik_stats {
@@ -78,6 +84,11 @@ typedef struct eik_stats {
   int fim_launches, check_launches;
   long long fim_slots, fim_halo, fim_owned; /* inputs streamed by the block-sweep kernel */
   long long h2d_bytes;       /* host-to-device bytes copied by the last solve (initial state) */
+  /* precision mode (precision = 1) */
+  long long flagged_tets;    /* tets whose updates run in FP64 */
+  double residual_max_abs;   /* FP64 check: max |T_v - min over incident tets of the FP64 update| */
+  double residual_max_rel;   /* the same relative to T_v */
+  long long residual_vertices; /* vertices with |residual| > 1e-5 * T_v */
 } eik_stats;
 
 /* Fills `o` with the reference's defaults (src/Eikonal.cu:4-24). */

@@ -34,6 +34,7 @@ class EikOptions(ctypes.Structure):
         ("square_block_depth", ctypes.c_int),
         ("max_iterations", ctypes.c_int), ("verbose", ctypes.c_int), ("keep_history", ctypes.c_int),
         ("fim_sweeps", ctypes.c_int), ("direct_launch", ctypes.c_int), ("threads_per_block", ctypes.c_int),
+        ("precision", ctypes.c_int), ("precision_kappa", ctypes.c_float),
     ]
 
 
@@ -51,6 +52,8 @@ class EikStats(ctypes.Structure):
         ("fim_launches", ctypes.c_int), ("check_launches", ctypes.c_int),
         ("fim_slots", ctypes.c_longlong), ("fim_halo", ctypes.c_longlong), ("fim_owned", ctypes.c_longlong),
         ("h2d_bytes", ctypes.c_longlong),
+        ("flagged_tets", ctypes.c_longlong), ("residual_max_abs", ctypes.c_double),
+        ("residual_max_rel", ctypes.c_double), ("residual_vertices", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -187,6 +190,7 @@ class Eikonal:
         "squareBlockDepth_": "square_block_depth", "maxIterations_": "max_iterations",
         "verbose_": "verbose", "keepHistory_": "keep_history", "fimSweeps_": "fim_sweeps",
         "directLaunch_": "direct_launch", "threadsPerBlock_": "threads_per_block",
+        "precisionMode_": "precision", "precisionKappa_": "precision_kappa",
     }
 
     def __init__(self, isTriMesh, fname="../src/test/test_data/sphere_74verts.ply", verbose=False):

@@ -44,6 +44,7 @@ struct eik_solver {
   int nb = 0;
   unsigned lay_mesh = ~0u, lay_part = ~0u, lay_speed = ~0u;
   std::string lay_key;
+  std::string prec_key;  // precision settings the layout's FP64 data was built for
   Layout layout;
   std::unique_ptr<DeviceSolve> dev;
   bool uploaded = false;
@@ -128,9 +129,26 @@ int host_prepare(eik_solver* h, bool* new_layout_out) {
       refresh_speed2d(h->prep, inv.data(), h->layout);
     }
     h->lay_speed = h->speed_ver;
+    h->prec_key.clear();  // FP64 products follow the metric
     if (h->uploaded) {
       std::string e = h->dev->upload_coef(h->layout);
       if (!e.empty()) return fail(h, EIK_ERR_CUDA, e);
+    }
+  }
+  // precision mode data (3D): flagged tets and their FP64 metric edge products
+  if (h->dim == 3) {
+    const bool on = h->opt.precision == 1;
+    const std::string pk = on ? ("1|" + std::to_string(h->opt.precision_kappa)) : "0";
+    if (new_layout || pk != h->prec_key) {
+      if (on) {
+        std::vector<float> M;
+        tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), M);
+        build_precision3d(h->xyz.data(), h->elems.data(), M.data(), (double)h->opt.precision_kappa, h->layout);
+      } else {
+        build_precision3d(nullptr, nullptr, nullptr, 0.0, h->layout);
+      }
+      if (!new_layout && pk != h->prec_key) h->uploaded = false;
+      h->prec_key = pk;
     }
   }
   *new_layout_out = new_layout;
@@ -193,6 +211,10 @@ void fill_stats(eik_stats& s, const SolveStats& st, const Layout& L, float setup
   s.fim_halo = st.fim_halo;
   s.fim_owned = st.fim_owned;
   s.h2d_bytes = st.h2d_bytes;
+  s.flagged_tets = L.flagged_tets;
+  s.residual_max_abs = st.residual_max_abs;
+  s.residual_max_rel = st.residual_max_rel;
+  s.residual_vertices = st.residual_vertices;
 }
 
 }  // namespace
@@ -214,6 +236,8 @@ void eik_default_options(eik_options* o) {
   o->fim_sweeps = -1;
   o->direct_launch = 0;
   o->threads_per_block = 0;
+  o->precision = 0;
+  o->precision_kappa = 1e4f;
 }
 
 int eik_create(int is_tri_mesh, eik_solver** out) {
@@ -236,6 +260,8 @@ int eik_set_options(eik_solver* h, const eik_options* o) {
   if (o->threads_per_block != 0 && o->threads_per_block != 128 && o->threads_per_block != 256 &&
       o->threads_per_block != 512 && o->threads_per_block != 1024)
     return fail(h, EIK_ERR_ARG, "threads_per_block must be 0, 128, 256, 512 or 1024");
+  if (o->precision != 0 && o->precision != 1) return fail(h, EIK_ERR_ARG, "precision must be 0 or 1");
+  if (!(o->precision_kappa >= 1.0f)) return fail(h, EIK_ERR_ARG, "precision_kappa must be at least 1");
   h->opt = *o;
   return EIK_OK;
 }

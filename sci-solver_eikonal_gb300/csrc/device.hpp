@@ -37,6 +37,9 @@ struct SolveStats {
   int fim_launches = 0, check_launches = 0;
   long long h2d_bytes = 0;       // host-to-device bytes the last solve copied (initial state)
   std::vector<int> inst_iters;   // outer iterations run by every instance
+  // precision mode: FP64 residual check after the solve
+  double residual_max_abs = 0, residual_max_rel = 0;
+  long long residual_vertices = 0;
 };
 
 struct SolveOptions {

@@ -99,6 +99,9 @@ struct DevArgs {
   int* inst_iters;
   int* inst_nnext;
   const int* inst_maxit;  // iteration cap of every instance
+  // precision mode (3D): per slot the FP64 product index of its tet (-1: FP32)
+  const int* slot_f64;
+  const double* coef64;
   int* inst_fail;
   int ninst;
   // serving: the loop also ends after an iteration in which some instance
@@ -240,7 +243,7 @@ __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd
 // 3D visit: kCheck = false -> FIMCuda (fim_sweeps sweeps, writes visit outputs);
 //           kCheck = true  -> run_check_neghbor (1 sweep, flags only)
 // ===========================================================================
-template <bool kCheck>
+template <bool kCheck, bool kPrec = false>
 __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
@@ -333,6 +336,24 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
           nw[0] = fminf(TA, tet_update(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC));
           nw[1] = fminf(TB, tet_update(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC));
           nw[2] = fminf(TC, tet_update(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD));
+          if constexpr (kPrec) {
+            // flagged tet: the same four updates again in FP64 from FP64 products
+            // (the FP32 group above stays exactly the FP32 kernel's code)
+            const int f = a.slot_f64[bd.slot_begin + j];
+            if (f >= 0) {
+              const double* g = a.coef64 + 6 * (size_t)f;
+              const double dACBC = g[0], dBCCD = g[1], dACCD = g[2], dADBD = g[3], dACAD = g[4], dBCBD = g[5];
+              const double dADBC = dACBC + dBCCD, dACBD = dACBC + dACCD;
+              const double dCDBD = dADBD - dACBD, dADCD = dADBD - dADBC;
+              const double dCDCD = dADCD - dACCD, dADAD = dADCD + dACAD, dACAC = dACAD - dACCD;
+              const double dBDBD = dBCBD + dCDBD, dBCBC = dBCBD - dBCCD;
+              const double A = TA, B = TB, C = TC, D = TD;
+              nw[3] = fminf(TD, (float)tet_update_f64(A, B, C, dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD));
+              nw[0] = fminf(TA, (float)tet_update_f64(B, D, C, dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC));
+              nw[1] = fminf(TB, (float)tet_update_f64(A, D, C, dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC));
+              nw[2] = fminf(TC, (float)tet_update_f64(A, B, D, dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD));
+            }
+          }
         }
         if (kCheck) {
 #pragma unroll
@@ -912,6 +933,54 @@ __global__ void k_gather_result(const float* Ta, const unsigned char* visited, c
     out[v] = (dim == 3) ? (visited[vblock[r]] ? Ta[r] : 0.0f) : Ta[r];
   }
 }
+// FP64 residual check (precision mode): for every vertex the smallest FP64 tet
+// update over its incident tets, from the final travel times.
+__global__ void k_residual3d(DevArgs a, unsigned long long* cand) {
+  for (int b = blockIdx.x; b < a.nb; b += gridDim.x) {
+    const BlockDesc bd = a.blocks[b];
+    const size_t np = (size_t)bd.nslots_pad;
+    for (int j = threadIdx.x; j < bd.nslots; j += blockDim.x) {
+      const uint2 l = a.lv[bd.slot_begin + j];
+      const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+      int gid[4];
+      double T[4];
+      for (int k = 0; k < 4; ++k) {
+        gid[k] = (id[k] < bd.nowned) ? bd.vbase + id[k] : a.halo[bd.halo_begin + id[k] - bd.nowned];
+        T[k] = (double)a.Ta[gid[k]];
+      }
+      double g[6];
+      const int f = a.slot_f64 ? a.slot_f64[bd.slot_begin + j] : -1;
+      for (int k = 0; k < 6; ++k)
+        g[k] = (f >= 0) ? a.coef64[6 * (size_t)f + k] : (double)a.coef[6 * (size_t)bd.slot_begin + k * np + j];
+      const double ACBC = g[0], BCCD = g[1], ACCD = g[2], ADBD = g[3], ACAD = g[4], BCBD = g[5];
+      const double ADBC = ACBC + BCCD, ACBD = ACBC + ACCD, CDBD = ADBD - ACBD, ADCD = ADBD - ADBC;
+      const double CDCD = ADCD - ACCD, ADAD = ADCD + ACAD, ACAC = ACAD - ACCD, BDBD = BCBD + CDBD;
+      const double BCBC = BCBD - BCCD;
+      double u[4];
+      u[3] = tet_update_f64(T[0], T[1], T[2], ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+      u[0] = tet_update_f64(T[1], T[3], T[2], BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC);
+      u[1] = tet_update_f64(T[0], T[3], T[2], ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC);
+      u[2] = tet_update_f64(T[0], T[1], T[3], ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD);
+      for (int k = 0; k < 4; ++k)
+        if (u[k] >= 0.0) atomicMin(&cand[gid[k]], (unsigned long long)__double_as_longlong(u[k]));
+    }
+  }
+}
+
+// out[0] = max |T - cand|, out[1] = max |T - cand| / T (as FP64 bits), out[2] =
+// vertices above 1e-5 relative; seeds (T = 0) and unreached vertices are skipped.
+__global__ void k_residual_reduce(DevArgs a, const unsigned long long* cand, unsigned long long* out) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x) {
+    const double T = (double)a.Ta[v];
+    const double c = __longlong_as_double((long long)cand[v]);
+    if (!(T > 0.0) || T >= (double)kLarge3DDev || c >= 1e300) continue;
+    const double d = fabs(T - c), rel = d / T;
+    atomicMax(&out[0], (unsigned long long)__double_as_longlong(d));
+    atomicMax(&out[1], (unsigned long long)__double_as_longlong(rel));
+    if (rel > 1e-5) atomicAdd(&out[2], 1ull);
+  }
+}
+
 __global__ void k_gather_hist(const float* h, const int* perm, int nv, float* out) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) out[v] = h[perm[v]];
 }
@@ -1125,6 +1194,11 @@ struct DeviceSolve::Impl {
   std::vector<int> h_seed_ids, h_act, h_vblock, h_done, h_maxit;
   int* seed_ids = nullptr;
   size_t seed_cap = 0;
+  // precision mode
+  int* slot_f64 = nullptr;
+  double* coef64 = nullptr;
+  unsigned long long* res_cand = nullptr;  // nv + 3 words: per-vertex FP64 minimum, then the reduction
+  bool prec = false;
   std::vector<unsigned long long> h_ktime;
   // graph
   cudaGraph_t graph = nullptr;
@@ -1176,9 +1250,14 @@ struct DeviceSolve::Impl {
   void free_all() {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
-                  blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids};
+                  blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids,
+                  slot_f64, coef64, res_cand};
     for (void* p : ps)
       if (p) cudaFree(p);
+    slot_f64 = nullptr;
+    coef64 = nullptr;
+    res_cand = nullptr;
+    prec = false;
     seed_ids = nullptr;
     seed_cap = 0;
     blocks = nullptr; coef = nullptr; lv = nullptr; halo = nullptr; nbr_off = nullptr; nbr = nullptr;
@@ -1221,6 +1300,8 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.inst_nnext = P.inst_nnext; a.inst_fail = P.inst_fail; a.ninst = P.ninst; a.inst_maxit = P.inst_maxit;
     a.serve = serve ? 1 : 0;
     a.pending = P.pending_dev;
+    a.slot_f64 = P.slot_f64;
+    a.coef64 = P.coef64;
     if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
@@ -1235,8 +1316,8 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     void* kv_fim;
     void* kv_chk;
     if (L.dim == 3) {
-      kv_fim = (void*)k_visit3d<false>;
-      kv_chk = (void*)k_visit3d<true>;
+      kv_fim = P.prec ? (void*)k_visit3d<false, true> : (void*)k_visit3d<false>;
+      kv_chk = P.prec ? (void*)k_visit3d<true, true> : (void*)k_visit3d<true>;
     } else if (slot2d) {
       vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
       vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
@@ -1363,6 +1444,16 @@ std::string DeviceSolve::upload(const Layout& L) {
     for (int k = 0; k < L.blocks[b].nowned; ++k) vb[L.blocks[b].vbase + k] = b;
   CK(cudaMemcpyAsync(P.vblock, vb.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(P.perm, L.perm.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  if (!L.slot_f64.empty()) {
+    if (L.dim != 3 || L.slot_f64.size() != (size_t)L.total_slots) return "precision data does not match the layout";
+    if (!(e = dev_alloc(P.slot_f64, L.slot_f64.size())).empty()) return e;
+    if (!(e = dev_alloc(P.coef64, std::max<size_t>(L.coef64.size(), 6))).empty()) return e;
+    if (!(e = dev_alloc(P.res_cand, (size_t)L.nv + 3)).empty()) return e;
+    CK(cudaMemcpyAsync(P.slot_f64, L.slot_f64.data(), sizeof(int) * L.slot_f64.size(), cudaMemcpyHostToDevice, st));
+    if (!L.coef64.empty())
+      CK(cudaMemcpyAsync(P.coef64, L.coef64.data(), sizeof(double) * L.coef64.size(), cudaMemcpyHostToDevice, st));
+    P.prec = true;
+  }
   std::vector<int> bi(L.blk_inst);
   if ((int)bi.size() != L.nb) bi.assign(L.nb, 0);
   CK(cudaMemcpyAsync(P.blk_inst, bi.data(), sizeof(int) * L.nb, cudaMemcpyHostToDevice, st));
@@ -1586,6 +1677,29 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     stats_.check_kernel_ms = (float)(chk * 1e-6);
     stats_.fim_launches = nf;
     stats_.check_launches = nc;
+  }
+  stats_.residual_max_abs = stats_.residual_max_rel = 0;
+  stats_.residual_vertices = 0;
+  if (P.prec && P.res_cand && !out.error) {
+    // FP64 residual of the final travel times (after the timed region)
+    CK(cudaMemsetAsync(P.res_cand, 0x7f, sizeof(unsigned long long) * L.nv, st));
+    CK(cudaMemsetAsync(P.res_cand + L.nv, 0, sizeof(unsigned long long) * 3, st));
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    k_residual3d<<<std::max(1, std::min(L.nb, 8 * nsm)), 256, 0, st>>>(P.args, P.res_cand);
+    k_residual_reduce<<<std::max(1, std::min(4 * nsm, (L.nv + 255) / 256)), 256, 0, st>>>(P.args, P.res_cand,
+                                                                                       P.res_cand + L.nv);
+    CK(cudaGetLastError());
+    unsigned long long r[3];
+    CK(cudaMemcpyAsync(r, P.res_cand + L.nv, sizeof(r), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double d0, d1;
+    std::memcpy(&d0, &r[0], sizeof(double));
+    std::memcpy(&d1, &r[1], sizeof(double));
+    stats_.residual_max_abs = d0;
+    stats_.residual_max_rel = d1;
+    stats_.residual_vertices = (long long)r[2];
   }
   if (out.error) return "device reported error flags " + std::to_string(out.error);
   return "";

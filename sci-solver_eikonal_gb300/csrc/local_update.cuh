@@ -196,6 +196,105 @@ __device__ __forceinline__ float tet_update(float TA, float TB, float TC, float 
   return TD;
 }
 
+// Square root of a non-negative candidate distance for the FP64 update: the
+// argument is formed in FP64 (where the cancellation is), the root taken in FP32
+// (relative error below 1e-7, far inside the scheme's 1e-5 tolerance), which
+// spares the slow FP64 unit.
+__device__ __forceinline__ double sqrt_pos(double x) { return (double)sqrtf((float)x); }
+
+// The same tet update carried out in FP64 (precision mode: slots of sliver or
+// ill-conditioned tets).  Same candidates and order as tet_update; the metric
+// edge products come from FP64 setup values, quotients are FP64 (one reciprocal
+// per candidate face); only the candidate roots use sqrt_pos.
+__device__ __forceinline__ double tet_update_f64(double TA, double TB, double TC, double ACAC, double ACBC,
+                                                 double ACCD, double BCBC, double BCCD, double CDCD) {
+  const double L = (double)kLarge3DDev;
+  if (TA >= L && TB >= L && TC >= L) return L;
+  double p, q, r, l1, l2, l3, delta, TE;
+  double fBC = L, fAB = L, fAC = L, TD = L;
+  const double TAC = TC - TA, TBC = TC - TB, TAB = TB - TA;
+  // face BC
+  p = BCBC * TBC * TBC - BCBC * BCBC;
+  q = (BCCD + BCCD) * TBC * TBC - 2 * BCBC * BCCD;
+  r = TBC * TBC * CDCD - BCCD * BCCD;
+  delta = q * q - 4 * p * r;
+  if (delta >= 0.0) {
+    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p);
+    for (int sg = 0; sg < 2; ++sg) {
+      l2 = (-q + (sg ? -sd : sd)) * i2p;
+      l3 = 1.0 - l2;
+      if (l2 >= 0 && l2 <= 1) {
+        TE = TB * l2 + TC * l3;
+        fBC = fmin(fBC, TE + sqrt_pos((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD)));
+      }
+    }
+  }
+  fBC = fmin(fBC, fmin(TB + sqrt_pos((BCBC + BCCD) + (BCCD + CDCD)), TC + sqrt_pos(CDCD)));
+  // face AB
+  const double gx = ACAC - ACBC, gy = ACBC - BCBC, gz = ACCD - BCCD;
+  p = (TAB * TAB * ACAC - gx * gx) + (BCBC * TAB * TAB - gy * gy) - ((ACBC + ACBC) * TAB * TAB - 2 * gx * gy);
+  q = -(BCBC * TAB * TAB - gy * gy) * 2 + ((ACBC + ACBC) * TAB * TAB - 2 * gx * gy) +
+      ((ACCD + ACCD) * TAB * TAB - 2 * gx * gz) - ((BCCD + BCCD) * TAB * TAB - 2 * gy * gz);
+  r = (TAB * TAB * BCBC - gy * gy) + ((BCCD + BCCD) * TAB * TAB - 2 * gy * gz) + (TAB * TAB * CDCD - gz * gz);
+  delta = q * q - 4 * p * r;
+  if (delta >= 0.0) {
+    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p);
+    for (int sg = 0; sg < 2; ++sg) {
+      l1 = (-q + (sg ? -sd : sd)) * i2p;
+      l2 = 1 - l1;
+      if (l1 >= 0 && l1 <= 1) {
+        TE = TA * l1 + TB * l2;
+        fAB = fmin(fAB, TE + sqrt_pos((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                                  (l1 * ACCD + l2 * BCCD + CDCD)));
+      }
+    }
+  }
+  fAB = fmin(fAB, fmin(TB + sqrt_pos((BCBC + BCCD) + (BCCD + CDCD)), TA + sqrt_pos((ACAC + ACCD) + (ACCD + CDCD))));
+  // face AC
+  p = ACAC * TAC * TAC - ACAC * ACAC;
+  q = (ACCD + ACCD) * TAC * TAC - 2 * ACAC * ACCD;
+  r = TAC * TAC * CDCD - ACCD * ACCD;
+  delta = q * q - 4 * p * r;
+  if (delta >= 0.0) {
+    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p);
+    for (int sg = 0; sg < 2; ++sg) {
+      l1 = (-q + (sg ? -sd : sd)) * i2p;
+      l3 = 1 - l1;
+      if (l1 >= 0 && l1 <= 1) {
+        TE = TA * l1 + TC * l3;
+        fAC = fmin(fAC, TE + sqrt_pos((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD)));
+      }
+    }
+  }
+  fAC = fmin(fAC, fmin(TA + sqrt_pos((ACAC + ACCD) + (ACCD + CDCD)), TC + sqrt_pos(CDCD)));
+  // inside face ABC
+  const double s = TAC * ACBC - TBC * ACAC;
+  const double t = TAC * BCCD - TBC * ACCD;
+  const double h = -(TAC * BCBC - TBC * ACBC);
+  p = (TAC * TAC * ACAC - ACAC * ACAC) * h * h + (BCBC * TAC * TAC - ACBC * ACBC) * s * s +
+      ((ACBC + ACBC) * TAC * TAC - 2 * ACAC * ACBC) * s * h;
+  q = (BCBC * TAC * TAC - ACBC * ACBC) * 2 * s * t + ((ACBC + ACBC) * TAC * TAC - 2 * ACAC * ACBC) * t * h +
+      ((ACCD + ACCD) * TAC * TAC - 2 * ACAC * ACCD) * h * h +
+      ((BCCD + BCCD) * TAC * TAC - 2 * ACBC * ACCD) * s * h;
+  r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - 2 * ACBC * ACCD) * t * h +
+      (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
+  delta = q * q - 4 * p * r;
+  if (delta >= 0.0) {
+    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p), ih = 1.0 / (h + 0.00000001);
+    for (int sg = 0; sg < 2; ++sg) {
+      l1 = (-q + (sg ? -sd : sd)) * i2p;
+      l2 = (s * l1 + t) * ih;
+      l3 = 1 - l1 - l2;
+      if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1) {
+        TE = TA * l1 + TB * l2 + TC * l3;
+        TD = fmin(TD, TE + sqrt_pos((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                                (l1 * ACCD + l2 * BCCD + CDCD)));
+      }
+    }
+  }
+  return fmin(TD, fmin(fBC, fmin(fAB, fAC)));
+}
+
 // Triangle update of corner C from A and B; F is the inverse speed.  Uses the
 // reference's MIN macro semantics ((a)<(b)?(a):(b)), not fminf.
 __device__ __forceinline__ float mn2(float a, float b) { return (a < b) ? a : b; }

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <cstring>
 #include <numeric>
 #include <set>
@@ -652,6 +653,111 @@ void refresh_speed2d(const TriPrep& P, const float* speed_inv, Layout& L) {
   }
 }
 
+double tet_condition(const float* xyz, const int* t, const float* m6) {
+  double P[4][3];
+  for (int k = 0; k < 4; ++k)
+    for (int d = 0; d < 3; ++d) P[k][d] = (double)xyz[3 * (size_t)t[k] + d];
+  double E[3][3];  // columns: B-A, C-A, D-A
+  for (int c = 0; c < 3; ++c)
+    for (int d = 0; d < 3; ++d) E[d][c] = P[c + 1][d] - P[0][d];
+  const double M[3][3] = {{m6[0], m6[1], m6[2]}, {m6[1], m6[3], m6[4]}, {m6[2], m6[4], m6[5]}};
+  double ME[3][3], G[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      ME[i][j] = 0;
+      for (int k = 0; k < 3; ++k) ME[i][j] += M[i][k] * E[k][j];
+    }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      G[i][j] = 0;
+      for (int k = 0; k < 3; ++k) G[i][j] += E[k][i] * ME[k][j];
+    }
+  // adjugate and determinant
+  const double c00 = G[1][1] * G[2][2] - G[1][2] * G[2][1], c01 = G[1][2] * G[2][0] - G[1][0] * G[2][2],
+               c02 = G[1][0] * G[2][1] - G[1][1] * G[2][0];
+  const double det = G[0][0] * c00 + G[0][1] * c01 + G[0][2] * c02;
+  double fro = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) fro += G[i][j] * G[i][j];
+  if (!(det > 0.0)) return std::numeric_limits<double>::infinity();
+  const double adj[9] = {c00, G[0][2] * G[2][1] - G[0][1] * G[2][2], G[0][1] * G[1][2] - G[0][2] * G[1][1],
+                         c01, G[0][0] * G[2][2] - G[0][2] * G[2][0], G[0][2] * G[1][0] - G[0][0] * G[1][2],
+                         c02, G[0][1] * G[2][0] - G[0][0] * G[2][1], G[0][0] * G[1][1] - G[0][1] * G[1][0]};
+  double ifro = 0;
+  for (double a : adj) ifro += a * a;
+  return std::sqrt(fro) * std::sqrt(ifro) / det;
+}
+
+void build_precision3d(const float* xyz, const int* tets, const float* M, double kappa, Layout& L) {
+  L.slot_f64.clear();
+  L.coef64.clear();
+  L.flagged_tets = 0;
+  if (!(kappa > 0) || L.dim != 3) return;
+  std::vector<int> idx(L.ne, -1);
+  for (int t = 0; t < L.ne; ++t) {
+    if (!(tet_condition(xyz, tets + 4 * (size_t)t, M + 6 * (size_t)t) > kappa)) continue;
+    idx[t] = (int)L.flagged_tets++;
+    // the six products of tet_gram, in FP64 from the FP32 inputs
+    const int* v = tets + 4 * (size_t)t;
+    const float* m = M + 6 * (size_t)t;
+    double P[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) P[k][d] = (double)xyz[3 * (size_t)v[k] + d];
+    double AC[3], AD[3], BC[3], CD[3], BD[3];
+    for (int d = 0; d < 3; ++d) {
+      AC[d] = P[2][d] - P[0][d];
+      AD[d] = P[3][d] - P[0][d];
+      BC[d] = P[2][d] - P[1][d];
+      CD[d] = P[3][d] - P[2][d];
+      BD[d] = P[3][d] - P[1][d];
+    }
+    const double md[6] = {m[0], m[1], m[2], m[3], m[4], m[5]};
+    auto uMw = [&md](const double* u, const double* w) {
+      return (u[0] * md[0] + u[1] * md[1] + u[2] * md[2]) * w[0] + (u[0] * md[1] + u[1] * md[3] + u[2] * md[4]) * w[1] +
+             (u[0] * md[2] + u[1] * md[4] + u[2] * md[5]) * w[2];
+    };
+    L.coef64.push_back(uMw(AC, BC));
+    L.coef64.push_back(uMw(BC, CD));
+    L.coef64.push_back(uMw(AC, CD));
+    L.coef64.push_back(uMw(AD, BD));
+    L.coef64.push_back(uMw(AC, AD));
+    L.coef64.push_back(uMw(BC, BD));
+  }
+  // Flagged slots move behind the unflagged ones inside each block's two slot
+  // groups (all corners owned / some corners foreign), so the FP64 updates run in
+  // few warps instead of diverging in most of them.  Slot order inside a block
+  // does not change results: every vertex takes the minimum over its slots.
+  std::vector<int> order;
+  std::vector<float> c6;
+  std::vector<uint16_t> lv4;
+  std::vector<int> el;
+  for (const BlockDesc& d : L.blocks) {
+    order.clear();
+    for (int part = 0; part < 2; ++part) {
+      const int j0 = part ? d.ninside : 0, j1 = part ? d.nslots : d.ninside;
+      for (int pass = 0; pass < 2; ++pass)
+        for (int j = j0; j < j1; ++j) {
+          const int t = L.slot_elem[(size_t)d.slot_begin + j];
+          const bool f = t >= 0 && idx[t] >= 0;
+          if (f == (pass == 1)) order.push_back(j);
+        }
+    }
+    const size_t np = (size_t)d.nslots_pad, sb = (size_t)d.slot_begin;
+    c6.assign(&L.coef[6 * sb], &L.coef[6 * sb] + 6 * np);
+    lv4.assign(&L.lv[4 * sb], &L.lv[4 * sb] + 4 * np);
+    el.assign(&L.slot_elem[sb], &L.slot_elem[sb] + np);
+    for (int j = 0; j < d.nslots; ++j) {
+      const int o = order[j];
+      for (int k = 0; k < 6; ++k) L.coef[6 * sb + k * np + j] = c6[k * np + o];
+      for (int k = 0; k < 4; ++k) L.lv[4 * (sb + j) + k] = lv4[4 * (size_t)o + k];
+      L.slot_elem[sb + j] = el[o];
+    }
+  }
+  L.slot_f64.assign(L.slot_elem.size(), -1);
+  for (size_t s = 0; s < L.slot_elem.size(); ++s)
+    if (L.slot_elem[s] >= 0) L.slot_f64[s] = idx[L.slot_elem[s]];
+}
+
 std::string concat_layouts(const std::vector<const Layout*>& parts, Layout& out) {
   out = Layout();
   if (parts.empty()) return "no instances";
@@ -672,6 +778,15 @@ std::string concat_layouts(const std::vector<const Layout*>& parts, Layout& out)
       out.blocks.push_back(d);
     }
     out.coef.insert(out.coef.end(), p->coef.begin(), p->coef.end());
+    if (!p->slot_f64.empty() || !out.slot_f64.empty()) {
+      // precision data: pad earlier parts with -1, offset this part's indices
+      out.slot_f64.resize((size_t)soff, -1);
+      const int f0 = (int)(out.coef64.size() / 6);
+      if (p->slot_f64.empty()) out.slot_f64.resize((size_t)soff + p->slot_elem.size(), -1);
+      for (int f : p->slot_f64) out.slot_f64.push_back(f >= 0 ? f + f0 : -1);
+      out.coef64.insert(out.coef64.end(), p->coef64.begin(), p->coef64.end());
+      out.flagged_tets += p->flagged_tets;
+    }
     out.lv.insert(out.lv.end(), p->lv.begin(), p->lv.end());
     for (int e : p->slot_elem) out.slot_elem.push_back(e);
     for (int h : p->halo_ids) out.halo_ids.push_back(h + voff);

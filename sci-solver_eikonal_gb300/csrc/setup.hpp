@@ -106,6 +106,11 @@ struct Layout {
   int ninst = 1;
   std::vector<int> blk_inst;      // instance of every block
   std::vector<int> inst_bbeg, inst_vbeg;
+  // 3D precision mode: per slot the index of its tet's FP64 metric edge products
+  // in coef64 (6 doubles each), -1 for tets that stay FP32; empty when off
+  std::vector<int> slot_f64;
+  std::vector<double> coef64;
+  long long flagged_tets = 0;
 };
 
 // One layout holding several independent meshes (same dimension), instance by
@@ -122,6 +127,14 @@ void refresh_gram3d(const float* xyz, const int* tets, const float* M, Layout& L
 std::string build_layout2d(int nv, const float* xyz, const TriPrep& P, const float* speed_inv,
                            const int* labels, int nb, Layout& L);
 void refresh_speed2d(const TriPrep& P, const float* speed_inv, Layout& L);
+
+// Precision mode (3D): flags tets whose metric edge Gram matrix G = E^T M E
+// (E = the edges from the first corner) has ||G||_F ||G^-1||_F > kappa, and stores
+// their six metric edge products computed in FP64 from the FP32 inputs.
+// kappa <= 0 clears the precision data.
+void build_precision3d(const float* xyz, const int* tets, const float* M, double kappa, Layout& L);
+// Condition estimate used for the flagging (FP64; infinite for degenerate tets).
+double tet_condition(const float* xyz, const int* tet, const float* M6);
 
 // Normalise element indices to 0-based like TetMesh::init (tetmesh.cu:27-52):
 // minimum index 0 or 1, anything else is an error.

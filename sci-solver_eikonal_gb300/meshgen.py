@@ -15,6 +15,9 @@
 Vertex numbering is lexicographic (index = i + n*j [+ n*n*k]) so the reference's
 structured-grid tiling applies to the grids.
 """
+import concurrent.futures as _fut
+import os
+
 import numpy as np
 
 
@@ -172,56 +175,98 @@ def _min_dihedral(P):
     return best
 
 
-def sliver_cube(n=49, fraction=0.10, seed=5, max_deg=5.0):
-    """Jittered Kuhn cube whose `fraction` of tets are flattened into slivers: a
-    vertex unique to the tet is not available in a conforming mesh, so the sliver
-    is made by moving one interior vertex of each chosen tet toward the opposite
-    face until the tet's minimum dihedral angle drops below `max_deg` degrees while
-    no tet around that vertex inverts.  Returns xyz, tets, sliver mask."""
+def _tet_volumes(P):
+    return np.einsum("...j,...j->...", np.cross(P[..., 1, :] - P[..., 0, :], P[..., 2, :] - P[..., 0, :]),
+                     P[..., 3, :] - P[..., 0, :])
+
+
+def _has_small_dihedral(P, lim):
+    """True where a tet (... x 4 x 3) has a dihedral angle below `lim` radians."""
+    faces = [(1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)]
+    nr = []
+    for a, b, c in faces:
+        x = np.cross(P[..., b, :] - P[..., a, :], P[..., c, :] - P[..., a, :])
+        nr.append(x / np.maximum(np.linalg.norm(x, axis=-1, keepdims=True), 1e-300))
+    c = np.cos(lim)
+    out = np.zeros(P.shape[:-2], dtype=bool)
+    for x in range(4):
+        for y in range(x + 1, 4):
+            out |= -np.sum(nr[x] * nr[y], axis=-1) > c
+    return out
+
+
+def sliver_cube(n=49, fraction=0.10, seed=5, max_deg=5.0, directions=12,
+                steps=(0.9, 0.95, 0.98, 0.995)):
+    """Jittered Kuhn cube (as kuhn_cube(n, 0.2, seed=1)) with about `fraction` of
+    its tets flattened into slivers: minimum dihedral angle below `max_deg`
+    degrees, every tet keeping its orientation and at least 1e-3 of its volume.
+
+    A conforming mesh has no vertex unique to one tet, so slivers come from moving
+    interior vertices toward the opposite face of a tet of their ring.  Vertices
+    are taken by lattice parity class (same-parity vertices share no tet, so a
+    class moves at once); for each vertex, `directions` random ring tets times
+    `steps` (fractions of the distance to that tet's opposite face) are tried and
+    the valid move that makes the most slivers in the ring is kept.  Classes run in
+    a random order (PCG64 seed `seed`) until the slivers reach the target.
+    Returns xyz (float32), tets, sliver mask (final dihedral test of every tet)."""
     xyz, tets = kuhn_cube(n, 0.2, seed=1)
     xyz = xyz.astype(np.float64)
     rng = np.random.Generator(np.random.PCG64(seed))
     nt = tets.shape[0]
-    chosen = rng.choice(nt, size=int(fraction * nt), replace=False)
-    # vertex -> tets map
+    target = int(fraction * nt)
+    lim = np.deg2rad(max_deg)
+    vol0 = _tet_volumes(xyz[tets])
     order = np.argsort(tets.ravel(), kind="stable")
-    vert_of = tets.ravel()[order]
     tet_of = order // 4
-    starts = np.searchsorted(vert_of, np.arange(xyz.shape[0] + 1))
+    starts = np.searchsorted(tets.ravel()[order], np.arange(xyz.shape[0] + 1))
     ii = np.arange(xyz.shape[0])
     gi, gj, gk = ii % n, (ii // n) % n, ii // (n * n)
     interior = (gi > 0) & (gi < n - 1) & (gj > 0) & (gj < n - 1) & (gk > 0) & (gk < n - 1)
-    moved = np.zeros(xyz.shape[0], dtype=bool)
-    sliver = np.zeros(nt, dtype=bool)
-    lim = np.deg2rad(max_deg)
+    if not interior.any():
+        return xyz.astype(np.float32), tets, np.zeros(nt, dtype=bool)
+    R = int((starts[1:] - starts[:-1])[interior].max())
+    made = int(_has_small_dihedral(xyz[tets], lim).sum())
+    for cls in rng.permutation(8):
+        if made >= target:
+            break
+        sel = np.nonzero(interior & (gi % 2 == (cls & 1)) & (gj % 2 == ((cls >> 1) & 1)) & (gk % 2 == (cls >> 2)))[0]
+        sel = rng.permutation(sel)
+        rings = np.stack([tet_of[starts[v]:starts[v] + R] for v in sel])  # S x R
+        T = tets[rings]
+        pos = T == sel[:, None, None]
+        P0 = xyz[T]
+        v0 = vol0[rings]
+        def trial(r):
+            # the best valid step toward the opposite face of ring tet r, per vertex
+            F = xyz[T[:, r][~pos[:, r]].reshape(len(sel), 3)]
+            nrm = np.cross(F[:, 1] - F[:, 0], F[:, 2] - F[:, 0])
+            nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+            dist = np.einsum("ij,ij->i", xyz[sel] - F[:, 0], nrm)
+            bc = np.zeros(len(sel), dtype=np.int64)
+            bp = xyz[sel].copy()
+            for f in steps:
+                newp = xyz[sel] - (f * dist)[:, None] * nrm
+                P = P0.copy()
+                P[pos] = np.repeat(newp, R, axis=0)
+                vn = _tet_volumes(P)
+                ok = np.all((vn * v0 > 0) & (np.abs(vn) >= 1e-3 * np.abs(v0)), axis=1)
+                cnt = np.where(ok, _has_small_dihedral(P, lim).sum(axis=1), 0)
+                upd = cnt > bc
+                bc[upd] = cnt[upd]
+                bp[upd] = newp[upd]
+            return bc, bp
 
-    def signed_vol(ts):
-        P = xyz[tets[ts]]
-        return np.einsum("ij,ij->i", np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), P[:, 3] - P[:, 0])
-
-    for t in chosen:
-        cand = [v for v in tets[t] if interior[v] and not moved[v]]
-        if not cand:
-            continue
-        v = cand[rng.integers(len(cand))]
-        k = list(tets[t]).index(v)
-        others = [tets[t][m] for m in range(4) if m != k]
-        F = xyz[others]
-        nrm = np.cross(F[1] - F[0], F[2] - F[0])
-        nrm /= np.linalg.norm(nrm)
-        dist = np.dot(xyz[v] - F[0], nrm)
-        ring = tet_of[starts[v]:starts[v + 1]]
-        sign0 = np.sign(signed_vol(ring))
-        orig = xyz[v].copy()
-        ok = False
-        for frac in (0.5, 0.75, 0.85, 0.9, 0.95, 0.97, 0.985):
-            xyz[v] = orig - frac * dist * nrm
-            if np.all(np.sign(signed_vol(ring)) == sign0) and _min_dihedral(xyz[tets[[t]]])[0] < lim:
-                ok = True
-                break
-        if ok:
-            moved[v] = True
-            sliver[t] = True
-        else:
-            xyz[v] = orig
-    return xyz.astype(np.float32), tets, sliver
+        dirs = rng.choice(R, size=min(directions, R), replace=False)
+        with _fut.ThreadPoolExecutor(max_workers=min(len(dirs), os.cpu_count() or 1)) as ex:
+            trials = list(ex.map(trial, dirs))
+        best = np.zeros(len(sel), dtype=np.int64)
+        best_pos = xyz[sel].copy()
+        for bc, bp in trials:  # in direction order: ties keep the earlier direction
+            upd = bc > best
+            best[upd] = bc[upd]
+            best_pos[upd] = bp[upd]
+        take = (best > 0) & (np.cumsum(best) <= max(0, target - made))
+        xyz[sel[take]] = best_pos[take]
+        made = int(_has_small_dihedral(xyz[tets], lim).sum())
+    xyz32 = xyz.astype(np.float32)
+    return xyz32, tets, _has_small_dihedral(xyz32[tets].astype(np.float64), lim)

@@ -1,0 +1,62 @@
+"""Precision mode (eik_options.precision = 1): tets flagged by the condition
+number of their metric edge Gram matrix run their local updates in FP64; the
+rest of the solve is the reference's FP32 arithmetic.  Held against an FP64 run
+of the same scheme (the oracle at precision 64, same partition)."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def prec_case(mg):
+    xyz, tets, sl = mg.sliver_cube(13, 0.10, seed=5)
+    M6 = mg.anisotropic_metrics(tets.shape[0], seed=6)
+    rng = np.random.Generator(np.random.PCG64(8))
+    seeds = rng.choice(xyz.shape[0], 4, replace=False).astype(np.int32)
+    return xyz, tets, sl, M6, seeds
+
+
+def _solve(eik, case, precision, kappa=1e4):
+    xyz, tets, _, M6, seeds = case
+    e = eik.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.initSpeedMtxMultipliers(M6.ravel())
+    e.setSeeds(seeds)
+    e.maxIterations_ = 1000
+    e.precisionMode_ = precision
+    e.precisionKappa_ = kappa
+    e.solveEikonal()
+    return e
+
+
+def test_precision_mode_moves_toward_fp64(need_gpu, eik, O, prec_case):
+    xyz, tets, sl, M6, seeds = prec_case
+    assert sl.mean() > 0.03  # the mesh does carry slivers
+    e32 = _solve(eik, prec_case, 0)
+    emx = _solve(eik, prec_case, 1)
+    lab, nb = e32.getPartition()
+    M = O.metrics_from_speeds(tets.shape[0], M6.ravel())
+    r64 = O.solve3d(xyz, tets, M, lab, nb, seeds, max_iters=1000, precision=64)["result"].astype(np.float64)
+    st = emx.stats()
+    assert st["flagged_tets"] > 0.5 * sl.sum()
+    assert e32.stats()["flagged_tets"] == 0
+    err32 = np.abs(e32.getFinalResult() - r64) / np.maximum(np.abs(r64), 1e-6)
+    errmx = np.abs(emx.getFinalResult() - r64) / np.maximum(np.abs(r64), 1e-6)
+    # FP64 on the flagged tets removes most of the FP32 error
+    assert errmx.mean() < 0.5 * err32.mean(), (errmx.mean(), err32.mean())
+    assert errmx.max() <= err32.max()
+    # the FP64 residual check ran and the solution is a fixed point up to the FIM tolerance
+    assert st["residual_max_rel"] > 0 and st["residual_max_rel"] < 1e-2
+
+
+def test_precision_kernel_without_flags_is_the_fp32_kernel(need_gpu, eik, prec_case):
+    """With nothing flagged the precision kernel takes the FP32 path for every
+    slot and must give the FP32 bits."""
+    e32 = _solve(eik, prec_case, 0)
+    enf = _solve(eik, prec_case, 1, kappa=1e30)
+    assert enf.stats()["flagged_tets"] == 0
+    assert bits_equal(e32.getFinalResult(), enf.getFinalResult())
+    assert e32.numIterations() == enf.numIterations()
