@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--serve-rates", default="50,200,500,1000,2000")
     p.add_argument("--serve-budget-gb", type=float, default=16.0)
     p.add_argument("--batch-count", type=int, default=256)
+    p.add_argument("--no-patterns", action="store_true",
+                   help="c3d only: skip the batched / served / precision summaries added to the line")
     p.add_argument("--launch", default="graph", choices=["graph", "direct"],
                    help="graph: one CUDA-graph launch per solve; direct: kernel by kernel (for ncu)")
     return p.parse_args()
@@ -598,8 +600,46 @@ def main():
         res["cpu_baseline"] = {k: v for k, v in cpu_sample(xyz, tets, metric, seed, labels, nb,
                                                            args.cpu_sample_iters or MAX_ITERS).items()
                                if k in ("value", "unit", "cores", "kind", "sample")}
+    if world == 1 and not args.no_patterns:
+        res.update(pattern_summaries(args, E, torch, local))
     print(json.dumps(res), flush=True)
     return 0
+
+
+def pattern_summaries(args, E, torch, local):
+    """The batched, served and precision workloads, summarised on the same line."""
+    out = {}
+    try:
+        b = bench_batch(args, E, torch, 1, local)
+        out["batched"] = {"workload": BATCH_WORKLOAD, "solves_per_s": b["value"],
+                          "plain_solves_per_s": b["plain"]["solves_per_s"], "ratio": b["batched_over_plain"],
+                          "vertex_updates_per_s": b["vertex_updates_per_s"], "ms_per_batch": b["ms_per_step"],
+                          "latency_ms": b["latency_ms"], "e2e_solves_per_s": b["e2e"]["value"],
+                          "bitwise_mismatches_vs_plain": b["bitwise_mismatches_vs_plain"],
+                          "verts_per_block": b["config"]["verts_per_block"], "clocks": b["clocks"]}
+    except Exception as ex:  # keep the headline line even if a pattern fails
+        out["batched"] = {"error": repr(ex)}
+    try:
+        sv = bench_serve(args, E, torch)
+        out["served"] = {"workload": SERVE_WORKLOAD,
+                         "per_rate": [{k: r[k] for k in ("rate_per_s", "solves_per_s", "p50_ms", "p99_ms")}
+                                      for r in sv["served"]["per_rate"]],
+                         "plain_per_rate": [{k: r[k] for k in ("rate_per_s", "solves_per_s", "p50_ms", "p99_ms")}
+                                            for r in sv["plain"]["per_rate"]],
+                         "ratio_at_top_rate": sv["served_over_plain"], "slots": sv["served"]["slots"],
+                         "device_bytes": sv["served"]["device_bytes"]}
+    except Exception as ex:
+        out["served"] = {"error": repr(ex)}
+    try:
+        pr = bench_prec(args, E, torch)
+        out["precision"] = {"workload": PREC_WORKLOAD, "sliver_fraction": pr["config"]["sliver_fraction"],
+                            "fp32": {k: pr["fp32"][k] for k in ("solve_ms", "error_vs_fp64")},
+                            "mixed": {k: pr["mixed"][k] for k in ("solve_ms", "error_vs_fp64", "flagged_tets",
+                                                                  "residual_max_rel")},
+                            "fp64_oracle_s": pr["fp64_oracle"]["seconds"]}
+    except Exception as ex:
+        out["precision"] = {"error": repr(ex)}
+    return out
 
 
 if __name__ == "__main__":
