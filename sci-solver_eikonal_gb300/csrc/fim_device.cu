@@ -104,6 +104,9 @@ struct DevArgs {
   const double* coef64;
   int* inst_fail;
   int ninst;
+  const int* inst_vbeg;  // renumbered vertex range of every instance (ninst + 1)
+  const int2* chunks;    // (instance, first vertex) of every 2D vertex-test chunk
+  int nchunks;
   // serving: the loop also ends after an iteration in which some instance
   // finished, or once the host raised *pending (requests waiting for admission)
   int serve;
@@ -866,16 +869,25 @@ __device__ __forceinline__ bool last_cta(int* counter) {
 }
 
 // 2D all-vertex convergence test (meshFIM2d_eikonal.cu:804-815) + iteration close
+constexpr int kVertexChunk = 2048;  // vertices per chunk of the 2D all-vertex test
+
 __global__ void k_vertex_test2d(DevArgs a) {
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x) {
-    const int inst = a.blk_inst[a.vblock[v]];
-    if (a.inst_done[inst]) continue;
-    const float cur = a.Ta[v];
-    float diff = a.prev[v] - cur;
-    if (diff < 0.0f) diff = -diff;
-    const bool ok = (diff <= kEps2D) && (cur < kLarge2DDev);
-    if (!ok && a.inst_fail[inst] == 0) atomicOr(&a.inst_fail[inst], 1);
-    a.prev[v] = cur;
+  // chunks of the running instances only (a server's idle slots and finished
+  // batch members cost one flag read per chunk)
+  for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+    const int2 ch = a.chunks[c];
+    if (a.inst_done[ch.x]) continue;  // uniform across the CTA
+    const int v1 = min(ch.y + kVertexChunk, a.inst_vbeg[ch.x + 1]);
+    int bad = 0;
+    for (int v = ch.y + threadIdx.x; v < v1; v += blockDim.x) {
+      const float cur = a.Ta[v];
+      float diff = a.prev[v] - cur;
+      if (diff < 0.0f) diff = -diff;
+      if (!((diff <= kEps2D) && (cur < kLarge2DDev))) bad = 1;
+      a.prev[v] = cur;
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0 && bad && a.inst_fail[ch.x] == 0) atomicOr(&a.inst_fail[ch.x], 1);
   }
   if (last_cta(&a.ctl->done_d)) finish_iteration_cta(a, true);
 }
@@ -1182,6 +1194,9 @@ struct DeviceSolve::Impl {
   int ktime_cap = 0;
   float* out_tmp = nullptr;
   int* blk_inst = nullptr;
+  int* inst_vbeg = nullptr;
+  int2* chunks = nullptr;
+  int nchunks = 0;
   int* inst_done = nullptr;
   int* inst_iters = nullptr;
   int* inst_nnext = nullptr;
@@ -1251,12 +1266,15 @@ struct DeviceSolve::Impl {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
                   blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids,
-                  slot_f64, coef64, res_cand};
+                  slot_f64, coef64, res_cand, inst_vbeg, chunks};
     for (void* p : ps)
       if (p) cudaFree(p);
     slot_f64 = nullptr;
     coef64 = nullptr;
     res_cand = nullptr;
+    inst_vbeg = nullptr;
+    chunks = nullptr;
+    nchunks = 0;
     prec = false;
     seed_ids = nullptr;
     seed_cap = 0;
@@ -1298,6 +1316,9 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.use_cond = 1;
     a.blk_inst = P.blk_inst; a.inst_done = P.inst_done; a.inst_iters = P.inst_iters;
     a.inst_nnext = P.inst_nnext; a.inst_fail = P.inst_fail; a.ninst = P.ninst; a.inst_maxit = P.inst_maxit;
+    a.inst_vbeg = P.inst_vbeg;
+    a.chunks = P.chunks;
+    a.nchunks = P.nchunks;
     a.serve = serve ? 1 : 0;
     a.pending = P.pending_dev;
     a.slot_f64 = P.slot_f64;
@@ -1429,6 +1450,7 @@ std::string DeviceSolve::upload(const Layout& L) {
   if (!(e = dev_alloc(P.blk_inst, (size_t)L.nb)).empty()) return e;
   for (int** t : {&P.inst_done, &P.inst_iters, &P.inst_nnext, &P.inst_fail, &P.inst_maxit})
     if (!(e = dev_alloc(*t, (size_t)P.ninst)).empty()) return e;
+  if (!(e = dev_alloc(P.inst_vbeg, (size_t)P.ninst + 1)).empty()) return e;
   cudaStream_t st = (cudaStream_t)stream_;
   CK(cudaMemcpyAsync(P.blocks, L.blocks.data(), sizeof(BlockDesc) * L.nb, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(P.coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice, st));
@@ -1457,6 +1479,19 @@ std::string DeviceSolve::upload(const Layout& L) {
   std::vector<int> bi(L.blk_inst);
   if ((int)bi.size() != L.nb) bi.assign(L.nb, 0);
   CK(cudaMemcpyAsync(P.blk_inst, bi.data(), sizeof(int) * L.nb, cudaMemcpyHostToDevice, st));
+  std::vector<int> vb0(L.inst_vbeg);
+  if ((int)vb0.size() != P.ninst + 1) vb0 = {0, L.nv};
+  CK(cudaMemcpyAsync(P.inst_vbeg, vb0.data(), sizeof(int) * vb0.size(), cudaMemcpyHostToDevice, st));
+  {
+    std::vector<int2> ch;
+    for (int i = 0; i < P.ninst; ++i)
+      for (int v = vb0[i]; v < vb0[i + 1]; v += kVertexChunk) ch.push_back(make_int2(i, v));
+    P.nchunks = (int)ch.size();
+    if (!(e = dev_alloc(P.chunks, std::max<size_t>(ch.size(), 1))).empty()) return e;
+    if (!ch.empty())
+      CK(cudaMemcpyAsync(P.chunks, ch.data(), sizeof(int2) * ch.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  }
   CK(cudaStreamSynchronize(st));
   P.coef_n = L.coef.size();
   P.max_slots_pad = (L.max_slots + 3) & ~3;
