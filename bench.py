@@ -377,10 +377,18 @@ def bench_serve(args, E, torch):
             per_rate.append({"rate_per_s": rate, "requests": len(comp), "solves_per_s": len(comp) / span,
                              "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                              "errors": sum(1 for c in comp if c["status"] != 0)})
+            if rate == rates[0]:
+                # per pool mesh: median latency at the lowest rate (little queueing)
+                per_rate[-1]["p50_ms_by_mesh"] = [
+                    statistics.median([1e3 * (c["done_s"] - c["submit_s"]) for c in comp if c["mesh"] == i] or [0.0])
+                    for i in ids]
         st = srv.stats()
         srv.close()
         modes[mode] = {"per_rate": per_rate, "setup_s": round(setup_s, 2), "device_bytes": st["device_bytes"],
-                       "slots": [x["slots"] for x in info], "device_loops": st["device_loops"]}
+                       "slots": [x["slots"] for x in info], "device_loops": st["device_loops"],
+                       "arena_busy_s": st["busy_s"], "arena_vertex_updates": st["vertex_updates"],
+                       "arena_vertex_updates_per_busy_s": [u / b if b > 0 else 0.0
+                                                           for u, b in zip(st["vertex_updates"], st["busy_s"])]}
     top = modes["served"]["per_rate"][-1]
     res["value"] = top["solves_per_s"]
     res["ms_per_step"] = 1e3 / top["solves_per_s"]

@@ -269,6 +269,8 @@ typedef struct {
   long long device_bytes;  /* slots of both arenas (layouts + state) */
   int slots_2d, slots_3d;
   long long device_loops;  /* launches of the serving loop */
+  double busy_s[2];        /* 2D, 3D arena: wall seconds inside device loops */
+  long long vertex_updates[2]; /* 2D, 3D arena: vertex updates done */
 } eik_server_stats;
 int eik_server_create(long long hbm_budget_bytes, int max_inflight, int keep_results, eik_server** out);
 /* Adds the handle's mesh, speeds, partition options and max_iterations to the pool

@@ -75,7 +75,8 @@ class EikCompletion(ctypes.Structure):
 class EikServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong), ("queued", ctypes.c_longlong),
                 ("running", ctypes.c_longlong), ("device_bytes", ctypes.c_longlong), ("slots_2d", ctypes.c_int),
-                ("slots_3d", ctypes.c_int), ("device_loops", ctypes.c_longlong)]
+                ("slots_3d", ctypes.c_int), ("device_loops", ctypes.c_longlong),
+                ("busy_s", ctypes.c_double * 2), ("vertex_updates", ctypes.c_longlong * 2)]
 
 
 SIGNATURES = {
@@ -507,7 +508,10 @@ class EikonalServer:
     def stats(self):
         s = EikServerStats()
         self._check(self._lib.eik_server_get_stats(self._h, ctypes.byref(s)))
-        return {f: getattr(s, f) for f, _ in EikServerStats._fields_}
+        out = {f: getattr(s, f) for f, _ in EikServerStats._fields_}
+        out["busy_s"] = list(s.busy_s)
+        out["vertex_updates"] = list(s.vertex_updates)
+        return out
 
 
 def selftest_local_update(which, inputs):

@@ -1990,6 +1990,7 @@ std::string DeviceSolve::serve_run() {
   CK(cudaMemcpy(&out, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
   stats_.iterations = out.iter;
   stats_.error = out.error;
+  stats_.vertex_updates = (long long)out.updates;  // cumulative since serve_setup
   if (out.error) return "device reported error flags " + std::to_string(out.error);
   return "";
 }

@@ -60,6 +60,8 @@ struct Arena {
   std::thread worker;
   long long loops = 0;
   size_t bytes = 0;
+  double busy_s = 0;
+  long long updates = 0;
 };
 
 double seconds_since(std::chrono::steady_clock::time_point t0) {
@@ -185,8 +187,10 @@ void worker_loop(eik_server* S, int ai) {
       *A.pending = 0;
     }
     std::string e;
+    const auto r0 = std::chrono::steady_clock::now();
     if (!adm.empty()) e = A.dev->serve_admit(adm);
     if (e.empty()) e = A.dev->serve_run();
+    const double run_s = seconds_since(r0);
     if (e.empty()) e = A.dev->serve_poll(done, iters);
     std::vector<int> fin;
     if (e.empty()) {
@@ -200,6 +204,8 @@ void worker_loop(eik_server* S, int ai) {
     std::lock_guard<std::mutex> lk(S->mu);
     if (S->stop) return;  // the other arena failed: its worker completed everything
     A.loops++;
+    A.busy_s += run_s;
+    A.updates = A.dev->stats().vertex_updates;
     if (!e.empty()) {
       S->err = "device loop (" + std::string(A.dim == 2 ? "2D" : "3D") + "): " + e;
       S->failed = EIK_ERR_CUDA;
@@ -428,6 +434,10 @@ int eik_server_get_stats(eik_server* s, eik_server_stats* out) {
   out->slots_2d = (int)s->arenas[0].inst_req.size();
   out->slots_3d = (int)s->arenas[1].inst_req.size();
   out->device_loops = s->arenas[0].loops + s->arenas[1].loops;
+  for (int i = 0; i < 2; ++i) {
+    out->busy_s[i] = s->arenas[i].busy_s;
+    out->vertex_updates[i] = s->arenas[i].updates;
+  }
   return EIK_OK;
 }
 
