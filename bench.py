@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--serve-rates", default="50,200,500,1000,2000")
     p.add_argument("--serve-budget-gb", type=float, default=16.0)
     p.add_argument("--batch-count", type=int, default=256)
+    p.add_argument("--batch-vpb", type=int, default=0, help="batch: vertices per block (0 = autotune)")
+    p.add_argument("--no-plain", action="store_true", help="batch: skip the one-at-a-time comparison")
     p.add_argument("--no-patterns", action="store_true",
                    help="c3d only: skip the batched / served / precision summaries added to the line")
     p.add_argument("--launch", default="graph", choices=["graph", "direct"],
@@ -206,10 +208,14 @@ def bench_batch(args, E, torch, world, local):
         e.initSpeedMtxMultipliers(speed)
         e.setSeeds(seeds)
         e.maxIterations_ = MAX_ITERS
+        e.directLaunch_ = 1 if args.launch == "direct" else 0
         solvers.append(e)
     nv_total = sum(w[0].shape[0] for w in work)
     t0 = time.perf_counter()
-    tuned, batch = tune.tune_batch(solvers, reps=2)
+    if args.batch_vpb > 0:
+        tuned, batch = tune.tune_batch(solvers, vpb_candidates=(args.batch_vpb,), reps=1)
+    else:
+        tuned, batch = tune.tune_batch(solvers, reps=2)
     tune_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(batch.stream())
 
@@ -224,7 +230,7 @@ def bench_batch(args, E, torch, world, local):
     sampler = ClockSampler(local)
     sampler.start()
     barrier()
-    times, upd, iters = [], 0, []
+    times, upd, iters, fim_ms, fim_bytes = [], 0, [], 0.0, 0
     for _ in range(args.steps):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
@@ -236,6 +242,10 @@ def bench_batch(args, E, torch, world, local):
         st = batch.stats()
         upd += st["vertex_updates"]
         iters.append(st["iterations"])
+        fim_ms += st["fim_kernel_ms"]
+        # 2D sweep visit: per slot 3 edge lengths + inverse speed (16 B) + corner ids (8 B)
+        fim_bytes += (24 * st["fim_slots"] + 4 * (st["fim_owned"] + st["fim_halo"]) + 4 * st["fim_owned"]
+                      + 4 * st["fim_visits"])
     barrier()
     clocks = sampler.stop()
     batched_ms = statistics.median(times)
@@ -253,7 +263,7 @@ def bench_batch(args, E, torch, world, local):
     # plain: the same solves one at a time (same partitions, each its own handle)
     plain_ms, plain_upd, plain_wall = [], 0, []
     mismatch = 0
-    for k, e in enumerate(solvers):
+    for k, e in enumerate([] if args.no_plain else solvers):
         e.solveEikonal()  # upload + graph build
         t = time.perf_counter()
         e.solveEikonal()
@@ -263,8 +273,10 @@ def bench_batch(args, E, torch, world, local):
         plain_upd += e.stats()["vertex_updates"]
         if not np.array_equal(r.view(np.uint32), res[k].view(np.uint32)):
             mismatch += 1
-    plain_total_ms = sum(plain_ms)
+    plain_total_ms = sum(plain_ms) if plain_ms else float("nan")
     lat = sorted(times)
+    peak, peak_src = measured_hbm_peak()
+    achieved = fim_bytes / (fim_ms * 1e-3) / 1e9 if fim_ms > 0 else 0.0
     return {
         "metric": METRIC, "value": n / (batched_ms * 1e-3), "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms, "higher_is_better": True,
@@ -276,15 +288,36 @@ def bench_batch(args, E, torch, world, local):
         "vertex_updates_per_s": (upd / args.steps) / (batched_ms * 1e-3),
         "plain": {"solves_per_s": n / (plain_total_ms * 1e-3), "ms_total": plain_total_ms,
                   "vertex_updates_per_s": plain_upd / (plain_total_ms * 1e-3),
-                  "e2e_solves_per_s": n / sum(plain_wall)},
+                  "e2e_solves_per_s": n / sum(plain_wall) if plain_wall else float("nan")},
         "batched_over_plain": (n / (batched_ms * 1e-3)) / (n / (plain_total_ms * 1e-3)),
         "bitwise_mismatches_vs_plain": mismatch,
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
         "e2e": {"value": n / statistics.median(e2e), "unit": "solves/s",
                 "h2d_bytes_per_step": int(batch.stats()["h2d_bytes"]), "d2h_bytes_per_step": 4 * nv_total},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profile_traffic("fim2d_slot_batch.md"), "peak_source": peak_src,
+                     "kernel": "k_visit2d_slot<false,7> (block sweeps)",
+                     "kernel_ms_per_step": fim_ms / args.steps},
         "clocks": clocks,
         "gpu_launches": int(1 + 4 * sum(iters)),
     }
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return json.load(open(path))["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch of a kernel, from its committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
+    if os.path.exists(path):
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    return None
 
 
 SERVE_WORKLOAD = ("serving: resident pool of icospheres L5, L6, L7 and L6 with other speeds (2D) and jittered "
