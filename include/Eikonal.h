@@ -52,6 +52,7 @@ class Eikonal {
     keepHistory_ = o.keep_history != 0;
     precisionMode_ = o.precision;
     precisionKappa_ = o.precision_kappa;
+    deviceSetup_ = o.device_setup;
     if (eik_create(isTriMesh ? 1 : 0, &h_) != EIK_OK) throw std::runtime_error("eik_create failed");
   }
   virtual ~Eikonal() { eik_destroy(h_); }
@@ -173,6 +174,8 @@ class Eikonal {
   // metric edge Gram condition number exceeds precisionKappa_, FP64 residual check
   int precisionMode_;
   float precisionKappa_;
+  // 1: 3D block layouts are built on the GPU; 0: on the host
+  int deviceSetup_;
 
  private:
   void check(int rc) const {
@@ -197,6 +200,7 @@ class Eikonal {
     o.keep_history = keepHistory_ ? 1 : 0;
     o.precision = precisionMode_;
     o.precision_kappa = precisionKappa_;
+    o.device_setup = deviceSetup_;
     check(eik_set_options(h_, &o));
   }
   eik_solver* h_ = nullptr;

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "-
               "-ffp-contract=off"]
 
 HOST_SRC = ["setup.cpp", "mesh_io.cpp", "capi.cpp", "serve.cpp"]
-CUDA_SRC = ["fim_device.cu"]
+CUDA_SRC = ["fim_device.cu", "setup_device.cu"]
 HEADERS = ["setup.hpp", "mesh_io.hpp", "device.hpp", "local_update.cuh", "solver_access.hpp"]
 
 

@@ -17,6 +17,9 @@
 
 using namespace eikgb;
 
+// 3D solves build their block layout on the GPU unless eik_options.device_setup = 0
+#define DEVICE_SETUP_DEFAULT 0
+
 struct eik_solver {
   int dim = 3;
   eik_options opt{};
@@ -46,6 +49,10 @@ struct eik_solver {
   std::string lay_key;
   std::string prec_key;  // precision settings the layout's FP64 data was built for
   Layout layout;
+  // 3D layout built on the device: its host part, and what it was built from
+  Layout dlayout;
+  unsigned dlay_mesh = ~0u, dlay_speed = ~0u;
+  std::string dlay_key;
   std::unique_ptr<DeviceSolve> dev;
   bool uploaded = false;
   bool solved = false;
@@ -217,6 +224,49 @@ void fill_stats(eik_stats& s, const SolveStats& st, const Layout& L, float setup
   s.residual_vertices = st.residual_vertices;
 }
 
+// The 3D layout built on the device (build_layout3d_device), cached while the mesh
+// and partition inputs are unchanged; a speed change recomputes the metric terms
+// on the device.  The partition itself stays on the host (make_partition).
+int device_prepare(eik_solver* h) {
+  const std::string key = partition_key(h);
+  if (!h->dev) h->dev.reset(new DeviceSolve);
+  if (h->dlay_mesh != h->mesh_ver || h->dlay_key != key || !h->dev->layout_built_on_device()) {
+    int rc = make_partition(h);
+    if (rc) return rc;
+    std::vector<float> M;
+    tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), M);
+    Built3D b;
+    std::string e = build_layout3d_device(h->nv, h->xyz.data(), h->ne, h->elems.data(), M.data(), h->labels.data(),
+                                          h->nb, (cudaStream_t)h->dev->stream(), b, h->dlayout);
+    if (!e.empty()) {
+      b.release();
+      h->dlay_mesh = ~0u;
+      return fail(h, e.find("too many local") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+    }
+    h->uploaded = false;  // the device now holds this layout, not the host-built one
+    e = h->dev->upload_built(h->dlayout, b);
+    if (!e.empty()) {
+      b.release();
+      h->dlay_mesh = ~0u;
+      return fail(h, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+    }
+    h->dlay_mesh = h->mesh_ver;
+    h->dlay_key = key;
+    h->dlay_speed = h->speed_ver;
+  } else if (h->dlay_speed != h->speed_ver) {
+    std::vector<float> M;
+    tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), M);
+    std::string e = h->dev->refresh_coef_built(M.data());
+    if (!e.empty()) return fail(h, EIK_ERR_CUDA, e);
+    h->dlay_speed = h->speed_ver;
+  }
+  return EIK_OK;
+}
+
+bool use_device_setup(const eik_solver* h) {
+  return h->dim == 3 && h->opt.device_setup == 1 && h->opt.precision == 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -238,6 +288,7 @@ void eik_default_options(eik_options* o) {
   o->threads_per_block = 0;
   o->precision = 0;
   o->precision_kappa = 1e4f;
+  o->device_setup = DEVICE_SETUP_DEFAULT;
 }
 
 int eik_create(int is_tri_mesh, eik_solver** out) {
@@ -262,6 +313,7 @@ int eik_set_options(eik_solver* h, const eik_options* o) {
     return fail(h, EIK_ERR_ARG, "threads_per_block must be 0, 128, 256, 512 or 1024");
   if (o->precision != 0 && o->precision != 1) return fail(h, EIK_ERR_ARG, "precision must be 0 or 1");
   if (!(o->precision_kappa >= 1.0f)) return fail(h, EIK_ERR_ARG, "precision_kappa must be at least 1");
+  if (o->device_setup != 0 && o->device_setup != 1) return fail(h, EIK_ERR_ARG, "device_setup must be 0 or 1");
   h->opt = *o;
   return EIK_OK;
 }
@@ -356,17 +408,23 @@ int eik_solve(eik_solver* h) {
   const float* init = nullptr;
   int rc = resolve_seeds(h, seeds, &init);
   if (rc) return rc;
-  bool new_layout = false;
-  rc = host_prepare(h, &new_layout);
-  if (rc) return rc;
-  if (!h->dev) h->dev.reset(new DeviceSolve);
-  if (new_layout || !h->uploaded) {
-    std::string e = h->dev->upload(h->layout);
-    if (!e.empty()) {
-      h->uploaded = false;
-      return fail(h, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+  const bool on_device = use_device_setup(h);
+  if (on_device) {
+    rc = device_prepare(h);
+    if (rc) return rc;
+  } else {
+    bool new_layout = false;
+    rc = host_prepare(h, &new_layout);
+    if (rc) return rc;
+    if (!h->dev) h->dev.reset(new DeviceSolve);
+    if (new_layout || !h->uploaded || h->dev->layout_built_on_device()) {
+      std::string e = h->dev->upload(h->layout);
+      if (!e.empty()) {
+        h->uploaded = false;
+        return fail(h, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+      }
+      h->uploaded = true;
     }
-    h->uploaded = true;
   }
   std::string e = h->dev->set_seeds(seeds, init);
   if (!e.empty()) return fail(h, EIK_ERR_ARG, e);
@@ -379,7 +437,7 @@ int eik_solve(eik_solver* h) {
   h->solved = true;
   const SolveStats& st = h->dev->stats();
   eik_stats& s = h->stats;
-  fill_stats(s, st, h->layout, std::chrono::duration<float, std::milli>(t1 - t0).count());
+  fill_stats(s, st, on_device ? h->dlayout : h->layout, std::chrono::duration<float, std::milli>(t1 - t0).count());
   if (h->opt.verbose) {
     std::printf("Eikonal GB300: %d blocks, %d iterations, %.3f ms solve, %.3f ms setup\n", h->nb, st.iterations,
                 st.solve_ms, s.setup_ms);

@@ -74,6 +74,32 @@ struct Admission {
   std::vector<int> seeds;
 };
 
+// A 3D block layout built on the device (build_layout3d_device): the arrays a
+// solve reads, plus the inputs kept for coefficient refreshes.  Owned until
+// handed to DeviceSolve::upload_built or released.
+struct Built3D {
+  BlockDesc* blocks = nullptr;
+  float* coef = nullptr;       // 6 per slot, SoA per block
+  uint16_t* lv = nullptr;      // 4 corner local ids per slot
+  int* halo = nullptr;
+  int* nbr_off = nullptr;
+  int* nbr = nullptr;
+  int* vblock = nullptr;       // renumbered vertex -> block
+  int* perm = nullptr;         // original -> renumbered
+  int* slot_elem = nullptr;
+  float* xyz = nullptr;
+  int* tets = nullptr;
+  float* M6 = nullptr;
+  int total_slots = 0, nhalo = 0, nnbr = 0;
+  void release();
+};
+
+// Builds the 3D layout of build_layout3d on the device (same arrays).  L receives
+// the host-side part: block descriptors, renumbering, statistics (no coefficient,
+// corner-id, halo or neighbour arrays).
+std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M6,
+                                  const int* labels, int nb, cudaStream_t st, Built3D& out, Layout& L);
+
 // Device bytes one instance of this layout occupies (layout arrays + state).
 size_t device_footprint(const Layout& L);
 
@@ -88,6 +114,12 @@ class DeviceSolve {
   std::string upload(const Layout& L);
   // Refresh only the per-slot coefficients (speed/metric change).
   std::string upload_coef(const Layout& L);
+  // Take over a device-built 3D layout (L: its host part, kept by the caller).
+  std::string upload_built(const Layout& L, Built3D& b);
+  // Device-built layouts: recompute the per-slot coefficients on the device from
+  // a new per-tet metric (6 entries per tet, host array).
+  std::string refresh_coef_built(const float* M6);
+  bool layout_built_on_device() const;
   // Seeds are original vertex ids.  init_vals (2D only, may be null) are the
   // vertex values the reference's all-vertex convergence test starts from.
   std::string set_seeds(const std::vector<int>& seeds_orig, const float* init_vals);
@@ -126,6 +158,7 @@ class DeviceSolve {
   void* stream() const { return stream_; }
 
  private:
+  std::string finish_upload(const Layout& L, bool layout_on_device);
   struct Impl;
   Impl* p_;
   const Layout* L_ = nullptr;

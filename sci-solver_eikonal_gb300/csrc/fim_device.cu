@@ -1237,6 +1237,7 @@ struct DeviceSolve::Impl {
   std::vector<int> inst_mesh;      // pool mesh of every instance
   int* slot_elem = nullptr;        // element id per slot (instance-local)
   float* host_res = nullptr;       // pinned: results of finished instances
+  bool built = false;              // layout built on the device (src[0], slot_elem kept)
   void free_serve() {
     for (Source& x : src) {
       if (x.xyz) cudaFree(x.xyz);
@@ -1247,6 +1248,7 @@ struct DeviceSolve::Impl {
     src.clear();
     if (slot_elem) cudaFree(slot_elem);
     slot_elem = nullptr;
+    built = false;
     if (host_res) cudaFreeHost(host_res);
     host_res = nullptr;
   }
@@ -1426,6 +1428,7 @@ std::string DeviceSolve::upload(const Layout& L) {
   Impl& P = *p_;
   if (!stream_) return "CUDA stream creation failed (no usable GPU?)";
   P.free_all();
+  P.free_serve();
   L_ = &L;
   P.dim = L.dim;
   P.nv = L.nv;
@@ -1440,6 +1443,67 @@ std::string DeviceSolve::upload(const Layout& L) {
   if (!(e = dev_alloc(P.nbr, L.nbr.size())).empty()) return e;
   if (!(e = dev_alloc(P.vblock, (size_t)L.nv)).empty()) return e;
   if (!(e = dev_alloc(P.perm, (size_t)L.nv)).empty()) return e;
+  cudaStream_t st = (cudaStream_t)stream_;
+  CK(cudaMemcpyAsync(P.blocks, L.blocks.data(), sizeof(BlockDesc) * L.nb, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.lv, L.lv.data(), sizeof(uint16_t) * L.lv.size(), cudaMemcpyHostToDevice, st));
+  if (!L.halo_ids.empty())
+    CK(cudaMemcpyAsync(P.halo, L.halo_ids.data(), sizeof(int) * L.halo_ids.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(P.nbr_off, L.nbr_off.data(), sizeof(int) * L.nbr_off.size(), cudaMemcpyHostToDevice, st));
+  if (!L.nbr.empty())
+    CK(cudaMemcpyAsync(P.nbr, L.nbr.data(), sizeof(int) * L.nbr.size(), cudaMemcpyHostToDevice, st));
+  P.coef_n = L.coef.size();
+  (void)ncoef;
+  return finish_upload(L, false);
+}
+
+std::string DeviceSolve::upload_built(const Layout& L, Built3D& b) {
+  Impl& P = *p_;
+  if (!stream_) return "CUDA stream creation failed (no usable GPU?)";
+  P.free_all();
+  P.free_serve();
+  L_ = &L;
+  P.dim = 3;
+  P.nv = L.nv;
+  P.nb = L.nb;
+  // the device arrays change owner here
+  P.blocks = b.blocks;
+  P.coef = b.coef;
+  P.lv = reinterpret_cast<uint2*>(b.lv);
+  P.halo = b.halo;
+  P.nbr_off = b.nbr_off;
+  P.nbr = b.nbr;
+  P.vblock = b.vblock;
+  P.perm = b.perm;
+  P.slot_elem = b.slot_elem;
+  P.src.assign(1, Impl::Source{});
+  P.src[0].xyz = b.xyz;
+  P.src[0].tets = b.tets;
+  P.src[0].M6 = b.M6;
+  P.coef_n = 6 * (size_t)b.total_slots;
+  P.built = true;
+  b = Built3D();
+  return finish_upload(L, true);
+}
+
+bool DeviceSolve::layout_built_on_device() const { return p_->built; }
+
+std::string DeviceSolve::refresh_coef_built(const float* M6) {
+  Impl& P = *p_;
+  if (!L_ || !P.built || P.src.empty()) return "no device-built layout";
+  const Layout& L = *L_;
+  cudaStream_t st = (cudaStream_t)stream_;
+  CK(cudaMemcpyAsync(P.src[0].M6, M6, sizeof(float) * 6 * (size_t)L.ne, cudaMemcpyHostToDevice, st));
+  k_admit_coef3d<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.slot_elem,
+                                                                    P.src[0].xyz, P.src[0].tets, P.src[0].M6, 1.0f);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  return "";
+}
+
+std::string DeviceSolve::finish_upload(const Layout& L, bool layout_on_device) {
+  Impl& P = *p_;
+  std::string e;
   for (float** t : {&P.Ta, &P.Tb, &P.Tinit, &P.prev, &P.out_tmp})
     if (!(e = dev_alloc(*t, (size_t)L.nv)).empty()) return e;
   for (int** t : {&P.conv, &P.stampA, &P.stampC, &P.list0, &P.list1, &P.list_new})
@@ -1452,20 +1516,14 @@ std::string DeviceSolve::upload(const Layout& L) {
     if (!(e = dev_alloc(*t, (size_t)P.ninst)).empty()) return e;
   if (!(e = dev_alloc(P.inst_vbeg, (size_t)P.ninst + 1)).empty()) return e;
   cudaStream_t st = (cudaStream_t)stream_;
-  CK(cudaMemcpyAsync(P.blocks, L.blocks.data(), sizeof(BlockDesc) * L.nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.lv, L.lv.data(), sizeof(uint16_t) * L.lv.size(), cudaMemcpyHostToDevice, st));
-  if (!L.halo_ids.empty())
-    CK(cudaMemcpyAsync(P.halo, L.halo_ids.data(), sizeof(int) * L.halo_ids.size(), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.nbr_off, L.nbr_off.data(), sizeof(int) * L.nbr_off.size(), cudaMemcpyHostToDevice, st));
-  if (!L.nbr.empty())
-    CK(cudaMemcpyAsync(P.nbr, L.nbr.data(), sizeof(int) * L.nbr.size(), cudaMemcpyHostToDevice, st));
   std::vector<int>& vb = P.h_vblock;
   vb.assign(L.nv, 0);
   for (int b = 0; b < L.nb; ++b)
     for (int k = 0; k < L.blocks[b].nowned; ++k) vb[L.blocks[b].vbase + k] = b;
-  CK(cudaMemcpyAsync(P.vblock, vb.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(P.perm, L.perm.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  if (!layout_on_device) {
+    CK(cudaMemcpyAsync(P.vblock, vb.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(P.perm, L.perm.data(), sizeof(int) * L.nv, cudaMemcpyHostToDevice, st));
+  }
   if (!L.slot_f64.empty()) {
     if (L.dim != 3 || L.slot_f64.size() != (size_t)L.total_slots) return "precision data does not match the layout";
     if (!(e = dev_alloc(P.slot_f64, L.slot_f64.size())).empty()) return e;
@@ -1493,11 +1551,10 @@ std::string DeviceSolve::upload(const Layout& L) {
     CK(cudaStreamSynchronize(st));
   }
   CK(cudaStreamSynchronize(st));
-  P.coef_n = L.coef.size();
   P.max_slots_pad = (L.max_slots + 3) & ~3;
   P.max_local = std::max(L.max_local, 1);
   P.max_owned = std::max(L.max_owned, 1);
-  P.smem = smem_bytes(ncoef, P.max_slots_pad, P.max_local, P.max_owned);
+  P.smem = smem_bytes((L.dim == 3) ? 6 : 4, P.max_slots_pad, P.max_local, P.max_owned);
   int dev = 0, maxsm = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));

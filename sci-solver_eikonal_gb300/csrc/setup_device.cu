@@ -1,0 +1,487 @@
+// setup_device.cu — the 3D block layout built on the GPU.
+//
+// Same layout as build_layout3d (setup.cpp), from the same inputs (coordinates,
+// tets, per-tet metric, partition labels), with sorts and scans instead of the
+// host's per-block lists:
+//   1. owned-vertex renumbering: stable sort of vertex ids by block label
+//      (ascending original id inside a block, the reference's m_PartitionInVerts
+//      order; meshFIM3dEikonal.cu:568-648);
+//   2. element slots: every tet emits (block, inside|shared) keys — one for a tet
+//      inside a block, one per distinct block for a shared tet — and a stable sort
+//      puts each block's inside tets first, then its shared tets, both in
+//      ascending tet id (m_PartitionTets / m_PartitionNbTets order);
+//   3. halo lists: (block, renumbered id) keys of foreign corners, sorted and
+//      made unique, so every block's halo is ascending in renumbered id;
+//   4. corner local ids (owned: offset in the block; halo: position found by
+//      binary search in the block's halo list) and the six metric edge products
+//      per slot, in the host build's operation order (gettetmem / vMv);
+//   5. the block-neighbour graph: sorted unique block pairs of shared tets.
+// The result equals the host layout's arrays.  Device sorts, scans and
+// selections come from CUB (part of the CUDA toolkit).
+#include <cuda_runtime.h>
+
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "device.hpp"
+
+namespace eikgb {
+namespace {
+
+#define CKS(x)                                                                          \
+  do {                                                                                  \
+    cudaError_t e_ = (x);                                                               \
+    if (e_ != cudaSuccess) return std::string(#x ": ") + cudaGetErrorString(e_);       \
+  } while (0)
+
+constexpr int kThreads = 256;
+inline int grid_for(long long n) {
+  return (int)std::max(1LL, std::min(65535LL * 8, (n + kThreads - 1) / kThreads));
+}
+
+__global__ void k_iota(int* a, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = i;
+}
+
+__global__ void k_count_labels(const int* lab, int n, int* cnt) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(&cnt[lab[i]], 1);
+}
+
+// perm[iperm[n]] = n; vblock[n] = block of renumbered vertex n
+__global__ void k_perm(const int* iperm, const int* lab_sorted, int nv, int* perm, int* vblock) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nv; n += gridDim.x * blockDim.x) {
+    perm[iperm[n]] = n;
+    vblock[n] = lab_sorted[n];
+  }
+}
+
+// distinct sorted labels of a tet's corners
+__device__ __forceinline__ int tet_labels(const int* tets, const int* lab, int t, int ls[4]) {
+  int n = 0;
+  for (int k = 0; k < 4; ++k) {
+    const int l = lab[tets[4 * (size_t)t + k]];
+    bool seen = false;
+    for (int j = 0; j < n; ++j) seen |= (ls[j] == l);
+    if (!seen) ls[n++] = l;
+  }
+  for (int x = 1; x < n; ++x)
+    for (int y = x; y > 0 && ls[y - 1] > ls[y]; --y) {
+      const int s = ls[y - 1];
+      ls[y - 1] = ls[y];
+      ls[y] = s;
+    }
+  return n;
+}
+
+// per tet: slot keys emitted (1 inside / n shared) and neighbour pairs n(n-1)
+__global__ void k_tet_counts(const int* tets, const int* lab, int nt, int* nslot, int* npair) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    int ls[4];
+    const int n = tet_labels(tets, lab, t, ls);
+    nslot[t] = n;
+    npair[t] = n * (n - 1);
+  }
+}
+
+__global__ void k_tet_emit(const int* tets, const int* lab, int nt, const int* slot_off, const int* pair_off,
+                           unsigned* key, int* val, unsigned long long* pairs) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    int ls[4];
+    const int n = tet_labels(tets, lab, t, ls);
+    int o = slot_off[t];
+    if (n == 1) {
+      key[o] = 2u * (unsigned)ls[0];
+      val[o] = t;
+    } else {
+      for (int j = 0; j < n; ++j) {
+        key[o + j] = 2u * (unsigned)ls[j] + 1u;
+        val[o + j] = t;
+      }
+    }
+    o = pair_off[t];
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b)
+        if (a != b) pairs[o++] = ((unsigned long long)(unsigned)ls[a] << 32) | (unsigned)ls[b];
+  }
+}
+
+__global__ void k_count_keys(const unsigned* key, int n, int* cnt) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(&cnt[key[i]], 1);
+}
+
+__global__ void k_pad_counts(const int* keycnt, int nb, int* padded) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
+    padded[b] = (keycnt[2 * b] + keycnt[2 * b + 1] + 3) & ~3;
+}
+
+// BlockDesc of every block except the halo fields
+__global__ void k_block_desc(const int* keycnt, const int* vbase, const int* slot_begin, int nb, BlockDesc* bd) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    BlockDesc d;
+    d.ninside = keycnt[2 * b];
+    d.nslots = keycnt[2 * b] + keycnt[2 * b + 1];
+    d.nslots_pad = (d.nslots + 3) & ~3;
+    d.slot_begin = slot_begin[b];
+    d.vbase = vbase[b];
+    d.nowned = vbase[b + 1] - vbase[b];
+    d.halo_begin = 0;
+    d.nhalo = 0;
+    bd[b] = d;
+  }
+}
+
+// sorted pair p -> slot: slot_elem, and the foreign-corner keys of the slot
+__global__ void k_place(const unsigned* key, const int* val, int np, const int* keybeg, const BlockDesc* bd,
+                        const int* tets, const int* lab, const int* perm, int* slot_elem, int* slot_of,
+                        unsigned long long* hkeys) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const int b = (int)(key[p] >> 1);
+    const int t = val[p];
+    const int s = bd[b].slot_begin + (p - keybeg[2 * b]);
+    slot_elem[s] = t;
+    slot_of[p] = s;
+    for (int k = 0; k < 4; ++k) {
+      const int v = tets[4 * (size_t)t + k];
+      hkeys[4 * (size_t)p + k] =
+          (lab[v] != b) ? (((unsigned long long)(unsigned)b << 32) | (unsigned)perm[v]) : ~0ull;
+    }
+  }
+}
+
+__global__ void k_count_halo(const unsigned long long* uk, int n, int* cnt) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (uk[i] != ~0ull) atomicAdd(&cnt[(int)(uk[i] >> 32)], 1);
+}
+
+__global__ void k_halo_ids(const unsigned long long* uk, int n, int* halo) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (uk[i] != ~0ull) halo[i] = (int)(uk[i] & 0xffffffffu);
+}
+
+__global__ void k_halo_desc(const int* hcnt, const int* hbeg, int nb, BlockDesc* bd, int* too_many) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    bd[b].halo_begin = hbeg[b];
+    bd[b].nhalo = hcnt[b];
+    if (bd[b].nowned + hcnt[b] > 32767) atomicOr(too_many, 1);
+  }
+}
+
+// the host build's tet_gram product u^T M w: float operations one at a time, in
+// its order
+__device__ __forceinline__ float uMw_host(const float* u, const float* m, const float* w) {
+  const float x = __fadd_rn(__fadd_rn(__fmul_rn(u[0], m[0]), __fmul_rn(u[1], m[1])), __fmul_rn(u[2], m[2]));
+  const float y = __fadd_rn(__fadd_rn(__fmul_rn(u[0], m[1]), __fmul_rn(u[1], m[3])), __fmul_rn(u[2], m[4]));
+  const float z = __fadd_rn(__fadd_rn(__fmul_rn(u[0], m[2]), __fmul_rn(u[1], m[4])), __fmul_rn(u[2], m[5]));
+  return __fadd_rn(__fadd_rn(__fmul_rn(x, w[0]), __fmul_rn(y, w[1])), __fmul_rn(z, w[2]));
+}
+
+// corner local ids and the six metric edge products of every slot
+__global__ void k_slot_fill(const unsigned* key, const int* val, const int* slot_of, int np, const BlockDesc* bd,
+                            const int* tets, const int* lab, const int* perm, const int* halo, const float* xyz,
+                            const float* M6, uint16_t* lv, float* coef) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const int b = (int)(key[p] >> 1);
+    const int t = val[p];
+    const int s = slot_of[p];
+    const BlockDesc d = bd[b];
+    const int* hl = halo + d.halo_begin;
+    float P[4][3];
+    for (int k = 0; k < 4; ++k) {
+      const int v = tets[4 * (size_t)t + k];
+      const int nvid = perm[v];
+      int lid;
+      if (lab[v] == b) {
+        lid = nvid - d.vbase;
+      } else {
+        int lo = 0, hi = d.nhalo - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (hl[mid] < nvid) lo = mid + 1;
+          else hi = mid;
+        }
+        lid = d.nowned + lo;
+      }
+      lv[4 * (size_t)s + k] = (uint16_t)lid;
+      for (int c = 0; c < 3; ++c) P[k][c] = xyz[3 * (size_t)v + c];
+    }
+    float m[6];
+    for (int q = 0; q < 6; ++q) m[q] = M6[6 * (size_t)t + q];
+    float AC[3], AD[3], BC[3], CD[3], BD[3];
+    for (int c = 0; c < 3; ++c) {
+      AC[c] = __fsub_rn(P[2][c], P[0][c]);
+      AD[c] = __fsub_rn(P[3][c], P[0][c]);
+      BC[c] = __fsub_rn(P[2][c], P[1][c]);
+      CD[c] = __fsub_rn(P[3][c], P[2][c]);
+      BD[c] = __fsub_rn(P[3][c], P[1][c]);
+    }
+    const size_t np_ = (size_t)d.nslots_pad;
+    float* base = coef + 6 * (size_t)d.slot_begin + (s - d.slot_begin);
+    base[0 * np_] = uMw_host(AC, m, BC);
+    base[1 * np_] = uMw_host(BC, m, CD);
+    base[2 * np_] = uMw_host(AC, m, CD);
+    base[3 * np_] = uMw_host(AD, m, BD);
+    base[4 * np_] = uMw_host(AC, m, AD);
+    base[5 * np_] = uMw_host(BC, m, BD);
+  }
+}
+
+__global__ void k_count_nbr(const unsigned long long* uk, int n, int* cnt) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(&cnt[(int)(uk[i] >> 32)], 1);
+}
+
+__global__ void k_nbr_ids(const unsigned long long* uk, int n, int* nbr) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    nbr[i] = (int)(uk[i] & 0xffffffffu);
+}
+
+// temporary device buffers of one build, freed on every exit
+struct Scratch {
+  std::vector<void*> ptrs;
+  ~Scratch() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  std::string get(T*& p, size_t n) {
+    p = nullptr;
+    CKS(cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)));
+    ptrs.push_back(p);
+    return "";
+  }
+};
+
+template <typename T>
+std::string keep(T*& p, size_t n) {
+  p = nullptr;
+  CKS(cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)));
+  return "";
+}
+
+int bits_for(unsigned long long maxval) {
+  int b = 1;
+  while (b < 64 && (maxval >> b) != 0) ++b;
+  return b;
+}
+
+std::string exclusive_scan(Scratch& S, const int* in, int* out, int n, cudaStream_t st) {
+  size_t tb = 0;
+  CKS(cub::DeviceScan::ExclusiveSum(nullptr, tb, in, out, n, st));
+  unsigned char* tmp;
+  std::string e = S.get(tmp, tb);
+  if (!e.empty()) return e;
+  CKS(cub::DeviceScan::ExclusiveSum(tmp, tb, in, out, n, st));
+  return "";
+}
+
+template <typename K, typename V>
+std::string sort_pairs(Scratch& S, const K* kin, K* kout, const V* vin, V* vout, int n, int end_bit,
+                       cudaStream_t st) {
+  size_t tb = 0;
+  CKS(cub::DeviceRadixSort::SortPairs(nullptr, tb, kin, kout, vin, vout, n, 0, end_bit, st));
+  unsigned char* tmp;
+  std::string e = S.get(tmp, tb);
+  if (!e.empty()) return e;
+  CKS(cub::DeviceRadixSort::SortPairs(tmp, tb, kin, kout, vin, vout, n, 0, end_bit, st));
+  return "";
+}
+
+// sorted unique 64-bit keys: out receives them, *count their number
+std::string sort_unique(Scratch& S, const unsigned long long* in, unsigned long long* sorted,
+                        unsigned long long* out, int n, int* d_count, int* count, cudaStream_t st) {
+  size_t tb = 0;
+  CKS(cub::DeviceRadixSort::SortKeys(nullptr, tb, in, sorted, n, 0, 64, st));
+  unsigned char* tmp;
+  std::string e = S.get(tmp, tb);
+  if (!e.empty()) return e;
+  CKS(cub::DeviceRadixSort::SortKeys(tmp, tb, in, sorted, n, 0, 64, st));
+  size_t tb2 = 0;
+  CKS(cub::DeviceSelect::Unique(nullptr, tb2, sorted, out, d_count, n, st));
+  unsigned char* tmp2;
+  if (!(e = S.get(tmp2, tb2)).empty()) return e;
+  CKS(cub::DeviceSelect::Unique(tmp2, tb2, sorted, out, d_count, n, st));
+  CKS(cudaMemcpyAsync(count, d_count, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CKS(cudaStreamSynchronize(st));
+  return "";
+}
+
+}  // namespace
+
+void Built3D::release() {
+  void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, slot_elem, xyz, tets, M6};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  *this = Built3D();
+}
+
+std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M6,
+                                  const int* labels, int nb, cudaStream_t st, Built3D& out, Layout& L) {
+  out.release();
+  L = Layout();
+  if (nv <= 0 || nt <= 0 || nb <= 0) return "empty mesh";
+  for (int v = 0; v < nv; ++v)
+    if (labels[v] < 0 || labels[v] >= nb) return "partition label out of range";
+  Scratch S;
+  std::string e;
+  // inputs, kept: a speed change recomputes the metric terms from them
+  if (!(e = keep(out.xyz, 3 * (size_t)nv)).empty() || !(e = keep(out.tets, 4 * (size_t)nt)).empty() ||
+      !(e = keep(out.M6, 6 * (size_t)nt)).empty())
+    return e;
+  int* d_lab;
+  if (!(e = S.get(d_lab, nv)).empty()) return e;
+  CKS(cudaMemcpyAsync(out.xyz, xyz, sizeof(float) * 3 * (size_t)nv, cudaMemcpyHostToDevice, st));
+  CKS(cudaMemcpyAsync(out.tets, tets, sizeof(int) * 4 * (size_t)nt, cudaMemcpyHostToDevice, st));
+  CKS(cudaMemcpyAsync(out.M6, M6, sizeof(float) * 6 * (size_t)nt, cudaMemcpyHostToDevice, st));
+  CKS(cudaMemcpyAsync(d_lab, labels, sizeof(int) * nv, cudaMemcpyHostToDevice, st));
+
+  // 1. owned-vertex renumbering
+  int *d_ids, *d_iperm, *d_lab_sorted, *d_cnt, *d_vbase;
+  if (!(e = S.get(d_ids, nv)).empty() || !(e = S.get(d_iperm, nv)).empty() ||
+      !(e = S.get(d_lab_sorted, nv)).empty() || !(e = S.get(d_cnt, nb + 1)).empty() ||
+      !(e = S.get(d_vbase, nb + 1)).empty() || !(e = keep(out.perm, nv)).empty() ||
+      !(e = keep(out.vblock, nv)).empty())
+    return e;
+  k_iota<<<grid_for(nv), kThreads, 0, st>>>(d_ids, nv);
+  if (!(e = sort_pairs(S, d_lab, d_lab_sorted, d_ids, d_iperm, nv, bits_for((unsigned long long)nb), st)).empty())
+    return e;
+  CKS(cudaMemsetAsync(d_cnt, 0, sizeof(int) * (nb + 1), st));
+  k_count_labels<<<grid_for(nv), kThreads, 0, st>>>(d_lab, nv, d_cnt);
+  if (!(e = exclusive_scan(S, d_cnt, d_vbase, nb + 1, st)).empty()) return e;
+  k_perm<<<grid_for(nv), kThreads, 0, st>>>(d_iperm, d_lab_sorted, nv, out.perm, out.vblock);
+
+  // 2. element slots and neighbour pairs
+  int *d_nslot, *d_npair, *d_slot_off, *d_pair_off;
+  if (!(e = S.get(d_nslot, nt + 1)).empty() || !(e = S.get(d_npair, nt + 1)).empty() ||
+      !(e = S.get(d_slot_off, nt + 1)).empty() || !(e = S.get(d_pair_off, nt + 1)).empty())
+    return e;
+  CKS(cudaMemsetAsync(d_nslot + nt, 0, sizeof(int), st));
+  CKS(cudaMemsetAsync(d_npair + nt, 0, sizeof(int), st));
+  k_tet_counts<<<grid_for(nt), kThreads, 0, st>>>(out.tets, d_lab, nt, d_nslot, d_npair);
+  if (!(e = exclusive_scan(S, d_nslot, d_slot_off, nt + 1, st)).empty()) return e;
+  if (!(e = exclusive_scan(S, d_npair, d_pair_off, nt + 1, st)).empty()) return e;
+  int np = 0, npairs = 0;
+  CKS(cudaMemcpyAsync(&np, d_slot_off + nt, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CKS(cudaMemcpyAsync(&npairs, d_pair_off + nt, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CKS(cudaStreamSynchronize(st));
+  unsigned *d_key, *d_key_s;
+  int *d_val, *d_val_s;
+  unsigned long long *d_pairs, *d_pairs_s;
+  if (!(e = S.get(d_key, np)).empty() || !(e = S.get(d_key_s, np)).empty() || !(e = S.get(d_val, np)).empty() ||
+      !(e = S.get(d_val_s, np)).empty() || !(e = S.get(d_pairs, npairs)).empty() ||
+      !(e = S.get(d_pairs_s, npairs)).empty())
+    return e;
+  k_tet_emit<<<grid_for(nt), kThreads, 0, st>>>(out.tets, d_lab, nt, d_slot_off, d_pair_off, d_key, d_val, d_pairs);
+  if (!(e = sort_pairs(S, d_key, d_key_s, d_val, d_val_s, np, bits_for(2ull * (unsigned long long)nb), st)).empty())
+    return e;
+  int *d_keycnt, *d_keybeg, *d_pad, *d_slot_begin;
+  if (!(e = S.get(d_keycnt, 2 * (size_t)nb + 1)).empty() || !(e = S.get(d_keybeg, 2 * (size_t)nb + 1)).empty() ||
+      !(e = S.get(d_pad, nb + 1)).empty() || !(e = S.get(d_slot_begin, nb + 1)).empty())
+    return e;
+  CKS(cudaMemsetAsync(d_keycnt, 0, sizeof(int) * (2 * (size_t)nb + 1), st));
+  k_count_keys<<<grid_for(np), kThreads, 0, st>>>(d_key_s, np, d_keycnt);
+  if (!(e = exclusive_scan(S, d_keycnt, d_keybeg, 2 * nb + 1, st)).empty()) return e;
+  CKS(cudaMemsetAsync(d_pad + nb, 0, sizeof(int), st));
+  k_pad_counts<<<grid_for(nb), kThreads, 0, st>>>(d_keycnt, nb, d_pad);
+  if (!(e = exclusive_scan(S, d_pad, d_slot_begin, nb + 1, st)).empty()) return e;
+  int total_slots = 0;
+  CKS(cudaMemcpyAsync(&total_slots, d_slot_begin + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (!(e = keep(out.blocks, nb)).empty()) return e;
+  k_block_desc<<<grid_for(nb), kThreads, 0, st>>>(d_keycnt, d_vbase, d_slot_begin, nb, out.blocks);
+  CKS(cudaStreamSynchronize(st));
+  if (!(e = keep(out.slot_elem, total_slots)).empty() || !(e = keep(out.lv, 4 * (size_t)total_slots)).empty() ||
+      !(e = keep(out.coef, 6 * (size_t)total_slots)).empty())
+    return e;
+  CKS(cudaMemsetAsync(out.slot_elem, 0xff, sizeof(int) * (size_t)total_slots, st));
+  CKS(cudaMemsetAsync(out.lv, 0, sizeof(uint16_t) * 4 * (size_t)total_slots, st));
+  CKS(cudaMemsetAsync(out.coef, 0, sizeof(float) * 6 * (size_t)total_slots, st));
+
+  // 3. halo lists
+  int *d_slot_of, *d_cnt1;
+  unsigned long long *d_hk, *d_hk_s, *d_hk_u;
+  if (!(e = S.get(d_slot_of, np)).empty() || !(e = S.get(d_hk, 4 * (size_t)np)).empty() ||
+      !(e = S.get(d_hk_s, 4 * (size_t)np)).empty() || !(e = S.get(d_hk_u, 4 * (size_t)np)).empty() ||
+      !(e = S.get(d_cnt1, 1)).empty())
+    return e;
+  k_place<<<grid_for(np), kThreads, 0, st>>>(d_key_s, d_val_s, np, d_keybeg, out.blocks, out.tets, d_lab, out.perm,
+                                             out.slot_elem, d_slot_of, d_hk);
+  int nu = 0;
+  if (!(e = sort_unique(S, d_hk, d_hk_s, d_hk_u, 4 * np, d_cnt1, &nu, st)).empty()) return e;
+  int *d_hcnt, *d_hbeg, *d_too;
+  if (!(e = S.get(d_hcnt, nb + 1)).empty() || !(e = S.get(d_hbeg, nb + 1)).empty() || !(e = S.get(d_too, 1)).empty())
+    return e;
+  CKS(cudaMemsetAsync(d_hcnt, 0, sizeof(int) * (nb + 1), st));
+  CKS(cudaMemsetAsync(d_too, 0, sizeof(int), st));
+  k_count_halo<<<grid_for(nu), kThreads, 0, st>>>(d_hk_u, nu, d_hcnt);
+  if (!(e = exclusive_scan(S, d_hcnt, d_hbeg, nb + 1, st)).empty()) return e;
+  int nhalo_total = 0;
+  CKS(cudaMemcpyAsync(&nhalo_total, d_hbeg + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CKS(cudaStreamSynchronize(st));
+  if (!(e = keep(out.halo, nhalo_total)).empty()) return e;
+  k_halo_ids<<<grid_for(nu), kThreads, 0, st>>>(d_hk_u, nu, out.halo);  // the owned-corner key sorts last
+  k_halo_desc<<<grid_for(nb), kThreads, 0, st>>>(d_hcnt, d_hbeg, nb, out.blocks, d_too);
+
+  // 4. corner local ids and metric edge products
+  k_slot_fill<<<grid_for(np), kThreads, 0, st>>>(d_key_s, d_val_s, d_slot_of, np, out.blocks, out.tets, d_lab,
+                                                 out.perm, out.halo, out.xyz, out.M6, out.lv, out.coef);
+
+  // 5. block-neighbour graph (sorted unique pairs -> CSR)
+  int nn = 0;
+  if (!(e = keep(out.nbr_off, nb + 1)).empty()) return e;
+  if (npairs > 0) {
+    unsigned long long* d_pu;
+    if (!(e = S.get(d_pu, npairs)).empty()) return e;
+    if (!(e = sort_unique(S, d_pairs, d_pairs_s, d_pu, npairs, d_cnt1, &nn, st)).empty()) return e;
+    int* d_ncnt;
+    if (!(e = S.get(d_ncnt, nb + 1)).empty()) return e;
+    CKS(cudaMemsetAsync(d_ncnt, 0, sizeof(int) * (nb + 1), st));
+    k_count_nbr<<<grid_for(nn), kThreads, 0, st>>>(d_pu, nn, d_ncnt);
+    if (!(e = exclusive_scan(S, d_ncnt, out.nbr_off, nb + 1, st)).empty()) return e;
+    if (!(e = keep(out.nbr, nn)).empty()) return e;
+    k_nbr_ids<<<grid_for(nn), kThreads, 0, st>>>(d_pu, nn, out.nbr);
+  } else {
+    CKS(cudaMemsetAsync(out.nbr_off, 0, sizeof(int) * (nb + 1), st));
+    if (!(e = keep(out.nbr, 1)).empty()) return e;
+  }
+  CKS(cudaGetLastError());
+
+  // host part of the layout
+  int too = 0;
+  L.dim = 3;
+  L.nv = nv;
+  L.ne = nt;
+  L.nb = nb;
+  L.total_slots = total_slots;
+  L.blocks.resize(nb);
+  L.perm.resize(nv);
+  CKS(cudaMemcpyAsync(&too, d_too, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CKS(cudaMemcpyAsync(L.blocks.data(), out.blocks, sizeof(BlockDesc) * nb, cudaMemcpyDeviceToHost, st));
+  CKS(cudaMemcpyAsync(L.perm.data(), out.perm, sizeof(int) * nv, cudaMemcpyDeviceToHost, st));
+  CKS(cudaStreamSynchronize(st));
+  if (too) return "block has too many local vertices (limit 32767)";
+  L.iperm.assign(nv, 0);
+  for (int v = 0; v < nv; ++v) L.iperm[L.perm[v]] = v;
+  double sl = 0, hl = 0;
+  for (const BlockDesc& d : L.blocks) {
+    L.max_slots = std::max(L.max_slots, d.nslots);
+    L.max_owned = std::max(L.max_owned, d.nowned);
+    L.max_halo = std::max(L.max_halo, d.nhalo);
+    L.max_local = std::max(L.max_local, d.nowned + d.nhalo);
+    sl += d.nslots;
+    hl += d.nhalo;
+  }
+  L.mean_slots_per_block = sl / nb;
+  L.mean_halo_per_block = hl / nb;
+  L.ninst = 1;
+  L.blk_inst.assign(nb, 0);
+  L.inst_bbeg = {0, nb};
+  L.inst_vbeg = {0, nv};
+  out.total_slots = total_slots;
+  out.nhalo = nhalo_total;
+  out.nnbr = nn;
+  return "";
+}
+
+}  // namespace eikgb
