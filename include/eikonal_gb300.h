@@ -59,7 +59,7 @@ typedef struct eik_options {
                               updates in FP64 from FP64 metric edge products; every other tet
                               stays FP32.  An FP64 residual check runs after the solve. */
   float precision_kappa;   /* flagging threshold on ||G||_F ||G^-1||_F (1e4) */
-  int device_setup;        /* 1: a 3D solve builds its block layout (renumbering, element slots,
+  int device_setup;        /* 1 (default): a 3D solve builds its block layout (renumbering, element slots,
                               halo lists, metric edge products, neighbour graph) on the GPU;
                               0: on the host.  Same layout, same results; precision mode,
                               batches and the server use the host build. */

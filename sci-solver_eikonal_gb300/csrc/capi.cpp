@@ -18,7 +18,7 @@
 using namespace eikgb;
 
 // 3D solves build their block layout on the GPU unless eik_options.device_setup = 0
-#define DEVICE_SETUP_DEFAULT 0
+#define DEVICE_SETUP_DEFAULT 1
 
 struct eik_solver {
   int dim = 3;
