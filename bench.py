@@ -47,7 +47,7 @@ MAX_ITERS = 100  # the reference default (src/Eikonal.cu:19); the workload conve
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-sample-iters", type=int, default=0, help="0 = choose automatically")
@@ -138,11 +138,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample(xyz, tets, metric, seed, labels, nb, sample_iters):
-    """The oracle on the first `sample_iters` outer iterations of the same solve."""
+def cpu_sample(xyz, tets, metric, seed, labels, nb, sample_iters, nthreads=0):
+    """The oracle on the first `sample_iters` outer iterations of the same solve
+    (nthreads 0: every host thread)."""
     from oracle import oracle as O  # CPU baseline only
     M = O.metrics_from_speeds(tets.shape[0], metric)
-    threads = O.num_threads()
+    threads = nthreads or O.num_threads()
     t0 = time.perf_counter()
     r = O.solve3d(xyz, tets, M, labels, nb, [seed], max_iters=sample_iters, nthreads=threads)
     dt = time.perf_counter() - t0
@@ -657,6 +658,10 @@ def main():
         res["cpu_baseline"] = {k: v for k, v in cpu_sample(xyz, tets, metric, seed, labels, nb,
                                                            args.cpu_sample_iters or MAX_ITERS).items()
                                if k in ("value", "unit", "cores", "kind", "sample")}
+        # one host thread, on the first 20 iterations (a bounded sample)
+        res["cpu_baseline_1thread"] = {k: v for k, v in cpu_sample(xyz, tets, metric, seed, labels, nb, 20,
+                                                                   nthreads=1).items()
+                                       if k in ("value", "unit", "cores", "kind", "sample")}
     if world == 1 and not args.no_patterns:
         res.update(pattern_summaries(args, E, torch, local))
     print(json.dumps(res), flush=True)
