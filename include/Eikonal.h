@@ -15,6 +15,10 @@
 //   * maxBlocks_ is overwritten with the block count the partition produced.
 // Different from the reference:
 //   * errors throw std::runtime_error where the reference prints and calls exit();
+//     compiled with EIKONAL_GB300_EXIT_ON_ERROR defined, the class prints the
+//     message and exits with the reference's codes instead (1: unreadable mesh,
+//     0: initial values of the wrong size, -1: any other failure), so programs and
+//     tests that expect the process to end keep working;
 //   * the reference's internal pointers (triMesh_, tetMesh_, FIMPtr2d_, FIMPtr3d_)
 //     have no counterpart; setMesh() takes vertex / element arrays instead;
 //   * keepHistory_ (default true) can be cleared to skip the per-iteration
@@ -25,6 +29,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -73,8 +78,9 @@ class Eikonal {
   }
   // Vertices set to 0 become seeds (src/Eikonal.cu:69-97); the mesh must be loaded.
   void initializeVertices(std::vector<float> values) {
-    if (!meshLoaded_) throw std::runtime_error("You must initialize the mesh first!");
-    check(eik_set_initial_values(h_, values.data(), (int)values.size()));
+    if (!meshLoaded_) fatal(0, "You must initialize the mesh first!");
+    if (eik_set_initial_values(h_, values.data(), (int)values.size()) != EIK_OK)
+      fatal(0, std::string("eikonal: ") + eik_last_error(h_));
     userSetInitial_ = true;
   }
   // Per-face speeds (2D), or per-tet scalar / 6-entry metric (3D) (src/Eikonal.cu:62-67).
@@ -178,8 +184,20 @@ class Eikonal {
   int deviceSetup_;
 
  private:
+  // the reference's exit codes for the failures it exits on (src/Eikonal.cu:71-88,
+  // :103-118; cutil.h for CUDA errors)
+  static int exit_code(int rc) { return (rc == EIK_ERR_MESH) ? 1 : -1; }
+  [[noreturn]] static void fatal(int code, const std::string& msg) {
+#ifdef EIKONAL_GB300_EXIT_ON_ERROR
+    std::fprintf(stderr, "%s\n", msg.c_str());
+    std::exit(code);
+#else
+    (void)code;
+    throw std::runtime_error(msg);
+#endif
+  }
   void check(int rc) const {
-    if (rc != EIK_OK) throw std::runtime_error(std::string("eikonal: ") + eik_last_error(h_));
+    if (rc != EIK_OK) fatal(exit_code(rc), std::string("eikonal: ") + eik_last_error(h_));
   }
   void push_options() {
     eik_options o;

@@ -57,3 +57,26 @@ def test_cpp_reference_tests_pass(need_gpu, tmp_path):
     _write_fixtures(str(tmp_path))
     r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_cpp_exit_codes_like_the_reference(tmp_path):
+    """With EIKONAL_GB300_EXIT_ON_ERROR the class ends the process with the
+    reference's codes (src/test/3d/3D-sanity.cc expects status 1 for a missing
+    mesh file); the mesh read fails before any GPU work, so this runs anywhere."""
+    src = tmp_path / "exit_test.cc"
+    src.write_text('#include "Eikonal.h"\n'
+                   'int main(int argc, char** argv) {\n'
+                   '  Eikonal data(argv[1][0] == \'2\');\n'
+                   '  data.filename_ = "notarealfile";\n'
+                   '  data.solveEikonal();\n'
+                   '  return 7;\n'
+                   '}\n')
+    exe = str(tmp_path / "exit_test")
+    cmd = ["g++", "-std=c++17", "-DEIKONAL_GB300_EXIT_ON_ERROR", "-I", os.path.join(ROOT, "include"), str(src),
+           "-o", exe, "-L", LIB_DIR, "-leikonal_gb300", "-Wl,-rpath," + LIB_DIR]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for dim in ("2", "3"):
+        r = subprocess.run([exe, dim], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 1, (dim, r.returncode, r.stderr)
+        assert "notarealfile" in r.stderr
