@@ -30,6 +30,7 @@ extern "C" {
 #define EIK_ERR_LIMIT 5  /* a block does not fit in shared memory; use smaller blocks */
 #define EIK_ERR_DEVICE 6 /* a device-side bounded wait expired */
 #define EIK_ERR_IO 7     /* file output failed */
+#define EIK_ERR_CANCELLED 8 /* a server request cancelled before it completed */
 
 #define EIK_SPEED_ONE 1 /* the reference's speedType_ ONE (src/core2d/include/TriMesh.h:15-16) */
 
@@ -175,6 +176,14 @@ int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned 
  *              3 outputs per case. */
 int eik_selftest_local_update(int which, const float* in, float* out, int n);
 
+/* Failure-path self-test (no counterpart in the reference, which has no bounded
+ * waits): launches a kernel whose barrier waits for a copy that never comes.  The
+ * wait gives up after about one second and reports it, as the solver kernels do
+ * when a bulk copy does not land; the GPU context stays usable.  Returns
+ * EIK_ERR_DEVICE when the wait gave up (the expected outcome), EIK_OK if it did not;
+ * waited_ms (may be null) receives how long it waited. */
+int eik_selftest_wait_timeout(double* waited_ms);
+
 /* Allocation-free 3D solve.  No counterpart in the reference: an addition for
  * callers that cannot call cudaMalloc, such as code running while another
  * component captures the stream into a CUDA graph, real-time or embedded hosts
@@ -250,7 +259,8 @@ const char* eik_batch_last_error(const eik_batch* b);
  * resident copy of one mesh's block layout and solver state (device_bytes per
  * slot, reported by eik_server_mesh_info).  A mesh added with slots = 0 gets
  * floor(share / device_bytes) slots (at least 1, at most 64), share being the
- * HBM budget divided evenly among such meshes.  A request is admitted when a
+ * HBM budget divided evenly among such meshes; eik_server_start fails with
+ * EIK_ERR_LIMIT when the slots need more bytes than a nonzero budget allows.  A request is admitted when a
  * slot of its mesh is free (and, with max_inflight > 0, fewer than max_inflight
  * requests run); it waits in arrival order otherwise.
  *
@@ -287,6 +297,10 @@ int eik_server_submit(eik_server* s, int mesh_id, const int* seeds, int nseeds, 
 int eik_server_poll(eik_server* s, eik_completion* out, int max, int wait_ms, int* n);
 /* Travel times of a completed request (keep_results = 1); releases them. */
 int eik_server_result(eik_server* s, long long id, float* out, int nv);
+/* Cancels a queued or running request: it completes with status
+ * EIK_ERR_CANCELLED (a running one at the end of its current outer iteration) and
+ * frees its slot.  EIK_ERR_ARG if the id is unknown or already completed. */
+int eik_server_cancel(eik_server* s, long long id);
 /* Waits until nothing is queued or running (timeout_ms < 0: no limit). */
 int eik_server_drain(eik_server* s, int timeout_ms);
 int eik_server_get_stats(eik_server* s, eik_server_stats* out);

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libeikonal_gb300.so")
 
 EIK_OK = 0
 ERRORS = {1: "EIK_ERR_ARG", 2: "EIK_ERR_STATE", 3: "EIK_ERR_MESH", 4: "EIK_ERR_CUDA",
-          5: "EIK_ERR_LIMIT", 6: "EIK_ERR_DEVICE", 7: "EIK_ERR_IO"}
+          5: "EIK_ERR_LIMIT", 6: "EIK_ERR_DEVICE", 7: "EIK_ERR_IO", 8: "EIK_ERR_CANCELLED"}
 ONE = 1  # speed type ONE
 
 
@@ -104,6 +104,7 @@ SIGNATURES = {
     "eik_tri_prep": (ctypes.c_int, [_P, _IP, _IP, _IP, _UP, _IP, _IP]),
     "eik_selftest_local_update": (ctypes.c_int, [ctypes.c_int, _FP, _FP, ctypes.c_int]),
     "eik_stream": (_P, [_P]),
+    "eik_selftest_wait_timeout": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "eik_solve3d_noalloc": (ctypes.c_int, [_FP, ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_longlong, _IP,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _FP, _P, _IP, ctypes.c_char_p,
                                            ctypes.c_int]),
@@ -130,6 +131,7 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_int)]),
     "eik_server_result": (ctypes.c_int, [_P, ctypes.c_longlong, _FP, ctypes.c_int]),
     "eik_server_drain": (ctypes.c_int, [_P, ctypes.c_int]),
+    "eik_server_cancel": (ctypes.c_int, [_P, ctypes.c_longlong]),
     "eik_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(EikServerStats)]),
     "eik_server_destroy": (None, [_P]),
     "eik_server_last_error": (ctypes.c_char_p, [_P]),
@@ -502,6 +504,9 @@ class EikonalServer:
         self._check(self._lib.eik_server_result(self._h, int(request_id), _fptr(out), out.size))
         return out
 
+    def cancel(self, request_id):
+        self._check(self._lib.eik_server_cancel(self._h, int(request_id)))
+
     def drain(self, timeout_ms=-1):
         self._check(self._lib.eik_server_drain(self._h, int(timeout_ms)))
 
@@ -523,6 +528,14 @@ def selftest_local_update(which, inputs):
     if rc:
         raise EikonalError(rc, "self-test kernel failed")
     return out if nout > 1 else out[:, 0]
+
+
+def selftest_wait_timeout():
+    """Runs the bounded-wait failure self-test: returns (status code, waited ms);
+    EIK_ERR_DEVICE (6) means the wait gave up as designed."""
+    ms = ctypes.c_double()
+    rc = lib().eik_selftest_wait_timeout(ctypes.byref(ms))
+    return rc, ms.value
 
 
 def solve3d_noalloc(xyz, tets, speeds=None, seeds=(0,), max_verts_per_block=64, max_iterations=100, stream=0):

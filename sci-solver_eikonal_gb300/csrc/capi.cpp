@@ -3,6 +3,7 @@
 // (src/Eikonal.cu:4-279): same defaults, same seed rules, same partition-size
 // rules, status codes where the reference exits.
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -52,6 +53,7 @@ struct eik_solver {
   // 3D layout built on the device: its host part, and what it was built from
   Layout dlayout;
   unsigned dlay_mesh = ~0u, dlay_speed = ~0u;
+  unsigned checked_speed = ~0u, checked_mesh = ~0u;  // speeds validated for these versions
   std::string dlay_key;
   std::unique_ptr<DeviceSolve> dev;
   bool uploaded = false;
@@ -101,10 +103,41 @@ std::vector<float> speed_inverse(const eik_solver* h) {
   return inv;
 }
 
+// Speeds / metrics the scheme can use: 2D speeds and 3D scalar metrics finite and
+// positive, 3D 6-entry metrics symmetric positive definite (leading minors > 0).
+// The reference accepts anything and returns NaN or garbage times instead.
+int check_speeds(eik_solver* h) {
+  if (h->checked_speed == h->speed_ver && h->checked_mesh == h->mesh_ver) return EIK_OK;
+  if (h->speeds_set) {
+    const size_t n = h->speeds.size();
+    if (n == (size_t)h->ne) {
+      for (size_t i = 0; i < n; ++i)
+        if (!(std::isfinite(h->speeds[i]) && h->speeds[i] > 0.0f))
+          return fail(h, EIK_ERR_ARG, (h->dim == 2 ? "speed of face " : "metric of tet ") + std::to_string(i) +
+                                          " is not a positive finite number");
+    } else if (h->dim == 3 && n == 6 * (size_t)h->ne) {
+      for (int t = 0; t < h->ne; ++t) {
+        const float* m = &h->speeds[6 * (size_t)t];
+        bool finite = true;
+        for (int k = 0; k < 6; ++k) finite = finite && std::isfinite(m[k]);
+        const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5];
+        const double m2 = a * d - b * b;
+        const double det = a * (d * f - e * e) - b * (b * f - e * c) + c * (b * e - d * c);
+        if (!finite || !(a > 0) || !(m2 > 0) || !(det > 0))
+          return fail(h, EIK_ERR_ARG, "metric of tet " + std::to_string(t) + " is not symmetric positive definite");
+      }
+    }
+  }
+  h->checked_speed = h->speed_ver;
+  h->checked_mesh = h->mesh_ver;
+  return EIK_OK;
+}
+
 // Partition + block layout on the host, cached while the mesh, the partition
 // inputs and the speeds are unchanged; refreshes only the metric terms when just
 // the speeds changed.
 int host_prepare(eik_solver* h, bool* new_layout_out) {
+  if (int rc = check_speeds(h)) return rc;
   bool new_layout = false;
   const std::string key = partition_key(h);
   if (h->lay_mesh != h->mesh_ver || h->lay_key != key) {
@@ -228,6 +261,7 @@ void fill_stats(eik_stats& s, const SolveStats& st, const Layout& L, float setup
 // and partition inputs are unchanged; a speed change recomputes the metric terms
 // on the device.  The partition itself stays on the host (make_partition).
 int device_prepare(eik_solver* h) {
+  if (int rc = check_speeds(h)) return rc;
   const std::string key = partition_key(h);
   if (!h->dev) h->dev.reset(new DeviceSolve);
   if (h->dlay_mesh != h->mesh_ver || h->dlay_key != key || !h->dev->layout_built_on_device()) {
@@ -537,6 +571,14 @@ int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned 
   if (vf_off) std::memcpy(vf_off, P.vf_off.data(), sizeof(int) * P.vf_off.size());
   if (vf_verts && !P.vf_verts.empty()) std::memcpy(vf_verts, P.vf_verts.data(), sizeof(int) * P.vf_verts.size());
   return EIK_OK;
+}
+
+int eik_selftest_wait_timeout(double* waited_ms) {
+  int status = 0;
+  double ms = 0;
+  if (!selftest_wait_timeout(&status, &ms).empty()) return EIK_ERR_CUDA;
+  if (waited_ms) *waited_ms = ms;
+  return status ? EIK_ERR_DEVICE : EIK_OK;
 }
 
 int eik_selftest_local_update(int which, const float* in, float* out, int n) {

@@ -146,6 +146,8 @@ class DeviceSolve {
                           int threads);
   std::string serve_admit(const std::vector<Admission>& adm);
   std::string serve_run();
+  // stop running instances now (their list entries are skipped, then dropped)
+  std::string serve_cancel(const std::vector<int>& insts);
   std::string serve_poll(std::vector<int>& done, std::vector<int>& iters);
   std::string serve_fetch(int inst);
   std::string serve_sync();
@@ -171,6 +173,10 @@ class DeviceSolve {
 // root_quot); 3 / 4: single-triangle blocks through the 2D sweep / check kernel
 // (7 inputs -> 3 outputs).  Host arrays.
 std::string selftest_device(int which, const float* in, float* out, int n);
+
+// Runs a one-CTA kernel whose bounded barrier wait cannot complete: status gets
+// the device error flag (nonzero when the wait gave up), waited_ms its duration.
+std::string selftest_wait_timeout(int* status, double* waited_ms);
 
 // Allocation-free 3D solve: the layout and every solver buffer live in a fixed
 // 32 MiB array of the library's device image (no cudaMalloc / cudaFree).  Runs on

@@ -28,6 +28,7 @@
 //     in the previous sweep; unchanged inputs reproduce the previous candidates
 //     bit for bit, so skipping them cannot change any result.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -147,10 +148,24 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
   return ok != 0;
 }
 // Bounded wait (a few seconds at most); false means the copy never completed.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: gives up after about one second of device time (global timer;
+// an iteration cap backs it up), so a copy that never lands becomes an error
+// flag the host reads instead of a kernel that never ends.
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-  for (int i = 0; i < (1 << 24); ++i) {
+  const unsigned long long t0 = global_ns();
+  for (int i = 0; i < (1 << 26); ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (i > 16) __nanosleep(256);
+    if (i > 16) {
+      __nanosleep(256);
+      if ((i & 63) == 0 && global_ns() - t0 > kWaitLimitNs) return false;
+    }
   }
   return false;
 }
@@ -158,11 +173,6 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
 // launch span of a visit kernel: earliest CTA start, latest CTA end
 __device__ __forceinline__ void stamp_start(const DevArgs& a, int iter, int which) {
   if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap) atomicMin(&a.ktime[4 * iter + 2 * which], global_ns());
@@ -1020,6 +1030,11 @@ __global__ void k_compact_active(DevArgs a) {
   if (threadIdx.x == 0) c->nact = m;
 }
 
+// Cancelled instances stop: marked finished, so visits skip their blocks.
+__global__ void k_cancel(DevArgs a, const int* insts, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a.inst_done[insts[i]] = 1;
+}
+
 // Fresh state for one instance: vertices [v0, v0+nv), blocks [b0, b0+nb).
 __global__ void k_admit_state(DevArgs a, int v0, int nv, int b0, int nb, float large) {
   const int stride = gridDim.x * blockDim.x;
@@ -1125,6 +1140,21 @@ __global__ void k_admit_seeds(DevArgs a, int inst, const int* seed_ids, int nsee
 }
 
 // element-wise evaluation of the device local updates (self-test entry points)
+// Failure-path self-test: a barrier that expects 16 bytes no copy ever brings;
+// the bounded wait must give up and report it.
+__global__ void k_selftest_wait(int* status, unsigned long long* waited_ns) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&bar, 16);
+    const unsigned long long t0 = global_ns();
+    const bool ok = mbar_wait(&bar, 0);
+    *waited_ns = global_ns() - t0;
+    *status = ok ? 0 : kErrWait;
+  }
+}
+
 __global__ void k_selftest_tet(const float* in, float* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -1166,6 +1196,12 @@ std::string dev_alloc(T*& p, size_t n) {
 // ===========================================================================
 // host side
 // ===========================================================================
+// NVTX range for profilers (a no-op unless a tool injects itself)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
 struct DeviceSolve::Impl {
   int dim = 3, nv = 0, nb = 0;
   BlockDesc* blocks = nullptr;
@@ -1425,6 +1461,7 @@ DeviceSolve::~DeviceSolve() {
 }
 
 std::string DeviceSolve::upload(const Layout& L) {
+  NvtxRange nvtx("eikonal: upload layout");
   Impl& P = *p_;
   if (!stream_) return "CUDA stream creation failed (no usable GPU?)";
   P.free_all();
@@ -1458,6 +1495,7 @@ std::string DeviceSolve::upload(const Layout& L) {
 }
 
 std::string DeviceSolve::upload_built(const Layout& L, Built3D& b) {
+  NvtxRange nvtx("eikonal: adopt device-built layout");
   Impl& P = *p_;
   if (!stream_) return "CUDA stream creation failed (no usable GPU?)";
   P.free_all();
@@ -1617,6 +1655,7 @@ std::string DeviceSolve::set_seeds_multi(const std::vector<std::vector<int>>& se
 }
 
 std::string DeviceSolve::solve(const SolveOptions& opt) {
+  NvtxRange nvtx("eikonal: solve");
   Impl& P = *p_;
   if (!L_) return "no layout uploaded";
   const Layout& L = *L_;
@@ -1979,6 +2018,7 @@ std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, con
 }
 
 std::string DeviceSolve::serve_admit(const std::vector<Admission>& adm) {
+  NvtxRange nvtx("eikonal: admit requests");
   Impl& P = *p_;
   if (!L_ || P.g_serve != 1) return "serving not set up";
   const Layout& L = *L_;
@@ -2037,7 +2077,26 @@ std::string DeviceSolve::serve_admit(const std::vector<Admission>& adm) {
   return "";
 }
 
+std::string DeviceSolve::serve_cancel(const std::vector<int>& insts) {
+  Impl& P = *p_;
+  if (!L_ || P.g_serve != 1) return "serving not set up";
+  if (insts.empty()) return "";
+  cudaStream_t st = (cudaStream_t)stream_;
+  if (insts.size() > P.seed_cap) {
+    if (P.seed_ids) cudaFree(P.seed_ids);
+    P.seed_ids = nullptr;
+    P.seed_cap = std::max<size_t>(insts.size(), 1024);
+    CK(cudaMalloc((void**)&P.seed_ids, sizeof(int) * P.seed_cap));
+  }
+  CK(cudaMemcpyAsync(P.seed_ids, insts.data(), sizeof(int) * insts.size(), cudaMemcpyHostToDevice, st));
+  k_cancel<<<1, 256, 0, st>>>(P.args, P.seed_ids, (int)insts.size());
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  return "";
+}
+
 std::string DeviceSolve::serve_run() {
+  NvtxRange nvtx("eikonal: serving loop");
   Impl& P = *p_;
   if (!L_ || P.g_serve != 1) return "serving not set up";
   cudaStream_t st = (cudaStream_t)stream_;
@@ -2090,6 +2149,23 @@ const float* DeviceSolve::serve_host_result(int inst) const {
 volatile int* DeviceSolve::serve_pending() const { return (volatile int*)p_->pending_host; }
 
 void DeviceSolve::bind_thread() const { cudaSetDevice(p_->device); }
+
+std::string selftest_wait_timeout(int* status, double* waited_ms) {
+  int* d_status = nullptr;
+  unsigned long long* d_ns = nullptr;
+  CK(cudaMalloc((void**)&d_status, sizeof(int)));
+  CK(cudaMalloc((void**)&d_ns, sizeof(unsigned long long)));
+  k_selftest_wait<<<1, 32>>>(d_status, d_ns);
+  cudaError_t e = cudaDeviceSynchronize();
+  unsigned long long ns = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(status, d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&ns, d_ns, sizeof(ns), cudaMemcpyDeviceToHost);
+  cudaFree(d_status);
+  cudaFree(d_ns);
+  if (e != cudaSuccess) return std::string("wait self-test: ") + cudaGetErrorString(e);
+  *waited_ms = (double)ns * 1e-6;
+  return "";
+}
 
 std::string selftest_device(int which, const float* in, float* out, int n) {
   if (which == 3 || which == 4) return selftest_tri_blocks(in, n, which == 4, out);

@@ -18,6 +18,7 @@
 #include <string>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/eikonal_gb300.h"
@@ -45,6 +46,7 @@ struct Request {
   float scale = 1.0f;
   double t_submit = 0, t_admit = 0;
   int inst = -1;
+  bool cancelled = false;
 };
 
 struct Arena {
@@ -85,6 +87,7 @@ struct eik_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request> queue;
+  std::unordered_set<long long> cancel_running;  // running requests to stop
   long long next_id = 1;
   int inflight = 0;
   bool stop = false;
@@ -159,10 +162,17 @@ void worker_loop(eik_server* S, int ai) {
   std::vector<int> done, iters;
   for (;;) {
     std::vector<Admission> adm;
+    std::vector<int> cancel;
     {
       std::unique_lock<std::mutex> lk(S->mu);
       S->cv_work.wait(lk, [&] { return S->stop || !A.running.empty() || has_admissible(S, ai); });
       if (S->stop) return;
+      for (auto& kv : A.running)
+        if (!kv.second.cancelled && S->cancel_running.count(kv.first)) {
+          kv.second.cancelled = true;
+          S->cancel_running.erase(kv.first);
+          cancel.push_back(kv.second.inst);
+        }
       for (auto it = S->queue.begin(); it != S->queue.end();) {
         if (S->meshes[it->mesh].arena != ai || !admissible(S, *it)) {
           ++it;
@@ -188,7 +198,8 @@ void worker_loop(eik_server* S, int ai) {
     }
     std::string e;
     const auto r0 = std::chrono::steady_clock::now();
-    if (!adm.empty()) e = A.dev->serve_admit(adm);
+    if (!cancel.empty()) e = A.dev->serve_cancel(cancel);
+    if (e.empty() && !adm.empty()) e = A.dev->serve_admit(adm);
     if (e.empty()) e = A.dev->serve_run();
     const double run_s = seconds_since(r0);
     if (e.empty()) e = A.dev->serve_poll(done, iters);
@@ -222,15 +233,16 @@ void worker_loop(eik_server* S, int ai) {
       c.id = r.id;
       c.mesh = r.mesh;
       c.iterations = iters[i];
-      c.status = EIK_OK;
+      c.status = r.cancelled ? EIK_ERR_CANCELLED : EIK_OK;
       c.submit_s = r.t_submit;
       c.admit_s = r.t_admit;
       c.done_s = t;
-      if (S->keep) {
+      if (S->keep && !r.cancelled) {
         const float* p = A.dev->serve_host_result(i);
         S->results[r.id].assign(p, p + S->meshes[r.mesh].snap.nv);
       }
       S->done.push_back(c);
+      S->cancel_running.erase(r.id);
       A.free_slots[r.mesh].push_back(i);
       A.inst_req[i] = -1;
       A.running.erase(it);
@@ -301,10 +313,15 @@ int eik_server_start(eik_server* s) {
     else fixed += (long long)m.slots_req * (long long)m.bytes;
   }
   const long long share = nauto ? std::max(0ll, (s->budget - fixed) / nauto) : 0;
+  long long need = 0;
   for (PoolMesh& m : s->meshes) {
     if (m.slots_req > 0) m.slots = m.slots_req;
     else m.slots = (int)std::min<long long>(64, std::max<long long>(1, share / (long long)std::max<size_t>(m.bytes, 1)));
+    need += (long long)m.slots * (long long)m.bytes;
   }
+  if (s->budget > 0 && need > s->budget)
+    return sfail(s, EIK_ERR_LIMIT, "the pool's slots need " + std::to_string(need) + " device bytes, over the budget of " +
+                                       std::to_string(s->budget));
   for (int ai = 0; ai < 2; ++ai) {
     Arena& A = s->arenas[ai];
     A.dim = ai == 0 ? 2 : 3;
@@ -408,6 +425,33 @@ int eik_server_result(eik_server* s, long long id, float* out, int nv) {
   std::memcpy(out, it->second.data(), sizeof(float) * (size_t)nv);
   s->results.erase(it);
   return EIK_OK;
+}
+
+int eik_server_cancel(eik_server* s, long long id) {
+  if (!s) return EIK_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+    if (it->id != id) continue;
+    eik_completion c{};
+    c.id = it->id;
+    c.mesh = it->mesh;
+    c.status = EIK_ERR_CANCELLED;
+    c.submit_s = it->t_submit;
+    c.done_s = seconds_since(s->t0);
+    s->done.push_back(c);
+    s->completed++;
+    s->queue.erase(it);
+    s->cv_done.notify_all();
+    return EIK_OK;
+  }
+  for (Arena& A : s->arenas)
+    if (A.running.count(id)) {
+      s->cancel_running.insert(id);
+      if (A.pending) *A.pending = 1;  // end the device loop after this iteration
+      s->cv_work.notify_all();
+      return EIK_OK;
+    }
+  return sfail(s, EIK_ERR_ARG, "no queued or running request with this id");
 }
 
 int eik_server_drain(eik_server* s, int timeout_ms) {

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <cub/cub.cuh>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstdint>
@@ -319,6 +320,10 @@ void Built3D::release() {
 
 std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M6,
                                   const int* labels, int nb, cudaStream_t st, Built3D& out, Layout& L) {
+  struct Range {
+    Range() { nvtxRangePushA("eikonal: device setup"); }
+    ~Range() { nvtxRangePop(); }
+  } nvtx_range;
   out.release();
   L = Layout();
   if (nv <= 0 || nt <= 0 || nb <= 0) return "empty mesh";

@@ -200,3 +200,46 @@ def test_server_host_side_and_no_gpu_failure(eik, mg):
         with pytest.raises(eik.EikonalError):
             srv.start()  # no device: fails loudly, no CPU fallback
     srv.close()
+
+
+def test_invalid_speeds_and_metrics_are_rejected(eik, mg):
+    """Host-side fault injection: values the scheme cannot use fail with
+    EIK_ERR_ARG before any setup or GPU work."""
+    xyz, tets = mg.kuhn_cube(5, 0.2, seed=1)
+    nt = tets.shape[0]
+    bad = [np.full(nt, -1.0, np.float32), np.full(nt, np.nan, np.float32), np.zeros(nt, np.float32)]
+    m6 = np.tile(np.array([1, 0, 0, 1, 0, 1], np.float32), nt)
+    m6_bad = m6.copy()
+    m6_bad[6 * 3 + 1] = 2.0  # M01 = 2 with M00 = M11 = 1: indefinite
+    bad.append(m6_bad)
+    for vals in bad:
+        e = eik.Eikonal(False)
+        e.set_mesh(xyz, tets)
+        e.initSpeedMtxMultipliers(vals)
+        with pytest.raises(eik.EikonalError) as ei:
+            e.prepare()
+        assert ei.value.code == 1
+    ok = eik.Eikonal(False)
+    ok.set_mesh(xyz, tets)
+    ok.initSpeedMtxMultipliers(m6)
+    ok.prepare()
+    fx, faces = mg.grid2d(5)
+    t = eik.Eikonal(True)
+    t.set_mesh(fx, faces)
+    sp = np.ones(faces.shape[0], np.float32)
+    sp[2] = np.inf
+    t.initSpeedMtxMultipliers(sp)
+    with pytest.raises(eik.EikonalError):
+        t.prepare()
+
+
+def test_server_rejects_pool_over_budget(eik, mg):
+    xyz, faces = mg.icosphere(3)
+    a = eik.Eikonal(True)
+    a.set_mesh(xyz, faces)
+    srv = eik.EikonalServer(hbm_budget_bytes=1000)
+    srv.add_mesh(a)
+    with pytest.raises(eik.EikonalError) as ei:
+        srv.start()  # fails on the budget before touching a GPU
+    assert ei.value.code == 5 and "budget" in str(ei.value)
+    srv.close()
