@@ -104,8 +104,9 @@ std::vector<float> speed_inverse(const eik_solver* h) {
 }
 
 // Speeds / metrics the scheme can use: 2D speeds and 3D scalar metrics finite and
-// positive, 3D 6-entry metrics symmetric positive definite (leading minors > 0).
-// The reference accepts anything and returns NaN or garbage times instead.
+// positive, 3D 6-entry metrics finite.  6-entry metrics are not required to be
+// positive definite: the reference's own anisotropic fixture (torus_matrices.txt)
+// holds indefinite matrices for half of its tets and the reference solves it.
 int check_speeds(eik_solver* h) {
   if (h->checked_speed == h->speed_ver && h->checked_mesh == h->mesh_ver) return EIK_OK;
   if (h->speeds_set) {
@@ -120,11 +121,7 @@ int check_speeds(eik_solver* h) {
         const float* m = &h->speeds[6 * (size_t)t];
         bool finite = true;
         for (int k = 0; k < 6; ++k) finite = finite && std::isfinite(m[k]);
-        const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5];
-        const double m2 = a * d - b * b;
-        const double det = a * (d * f - e * e) - b * (b * f - e * c) + c * (b * e - d * c);
-        if (!finite || !(a > 0) || !(m2 > 0) || !(det > 0))
-          return fail(h, EIK_ERR_ARG, "metric of tet " + std::to_string(t) + " is not symmetric positive definite");
+        if (!finite) return fail(h, EIK_ERR_ARG, "metric of tet " + std::to_string(t) + " is not finite");
       }
     }
   }

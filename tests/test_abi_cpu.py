@@ -210,8 +210,11 @@ def test_invalid_speeds_and_metrics_are_rejected(eik, mg):
     bad = [np.full(nt, -1.0, np.float32), np.full(nt, np.nan, np.float32), np.zeros(nt, np.float32)]
     m6 = np.tile(np.array([1, 0, 0, 1, 0, 1], np.float32), nt)
     m6_bad = m6.copy()
-    m6_bad[6 * 3 + 1] = 2.0  # M01 = 2 with M00 = M11 = 1: indefinite
+    m6_bad[6 * 3 + 1] = np.nan
     bad.append(m6_bad)
+    # an indefinite 6-entry metric is accepted, as the reference's torus fixture needs
+    m6_indef = m6.copy()
+    m6_indef[6 * 3 + 1] = 2.0
     for vals in bad:
         e = eik.Eikonal(False)
         e.set_mesh(xyz, tets)
@@ -219,10 +222,11 @@ def test_invalid_speeds_and_metrics_are_rejected(eik, mg):
         with pytest.raises(eik.EikonalError) as ei:
             e.prepare()
         assert ei.value.code == 1
-    ok = eik.Eikonal(False)
-    ok.set_mesh(xyz, tets)
-    ok.initSpeedMtxMultipliers(m6)
-    ok.prepare()
+    for vals in (m6, m6_indef):
+        ok = eik.Eikonal(False)
+        ok.set_mesh(xyz, tets)
+        ok.initSpeedMtxMultipliers(vals)
+        ok.prepare()
     fx, faces = mg.grid2d(5)
     t = eik.Eikonal(True)
     t.set_mesh(fx, faces)
