@@ -1,0 +1,99 @@
+"""Edge cases of the solve: the smallest meshes, every vertex a seed, repeated
+seeds, no iterations, a mesh in two pieces, a single block.  Where a value is
+known it is checked; elsewhere the CPU restatement of the reference scheme (same
+partition) is the check, within the tolerances of the parity tests."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def _tet(eik, xyz, tets, seeds, **opts):
+    e = eik.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.setSeeds(list(seeds))
+    for k, v in opts.items():
+        setattr(e, k, v)
+    e.solveEikonal()
+    return e
+
+
+def test_single_tet(need_gpu, eik, O):
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    tets = np.array([[0, 1, 2, 3]], np.int32)
+    e = _tet(eik, xyz, tets, [0])
+    r = e.getFinalResult()
+    assert r[0] == 0.0
+    assert np.allclose(r[1:], 1.0, rtol=1e-6)  # unit speed, unit edges from the seed
+    lab, nb = e.getPartition()
+    want = O.solve3d(xyz, tets, O.metrics_from_speeds(1, None), lab, nb, [0])["result"]
+    assert np.max(relerr(r, want)) <= 1e-6
+
+
+def test_every_vertex_a_seed_and_repeated_seeds(need_gpu, eik, mg):
+    xyz, tets = mg.kuhn_cube(7, 0.2, seed=2)
+    e = _tet(eik, xyz, tets, range(xyz.shape[0]))
+    assert np.all(e.getFinalResult() == 0.0)
+    a = _tet(eik, xyz, tets, [10, 10, 10, 200])
+    b = _tet(eik, xyz, tets, [200, 10])
+    assert bits_equal(a.getFinalResult(), b.getFinalResult())
+    assert a.numIterations() == b.numIterations()
+
+
+def test_zero_iterations_leaves_seeds(need_gpu, eik, mg):
+    xyz, tets = mg.kuhn_cube(7, 0.2, seed=2)
+    e = _tet(eik, xyz, tets, [5], maxIterations_=0, keepHistory_=0)
+    r = e.getFinalResult()
+    assert e.stats()["iterations"] == 0
+    # no block was visited: the reference's result buffer holds 0 for every vertex
+    assert np.all(r == 0.0)
+
+
+def test_two_pieces_unreached_piece(need_gpu, eik, mg, O):
+    """A mesh in two disconnected cubes, seeded in one: the reached cube matches
+    the oracle; the other is never visited and reads 0, as in the reference
+    (vertices of unvisited blocks come from its zeroed buffer)."""
+    x1, t1 = mg.kuhn_cube(6, 0.2, seed=3)
+    x2 = x1 + np.float32(5.0)
+    xyz = np.concatenate([x1, x2]).astype(np.float32)
+    tets = np.concatenate([t1, t1 + x1.shape[0]]).astype(np.int32)
+    e = _tet(eik, xyz, tets, [0], maxVertsPerBlock_=32)
+    r = e.getFinalResult()
+    lab, nb = e.getPartition()
+    want = O.solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], None), lab, nb, [0])["result"]
+    n1 = x1.shape[0]
+    assert np.max(relerr(r[:n1], want[:n1])) <= 1e-4
+    assert np.all(r[n1:] == 0.0) and np.all(want[n1:] == 0.0)
+
+
+def test_one_block_holds_the_whole_mesh(need_gpu, eik, mg, O):
+    xyz, tets = mg.kuhn_cube(5, 0.2, seed=4)
+    lab = np.zeros(xyz.shape[0], np.int32)
+    e = eik.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.setSeeds([62])
+    e.setPartition(lab, 1)
+    e.solveEikonal()
+    assert e.stats()["num_blocks"] == 1
+    want = O.solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], None), lab, 1, [62])["result"]
+    assert np.max(relerr(e.getFinalResult(), want)) <= 1e-4
+
+
+def test_single_triangle_and_2d_all_seeds(need_gpu, eik, mg):
+    xyz = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    faces = np.array([[0, 1, 2]], np.int32)
+    e = eik.Eikonal(True)
+    e.set_mesh(xyz, faces)
+    e.setSeeds([0])
+    e.solveEikonal()
+    r = e.getFinalResult()
+    assert r[0] == 0.0 and np.allclose(r[1:], 1.0, rtol=1e-6)
+    gx, gf = mg.grid2d(5)
+    e = eik.Eikonal(True)
+    e.set_mesh(gx, gf)
+    e.setSeeds(list(range(gx.shape[0])))
+    e.maxVertsPerBlock_ = 8
+    e.solveEikonal()
+    assert np.all(e.getFinalResult() == 0.0)
