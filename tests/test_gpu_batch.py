@@ -104,3 +104,20 @@ def test_batch_resolve_with_new_seeds_and_repeated_handle(need_gpu, eik, mg):
     assert bits_equal(got[0], wa) and bits_equal(got[2], wa)
     assert bits_equal(got[1], wc)
     assert not bits_equal(got[0], r0[0])
+
+
+def test_autotuner_picks_a_measured_shape_and_keeps_results(need_gpu, eik, mg):
+    tune = __import__("importlib").import_module("sci-solver_eikonal_gb300.autotune")
+    rng = np.random.default_rng(21)
+    solvers = [_sphere_solver(eik, mg, lv, rng.choice(10 * 4 ** lv + 2, size=3, replace=False))
+               for lv in (2, 3, 3, 4)]
+    res, batch = tune.tune_batch(solvers, vpb_candidates=(16, 64), reps=1, workers=2)
+    assert res.verts_per_block in (16, 64)
+    assert len(res.table) == 2 and all("solve_ms" in r for r in res.table)
+    best = min(res.table, key=lambda r: r["solve_ms"])
+    assert best["verts_per_block"] == res.verts_per_block
+    batch.solveEikonal()
+    for i, e in enumerate(solvers):  # handles keep the chosen block size
+        assert e.maxVertsPerBlock_ == res.verts_per_block
+        want, it = _alone(e)
+        assert bits_equal(batch.getFinalResult(i), want)
