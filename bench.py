@@ -138,19 +138,29 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample(xyz, tets, metric, seed, labels, nb, sample_iters, nthreads=0):
-    """The oracle on the first `sample_iters` outer iterations of the same solve
-    (nthreads 0: every host thread)."""
+def cpu_sample(xyz, tets, metric, seeds, labels, nb, sample_iters, nthreads=0, precision=32):
+    """CPU baseline leg: the oracle (CPU restatement of the reference scheme) on the
+    first `sample_iters` outer iterations of the same solve (nthreads 0: every host
+    thread).  precision 64 is the FP64 run of the scheme, the error reference."""
     from oracle import oracle as O  # CPU baseline only
     M = O.metrics_from_speeds(tets.shape[0], metric)
     threads = nthreads or O.num_threads()
     t0 = time.perf_counter()
-    r = O.solve3d(xyz, tets, M, labels, nb, [seed], max_iters=sample_iters, nthreads=threads)
+    r = O.solve3d(xyz, tets, M, labels, nb, list(np.atleast_1d(seeds)), max_iters=sample_iters, nthreads=threads,
+                  precision=precision)
     dt = time.perf_counter() - t0
     return {"value": r["vertex_updates"] / dt, "unit": "vertex-updates/s", "cores": threads, "kind": "port",
             "sample": f"first {r['iterations']} outer iterations of the same solve "
-                      f"({r['vertex_updates']} vertex updates in {dt:.1f} s)",
-            "seconds": dt, "iterations": r["iterations"]}
+                      f"({r['vertex_updates']} vertex updates in {dt:.1f} s, FP{precision})",
+            "seconds": dt, "iterations": r["iterations"], "result": r["result"]}
+
+
+def error_stats(got, ref):
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-6)
+    return {"max": float(rel.max()), "p99": float(np.percentile(rel, 99)), "mean": float(rel.mean()),
+            "vertices_above_1e-5": int((rel > 1e-5).sum())}
 
 
 def run_reference(args, rank, world):
@@ -442,7 +452,6 @@ PREC_WORKLOAD = ("precision: 49^3 jittered Kuhn cube with sliver tets (min dihed
 
 def bench_prec(args, E, torch):
     mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
-    from oracle import oracle as O  # the FP64 run of the same scheme (error reference)
     t0 = time.perf_counter()
     xyz, tets, sl = mg.sliver_cube(49, 0.10, seed=5)
     M6 = mg.anisotropic_metrics(tets.shape[0], seed=6)
@@ -467,16 +476,12 @@ def bench_prec(args, E, torch):
         st = e.stats()
         runs[name] = {"e": e, "ms": statistics.median(ms), "stats": st, "result": e.getFinalResult()}
     lab, nb = runs["fp32"]["e"].getPartition()
-    t1 = time.perf_counter()
-    r64 = O.solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], M6.ravel()), lab, nb, seeds,
-                    max_iters=1000, precision=64, nthreads=O.num_threads())
-    t64 = time.perf_counter() - t1
-    ref = r64["result"].astype(np.float64)
+    # CPU baseline leg: the FP64 run of the same scheme, which is also the error reference
+    c64 = cpu_sample(xyz, tets, M6.ravel(), seeds, lab, nb, 1000, precision=64)
+    ref = c64["result"]
 
     def err(r):
-        rel = np.abs(r.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-6)
-        return {"max": float(rel.max()), "p99": float(np.percentile(rel, 99)), "mean": float(rel.mean()),
-                "vertices_above_1e-5": int((rel > 1e-5).sum())}
+        return error_stats(r, ref)
 
     out = {"metric": METRIC, "unit": "vertex-updates/s", "n_gpus": 1, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
@@ -493,7 +498,8 @@ def bench_prec(args, E, torch):
                      "residual_max_rel": st["residual_max_rel"], "residual_vertices": st["residual_vertices"]}
     out["value"] = out["mixed"]["vertex_updates_per_s"]
     out["ms_per_step"] = runs["mixed"]["ms"]
-    out["fp64_oracle"] = {"seconds": t64, "iterations": r64["iterations"], "threads": O.num_threads()}
+    out["fp64_oracle"] = {"seconds": c64["seconds"], "iterations": c64["iterations"], "threads": c64["cores"]}
+    out["cpu_baseline"] = {k: c64[k] for k in ("value", "unit", "cores", "kind", "sample")}
     out["e2e"] = None
     return out
 
@@ -655,13 +661,16 @@ def main():
     }
     if not args.no_cpu_baseline and world == 1:
         labels, nb = e.getPartition()
-        res["cpu_baseline"] = {k: v for k, v in cpu_sample(xyz, tets, metric, seed, labels, nb,
-                                                           args.cpu_sample_iters or MAX_ITERS).items()
-                               if k in ("value", "unit", "cores", "kind", "sample")}
+        base = cpu_sample(xyz, tets, metric, seed, labels, nb, args.cpu_sample_iters or MAX_ITERS)
+        res["cpu_baseline"] = {k: v for k, v in base.items() if k in ("value", "unit", "cores", "kind", "sample")}
         # one host thread, on the first 20 iterations (a bounded sample)
         res["cpu_baseline_1thread"] = {k: v for k, v in cpu_sample(xyz, tets, metric, seed, labels, nb, 20,
                                                                    nthreads=1).items()
                                        if k in ("value", "unit", "cores", "kind", "sample")}
+        # the result's error against the FP64 run of the same scheme (same partition)
+        f64 = cpu_sample(xyz, tets, metric, seed, labels, nb, MAX_ITERS, precision=64)
+        res["error_vs_fp64"] = error_stats(out, f64["result"])
+        res["error_vs_fp64"]["fp64_run_s"] = round(f64["seconds"], 2)
     if world == 1 and not args.no_patterns:
         res.update(pattern_summaries(args, E, torch, local))
     print(json.dumps(res), flush=True)
