@@ -191,6 +191,19 @@ def run_reference(args, rank, world):
     return 0
 
 
+def aggregate_replicas(torch, total_ms, updates, world, device):
+    """Replicas (one independent solve stream per rank, no collective in the solve):
+    the job's time is the slowest rank's, its work the sum over ranks."""
+    if world <= 1:
+        return float(total_ms), float(updates)
+    tt = torch.tensor([float(total_ms), float(updates)], dtype=torch.float64, device=device)
+    mx = tt.clone()
+    torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+    sm = tt.clone()
+    torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+    return float(mx[0]), float(sm[1])
+
+
 def partition_host(E, xyz, tets, metric):
     """Labels from the product's partitioner (host-only call, no GPU work)."""
     e = E.Eikonal(False)
@@ -588,16 +601,7 @@ def main():
         launches += 1 + 4 * st["iterations"]
     barrier()
     clocks = sampler.stop()
-    total_ms = sum(times)
-    if world > 1:
-        tt = torch.tensor([total_ms, float(upd)], dtype=torch.float64, device="cuda")
-        mx = tt.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        sm = tt.clone()
-        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
-        total_ms, upd_all = float(mx[0]), float(sm[1])
-    else:
-        upd_all = float(upd)
+    total_ms, upd_all = aggregate_replicas(torch, sum(times), upd, world, "cuda")
     value = upd_all / (total_ms * 1e-3)
 
     # end to end through the C ABI with host buffers
