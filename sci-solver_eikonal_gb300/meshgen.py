@@ -196,7 +196,7 @@ def _has_small_dihedral(P, lim):
 
 
 def sliver_cube(n=49, fraction=0.10, seed=5, max_deg=5.0, directions=12,
-                steps=(0.9, 0.95, 0.98, 0.995)):
+                steps=(0.9, 0.95, 0.98, 0.995), rounds=3):
     """Jittered Kuhn cube (as kuhn_cube(n, 0.2, seed=1)) with about `fraction` of
     its tets flattened into slivers: minimum dihedral angle below `max_deg`
     degrees, every tet keeping its orientation and at least 1e-3 of its volume.
@@ -206,8 +206,9 @@ def sliver_cube(n=49, fraction=0.10, seed=5, max_deg=5.0, directions=12,
     are taken by lattice parity class (same-parity vertices share no tet, so a
     class moves at once); for each vertex, `directions` random ring tets times
     `steps` (fractions of the distance to that tet's opposite face) are tried and
-    the valid move that makes the most slivers in the ring is kept.  Classes run in
-    a random order (PCG64 seed `seed`) until the slivers reach the target.
+    the valid move that most raises the ring's sliver count is kept.  Rounds over
+    the classes (each round in a random order, PCG64 seed `seed`) run until the
+    slivers reach the target.
     Returns xyz (float32), tets, sliver mask (final dihedral test of every tet)."""
     xyz, tets = kuhn_cube(n, 0.2, seed=1)
     xyz = xyz.astype(np.float64)
@@ -226,7 +227,8 @@ def sliver_cube(n=49, fraction=0.10, seed=5, max_deg=5.0, directions=12,
         return xyz.astype(np.float32), tets, np.zeros(nt, dtype=bool)
     R = int((starts[1:] - starts[:-1])[interior].max())
     made = int(_has_small_dihedral(xyz[tets], lim).sum())
-    for cls in rng.permutation(8):
+    classes = [c for _ in range(rounds) for c in rng.permutation(8)]
+    for cls in classes:
         if made >= target:
             break
         sel = np.nonzero(interior & (gi % 2 == (cls & 1)) & (gj % 2 == ((cls >> 1) & 1)) & (gk % 2 == (cls >> 2)))[0]
@@ -259,13 +261,15 @@ def sliver_cube(n=49, fraction=0.10, seed=5, max_deg=5.0, directions=12,
         dirs = rng.choice(R, size=min(directions, R), replace=False)
         with _fut.ThreadPoolExecutor(max_workers=min(len(dirs), os.cpu_count() or 1)) as ex:
             trials = list(ex.map(trial, dirs))
-        best = np.zeros(len(sel), dtype=np.int64)
+        cur = _has_small_dihedral(P0, lim).sum(axis=1)  # ring slivers where the vertex is now
+        best = cur.astype(np.int64)
         best_pos = xyz[sel].copy()
         for bc, bp in trials:  # in direction order: ties keep the earlier direction
             upd = bc > best
             best[upd] = bc[upd]
             best_pos[upd] = bp[upd]
-        take = (best > 0) & (np.cumsum(best) <= max(0, target - made))
+        gain = best - cur
+        take = (gain > 0) & (np.cumsum(gain) <= max(0, target - made))
         xyz[sel[take]] = best_pos[take]
         made = int(_has_small_dihedral(xyz[tets], lim).sum())
     xyz32 = xyz.astype(np.float32)
