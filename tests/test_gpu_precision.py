@@ -48,8 +48,12 @@ def test_precision_mode_moves_toward_fp64(need_gpu, eik, O, prec_case):
     # FP64 on the flagged tets removes most of the FP32 error
     assert errmx.mean() < 0.5 * err32.mean(), (errmx.mean(), err32.mean())
     assert errmx.max() <= err32.max()
-    # the FP64 residual check ran and the solution is a fixed point up to the FIM tolerance
-    assert st["residual_max_rel"] > 0 and st["residual_max_rel"] < 1e-2
+    # the FP64 residual check ran: the solution is a fixed point of the FP64 local
+    # updates up to the FIM stopping tolerance (largest relative gaps sit at small
+    # travel times next to the seeds)
+    assert 0 < st["residual_max_rel"] < 5e-2
+    assert 0 < st["residual_max_abs"] < 5e-2 * float(np.max(emx.getFinalResult()))
+    assert st["residual_vertices"] < 0.05 * xyz.shape[0]
 
 
 def test_precision_kernel_without_flags_is_the_fp32_kernel(need_gpu, eik, prec_case):
