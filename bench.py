@@ -19,7 +19,7 @@ solve (seed -> every block converged).
          host threads on a bounded sample of the same solve
 
 --impl reference times that CPU restatement alone (the reference has no CPU
-driver of its own).  With N > 1 ranks every rank runs its own
+driver of its own, and its CUDA build needs METIS 4 and cusp).  With N > 1 ranks every rank runs its own
 replica (no collective in the solve path); value sums all ranks' updates over
 the slowest rank's time.
 """
@@ -657,7 +657,7 @@ def main():
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                      "kernel": "k_visit3d<false> (block sweeps)",
                      "kernel_ms_per_step": fim_ms / args.steps,
-                     "note": "the sweep kernel is FP32-issue bound (tet local solver); see DESIGN.md"},
+                     "note": "the sweep kernel is FP32-issue bound (tet local solver), not HBM bound"},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times)},
         "clocks": clocks,
