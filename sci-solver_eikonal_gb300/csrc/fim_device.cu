@@ -112,6 +112,9 @@ struct DevArgs {
   // finished, or once the host raised *pending (requests waiting for admission)
   int serve;
   const volatile int* pending;
+  // 3D check visits: per slot the four input times of an earlier check of this
+  // solve that lowered no owned vertex by EPS (all ones: none recorded)
+  uint4* chk_memo;
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -326,6 +329,17 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
           ch |= c << k;
         }
         if (sw == 0) ch = 0xfu;
+        // The check's verdict is a function of the slot's four input times (its
+        // coefficients are fixed for the solve): inputs an earlier check found
+        // lowering no owned vertex by EPS give that verdict again, so the slot is
+        // skipped.
+        bool memo = false;
+        if (kCheck && a.chk_memo) {
+          const uint4 R = a.chk_memo[bd.slot_begin + j];
+          memo = R.x == __float_as_uint(T[0]) && R.y == __float_as_uint(T[1]) && R.z == __float_as_uint(T[2]) &&
+                 R.w == __float_as_uint(T[3]);
+          if (memo) ch = 0u;
+        }
         const float ACBC = s.coef[0 * np + j], BCCD = s.coef[1 * np + j], ACCD = s.coef[2 * np + j];
         const float ADBD = s.coef[3 * np + j], ACAD = s.coef[4 * np + j], BCBD = s.coef[5 * np + j];
         // remaining metric edge products (CUDA_kernels.cu:429-437)
@@ -369,9 +383,15 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
           }
         }
         if (kCheck) {
+          bool moved = false;
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (own[k] && !((T[k] - nw[k]) <= kEps3DLe)) s_moved = 1;  // (double)(old - c) >= 1e-5
+            if (own[k] && !((T[k] - nw[k]) <= kEps3DLe)) moved = true;  // (double)(old - c) >= 1e-5
+          if (moved)
+            s_moved = 1;
+          else if (a.chk_memo && !memo)
+            a.chk_memo[bd.slot_begin + j] = make_uint4(__float_as_uint(T[0]), __float_as_uint(T[1]),
+                                                       __float_as_uint(T[2]), __float_as_uint(T[3]));
         } else {
           unsigned m = 0;
 #pragma unroll
@@ -1240,6 +1260,7 @@ struct DeviceSolve::Impl {
   int* inst_maxit = nullptr;
   int ninst = 1;
   size_t coef_n = 0;
+  uint4* chk_memo = nullptr;  // 3D: coef_n / 6 slots
   // host staging for the initial state
   std::vector<float> h_prev;  // caller's initial values (renumbered), empty when none
   std::vector<int> h_seed_ids, h_act, h_vblock, h_done, h_maxit;
@@ -1304,7 +1325,7 @@ struct DeviceSolve::Impl {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
                   blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids,
-                  slot_f64, coef64, res_cand, inst_vbeg, chunks};
+                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo};
     for (void* p : ps)
       if (p) cudaFree(p);
     slot_f64 = nullptr;
@@ -1312,6 +1333,7 @@ struct DeviceSolve::Impl {
     res_cand = nullptr;
     inst_vbeg = nullptr;
     chunks = nullptr;
+    chk_memo = nullptr;
     nchunks = 0;
     prec = false;
     seed_ids = nullptr;
@@ -1361,6 +1383,8 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.pending = P.pending_dev;
     a.slot_f64 = P.slot_f64;
     a.coef64 = P.coef64;
+    // serving changes an instance's coefficients on admission; its checks keep no memo
+    a.chk_memo = (L.dim == 3 && !serve) ? P.chk_memo : nullptr;
     if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
@@ -1729,6 +1753,15 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   CK(cudaMemsetAsync(P.stampC, 0, sizeof(int) * L.nb, st));
   CK(cudaMemsetAsync(P.visited, 0, L.nb, st));
   CK(cudaMemsetAsync(P.conv, 0, sizeof(int) * L.nb, st));
+  // 3D check memos (16 B per slot) hold only for this solve's coefficients and kernel
+  if (L.dim == 3) {
+    if (!P.chk_memo) {
+      std::string e = dev_alloc(P.chk_memo, P.coef_n / 6);
+      if (!e.empty()) return e;
+      P.drop_graph();
+    }
+    CK(cudaMemsetAsync(P.chk_memo, 0xff, sizeof(uint4) * (P.coef_n / 6), st));
+  }
   {
     std::vector<int> done(P.h_done);
     for (int i = 0; i < P.ninst; ++i)
