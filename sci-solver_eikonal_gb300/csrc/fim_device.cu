@@ -1082,11 +1082,13 @@ __device__ __forceinline__ float uMw_rn(const float* u, const float* m, const fl
   return __fadd_rn(__fadd_rn(__fmul_rn(x, w[0]), __fmul_rn(y, w[1])), __fmul_rn(z, w[2]));
 }
 
+// `memo` (optional): check memos of the same slots, cleared with the new coefficients
 __global__ void k_admit_coef3d(const BlockDesc* blocks, int nb, float* coef, const int* slot_elem, const float* xyz,
-                               const int* tets, const float* M6, float k) {
+                               const int* tets, const float* M6, float k, uint4* memo) {
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const BlockDesc d = blocks[b];
     for (int j = threadIdx.x; j < d.nslots; j += blockDim.x) {
+      if (memo) memo[d.slot_begin + j] = make_uint4(~0u, ~0u, ~0u, ~0u);
       const int t = slot_elem[d.slot_begin + j];
       float P[4][3], m[6];
       for (int q = 0; q < 4; ++q) {
@@ -1383,8 +1385,8 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.pending = P.pending_dev;
     a.slot_f64 = P.slot_f64;
     a.coef64 = P.coef64;
-    // serving changes an instance's coefficients on admission; its checks keep no memo
-    a.chk_memo = (L.dim == 3 && !serve) ? P.chk_memo : nullptr;
+    // (serving clears an instance's memos when admission rewrites its coefficients)
+    a.chk_memo = (L.dim == 3) ? P.chk_memo : nullptr;
     if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
@@ -1557,7 +1559,8 @@ std::string DeviceSolve::refresh_coef_built(const float* M6) {
   cudaStream_t st = (cudaStream_t)stream_;
   CK(cudaMemcpyAsync(P.src[0].M6, M6, sizeof(float) * 6 * (size_t)L.ne, cudaMemcpyHostToDevice, st));
   k_admit_coef3d<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.slot_elem,
-                                                                    P.src[0].xyz, P.src[0].tets, P.src[0].M6, 1.0f);
+                                                                    P.src[0].xyz, P.src[0].tets, P.src[0].M6, 1.0f,
+                                                                    nullptr);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   return "";
@@ -1981,6 +1984,7 @@ std::string selftest_tri_blocks(const float* in, int n, bool check, float* out) 
 size_t device_footprint(const Layout& L) {
   const size_t nv = (size_t)L.nv, nb = (size_t)L.nb;
   return nb * sizeof(BlockDesc) + L.coef.size() * sizeof(float) + (size_t)L.total_slots * (sizeof(uint2) + sizeof(int)) +
+         (L.dim == 3 ? (size_t)L.total_slots * sizeof(uint4) : 0) +
          L.halo_ids.size() * sizeof(int) + (L.nbr_off.size() + L.nbr.size()) * sizeof(int) +
          nv * (2 * sizeof(int) + 5 * sizeof(float)) + nb * (7 * sizeof(int) + 1) + 5 * sizeof(int);
 }
@@ -2019,6 +2023,11 @@ std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, con
     if (!(e = dev_alloc(P.slot_elem, (size_t)std::max(L.total_slots, 1))).empty()) return e;
   }
   CK(cudaMemcpyAsync(P.slot_elem, L.slot_elem.data(), sizeof(int) * L.slot_elem.size(), cudaMemcpyHostToDevice, st));
+  if (L.dim == 3) {
+    std::string e;
+    if (!P.chk_memo && !(e = dev_alloc(P.chk_memo, P.coef_n / 6)).empty()) return e;
+    CK(cudaMemsetAsync(P.chk_memo, 0xff, sizeof(uint4) * (P.coef_n / 6), st));
+  }
   CK(cudaHostAlloc((void**)&P.host_res, sizeof(float) * std::max(L.nv, 1), cudaHostAllocDefault));
   if (!P.pending_host) {
     CK(cudaHostAlloc((void**)&P.pending_host, sizeof(int), cudaHostAllocMapped));
@@ -2100,7 +2109,7 @@ std::string DeviceSolve::serve_admit(const std::vector<Admission>& adm) {
     const int g = std::max(1, std::min(nbi, 4096));
     if (L.dim == 3)
       k_admit_coef3d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.xyz, src.tets, src.M6,
-                                        x.coef_scale);
+                                        x.coef_scale, P.chk_memo);
     else
       k_admit_coef2d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.speed, x.coef_scale);
     k_admit_seeds<<<1, 256, 0, st>>>(P.args, i, P.seed_ids + off[q], nsd[q], P.seed_ids + boff[q], nbk[q],
