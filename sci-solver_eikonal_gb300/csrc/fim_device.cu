@@ -222,7 +222,7 @@ __device__ __forceinline__ Smem carve(unsigned char* sm, const DevArgs& a, int n
   return s;
 }
 
-size_t smem_bytes(int ncoef, int max_slots_pad, int max_local, int max_owned) {
+__host__ __device__ inline size_t smem_bytes(int ncoef, int max_slots_pad, int max_local, int max_owned) {
   size_t n = (size_t)ncoef * max_slots_pad * 4 + (size_t)max_slots_pad * 8 + 2 * 16 * (size_t)max_slots_pad +
              2 * (size_t)max_slots_pad + 4 * (size_t)max_local + 4 * (size_t)max_owned + (size_t)max_owned;
   return (n + 15) & ~(size_t)15;
@@ -231,15 +231,18 @@ size_t smem_bytes(int ncoef, int max_slots_pad, int max_local, int max_owned) {
 // Issue the two bulk copies of block `bd` (coefficients + corner ids) and gather
 // the owned / halo travel times from `Tsrc`.  Returns false on a copy timeout.
 __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd, int ncoef, const Smem& s,
-                                           unsigned long long* bar, unsigned& parity, const float* Tsrc) {
+                                           unsigned long long* bar, unsigned& parity, const float* Tsrc,
+                                           uint4* smemo = nullptr) {
   const int tid = threadIdx.x, NT = blockDim.x;
   if (tid == 0) {
     fence_proxy_async();
     const unsigned bc = 4u * ncoef * bd.nslots_pad, bl = 8u * bd.nslots_pad;
-    if (bc + bl > 0) {
-      mbar_expect_tx(bar, bc + bl);
+    const unsigned bm = smemo ? 16u * bd.nslots_pad : 0u;
+    if (bc + bl + bm > 0) {
+      mbar_expect_tx(bar, bc + bl + bm);
       bulk_g2s(s.coef, a.coef + (size_t)ncoef * bd.slot_begin, bc, bar);
       bulk_g2s(s.lv, a.lv + bd.slot_begin, bl, bar);
+      if (bm) bulk_g2s(smemo, a.chk_memo + bd.slot_begin, bm, bar);
     } else {
       mbar_expect_tx(bar, 0);
     }
@@ -266,6 +269,10 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   __shared__ int s_item;
   __shared__ volatile int s_moved;  // check visits: some owned vertex drops by >= EPS
   const Smem s0 = carve(sm, a, 6);
+  // check memos of the block's slots, staged behind the visit's carve
+  uint4* const smemo = (kCheck && a.chk_memo)
+                           ? reinterpret_cast<uint4*>(sm + smem_bytes(6, a.max_slots_pad, a.max_local, a.max_owned))
+                           : nullptr;
   const int tid = threadIdx.x, NT = blockDim.x;
   const Ctl* ctl = a.ctl;
   const int iter = ctl->iter;
@@ -290,7 +297,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
     }
     const BlockDesc bd = a.blocks[b];
     Smem s = s0;
-    const bool ok = load_block(a, bd, 6, s, &bar, parity, a.Ta);
+    const bool ok = load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo);
     if (!ok) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);
@@ -334,8 +341,8 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
         // lowering no owned vertex by EPS give that verdict again, so the slot is
         // skipped.
         bool memo = false;
-        if (kCheck && a.chk_memo) {
-          const uint4 R = a.chk_memo[bd.slot_begin + j];
+        if (kCheck && smemo) {
+          const uint4 R = smemo[j];
           memo = R.x == __float_as_uint(T[0]) && R.y == __float_as_uint(T[1]) && R.z == __float_as_uint(T[2]) &&
                  R.w == __float_as_uint(T[3]);
           if (memo) ch = 0u;
@@ -389,7 +396,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
             if (own[k] && !((T[k] - nw[k]) <= kEps3DLe)) moved = true;  // (double)(old - c) >= 1e-5
           if (moved)
             s_moved = 1;
-          else if (a.chk_memo && !memo)
+          else if (smemo && !memo)
             a.chk_memo[bd.slot_begin + j] = make_uint4(__float_as_uint(T[0]), __float_as_uint(T[1]),
                                                        __float_as_uint(T[2]), __float_as_uint(T[3]));
         } else {
@@ -1403,6 +1410,16 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     if (L.dim == 3) {
       kv_fim = P.prec ? (void*)k_visit3d<false, true> : (void*)k_visit3d<false>;
       kv_chk = P.prec ? (void*)k_visit3d<true, true> : (void*)k_visit3d<true>;
+      // the check kernel stages the block's check memos (16 B per slot) in shared memory
+      if (a.chk_memo) {
+        int maxsm = 0;
+        CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const size_t with_memo = P.smem + sizeof(uint4) * (size_t)P.max_slots_pad;
+        if (with_memo + 64 <= (size_t)maxsm)
+          vsmem = with_memo;
+        else
+          a.chk_memo = nullptr;
+      }
     } else if (slot2d) {
       vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
       vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
