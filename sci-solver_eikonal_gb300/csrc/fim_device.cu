@@ -335,7 +335,18 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
           const unsigned c = own[k] ? (unsigned)s.vchg[id[k]] : ((unsigned)s.m0[j] >> k) & 1u;
           ch |= c << k;
         }
-        if (sw == 0) ch = 0xfu;
+        if (sw == 0) {
+          ch = 0xfu;
+        } else if (sw == nsweeps - 1) {
+          // Last sweep: only the owned apexes count (copies of other blocks' corners
+          // are dropped after the visit).  An owned apex whose three other corners
+          // did not change repeats its previous candidate, which its time already
+          // absorbed, so a slot with no such change for any owned apex is skipped.
+          unsigned need = 0;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) need |= (own[k] && (ch & ~(1u << k))) ? 1u : 0u;
+          if (!need) ch = 0u;
+        }
         // The check's verdict is a function of the slot's four input times (its
         // coefficients are fixed for the solve): inputs an earlier check found
         // lowering no owned vertex by EPS give that verdict again, so the slot is
