@@ -393,10 +393,18 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
               const double dCDCD = dADCD - dACCD, dADAD = dADCD + dACAD, dACAC = dACAD - dACCD;
               const double dBDBD = dBCBD + dCDBD, dBCBC = dBCBD - dBCCD;
               const double A = TA, B = TB, C = TC, D = TD;
-              nw[3] = fminf(TD, (float)tet_update_f64(A, B, C, dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD));
-              nw[0] = fminf(TA, (float)tet_update_f64(B, D, C, dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC));
-              nw[1] = fminf(TB, (float)tet_update_f64(A, D, C, dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC));
-              nw[2] = fminf(TC, (float)tet_update_f64(A, B, D, dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD));
+              // in a check and in a visit's last sweep only the owned apexes count
+              // (the copies of other blocks' corners are dropped), so the FP64
+              // updates of the others are left out there
+              const bool all = !kCheck && sw != nsweeps - 1;
+              if (all || own[3])
+                nw[3] = fminf(TD, (float)tet_update_f64(A, B, C, dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD));
+              if (all || own[0])
+                nw[0] = fminf(TA, (float)tet_update_f64(B, D, C, dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC));
+              if (all || own[1])
+                nw[1] = fminf(TB, (float)tet_update_f64(A, D, C, dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC));
+              if (all || own[2])
+                nw[2] = fminf(TC, (float)tet_update_f64(A, B, D, dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD));
             }
           }
         }
