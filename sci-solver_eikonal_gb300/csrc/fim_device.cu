@@ -935,12 +935,28 @@ __global__ void k_vertex_test2d(DevArgs a) {
     if (a.inst_done[ch.x]) continue;  // uniform across the CTA
     const int v1 = min(ch.y + kVertexChunk, a.inst_vbeg[ch.x + 1]);
     int bad = 0;
-    for (int v = ch.y + threadIdx.x; v < v1; v += blockDim.x) {
-      const float cur = a.Ta[v];
-      float diff = a.prev[v] - cur;
-      if (diff < 0.0f) diff = -diff;
-      if (!((diff <= kEps2D) && (cur < kLarge2DDev))) bad = 1;
-      a.prev[v] = cur;
+    // four vertices per thread per step, all loads issued before the stores
+    constexpr int kU = 4;
+    const float* __restrict__ Ta = a.Ta;
+    float* __restrict__ prev = a.prev;
+    for (int v0 = ch.y + threadIdx.x; v0 < v1; v0 += kU * blockDim.x) {
+      float cur[kU], old[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int v = v0 + u * blockDim.x;
+        cur[u] = (v < v1) ? Ta[v] : 0.0f;
+        old[u] = (v < v1) ? prev[v] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int v = v0 + u * blockDim.x;
+        if (v < v1) {
+          float diff = old[u] - cur[u];
+          if (diff < 0.0f) diff = -diff;
+          if (!((diff <= kEps2D) && (cur[u] < kLarge2DDev))) bad = 1;
+          prev[v] = cur[u];
+        }
+      }
     }
     bad = __syncthreads_or(bad);
     if (threadIdx.x == 0 && bad && a.inst_fail[ch.x] == 0) atomicOr(&a.inst_fail[ch.x], 1);
