@@ -935,8 +935,8 @@ __global__ void k_vertex_test2d(DevArgs a) {
     if (a.inst_done[ch.x]) continue;  // uniform across the CTA
     const int v1 = min(ch.y + kVertexChunk, a.inst_vbeg[ch.x + 1]);
     int bad = 0;
-    // four vertices per thread per step, all loads issued before the stores
-    constexpr int kU = 4;
+    // eight vertices per thread per step, all loads issued before the stores
+    constexpr int kU = 8;
     const float* __restrict__ Ta = a.Ta;
     float* __restrict__ prev = a.prev;
     for (int v0 = ch.y + threadIdx.x; v0 < v1; v0 += kU * blockDim.x) {
