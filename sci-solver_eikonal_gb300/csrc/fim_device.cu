@@ -826,11 +826,9 @@ __global__ void k_commit3d(DevArgs a) {
   const int count = a.ctl->nact;
   const int* act = act_list(a, iter);
   int* nxt = next_list(a, iter);
-  for (;;) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(&a.ctl->work_b, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= count) break;
+  // one warp per list entry, assigned by warp index (no claim round trip)
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int item = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); item < count; item += nwarps) {
     const int b = act[item];
     if (a.inst_done[a.blk_inst[b]]) continue;
     const BlockDesc bd = a.blocks[b];
@@ -855,11 +853,9 @@ __global__ void k_activate2d(DevArgs a) {
   const int iter = a.ctl->iter, stamp = iter + 1;
   const int count = a.ctl->nact;
   const int* act = act_list(a, iter);
-  for (;;) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(&a.ctl->work_b, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= count) break;
+  // one warp per list entry, assigned by warp index (no claim round trip)
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int item = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); item < count; item += nwarps) {
     const int b = act[item];
     if (a.inst_done[a.blk_inst[b]] || !a.conv[b]) continue;
     for (int e = a.nbr_off[b] + lane; e < a.nbr_off[b + 1]; e += 32) {
