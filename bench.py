@@ -29,6 +29,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -102,7 +103,7 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{gpu_index}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"eikonal_clocks_{os.getpid()}_{gpu_index}.csv")
 
     def start(self):
         try:
@@ -128,6 +129,10 @@ class ClockSampler:
             f = [x.strip() for x in line.split(",")]
             if len(f) >= 9:
                 rows.append(f)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         if not rows:
             return None
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]

@@ -347,9 +347,9 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
           for (int k = 0; k < 4; ++k) need |= (own[k] && (ch & ~(1u << k))) ? 1u : 0u;
           if (!need) ch = 0u;
         }
-        // The check's verdict is a function of the slot's four input times (its
+        // The check's outcome is a function of the slot's four input times (its
         // coefficients are fixed for the solve): inputs an earlier check found
-        // lowering no owned vertex by EPS give that verdict again, so the slot is
+        // lowering no owned vertex by EPS give that outcome again, so the slot is
         // skipped.
         bool memo = false;
         if (kCheck && smemo) {
