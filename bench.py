@@ -326,7 +326,8 @@ def bench_batch(args, E, torch, world, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profile_traffic("fim2d_slot_batch.md"), "peak_source": peak_src,
                      "kernel": "k_visit2d_slot<false,7> (block sweeps)",
-                     "kernel_ms_per_step": fim_ms / args.steps},
+                     "kernel_ms_per_step": fim_ms / args.steps,
+                     "issue": issue_roofline("fim2d_slot_batch.md")},
         "clocks": clocks,
         "gpu_launches": int(1 + 4 * sum(iters)),
     }
@@ -339,14 +340,27 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def profile_traffic(name):
-    """DRAM bytes per launch of a kernel, from its committed ncu summary."""
+def profile_value(name, key):
+    """A `key: value` figure of a committed ncu summary (None when absent)."""
     path = os.path.join(ROOT, "profiles", name)
     if os.path.exists(path):
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     return None
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch of a kernel, from its committed ncu summary."""
+    return profile_value(name, "traffic_bytes_per_launch")
+
+
+def issue_roofline(name):
+    """The sweep kernels are bound by instruction issue, not HBM: the issue-slot
+    utilisation ncu measured for the kernel (from its committed summary)."""
+    v = profile_value(name, "issue_active_pct")
+    return None if v is None else {"issue_active_frac_of_peak": v / 100.0,
+                                   "source": f"ncu --set full capture in profiles/{name}"}
 
 
 SERVE_WORKLOAD = ("serving: resident pool of icospheres L5, L6, L7 and L6 with other speeds (2D) and jittered "
@@ -662,7 +676,8 @@ def main():
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                      "kernel": "k_visit3d<false> (block sweeps)",
                      "kernel_ms_per_step": fim_ms / args.steps,
-                     "note": "the sweep kernel is FP32-issue bound (tet local solver), not HBM bound"},
+                     "note": "the sweep kernel is FP32-issue bound (tet local solver), not HBM bound",
+                     "issue": issue_roofline("fim3d_visit_c3d.md")},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times)},
         "clocks": clocks,
