@@ -268,7 +268,16 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
   __shared__ volatile int s_moved;  // check visits: some owned vertex drops by >= EPS
+  __shared__ int s_nlist;
   const Smem s0 = carve(sm, a, 6);
+  // sweep visits: the slots the last sweep must recompute, packed into a list so
+  // they fill few warps (the region behind the carve that check visits use for
+  // memos; present whenever the check memo is).  Not in the precision kernel: there
+  // the changed loop made the compiler fuse its FP32 path differently from the
+  // FP32 kernel's, which it must equal bit for bit.
+  int* const slist = (!kCheck && !kPrec && a.chk_memo)
+                         ? reinterpret_cast<int*>(sm + smem_bytes(6, a.max_slots_pad, a.max_local, a.max_owned))
+                         : nullptr;
   // check memos of the block's slots, staged behind the visit's carve
   uint4* const smemo = (kCheck && a.chk_memo)
                            ? reinterpret_cast<uint4*>(sm + smem_bytes(6, a.max_slots_pad, a.max_local, a.max_owned))
@@ -318,7 +327,10 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
     __syncthreads();
     int myconv = 1;
     for (int sw = 0; sw < nsweeps; ++sw) {
-      for (int j = tid; j < ns; j += NT) {
+      const bool packed = (slist != nullptr) && sw > 0 && sw == nsweeps - 1;
+      const int cnt = packed ? s_nlist : ns;
+      for (int i = tid; i < cnt; i += NT) {
+        const int j = packed ? slist[i] : i;
         // A check only decides whether the block stays converged; one candidate
         // that lowers an owned vertex by EPS or more decides it (the minimum can
         // only be lower), so the remaining slots are skipped.
@@ -452,6 +464,35 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
       float* th = s.h0; s.h0 = s.h1; s.h1 = th;
       unsigned char* tm = s.m0; s.m0 = s.m1; s.m1 = tm;
       __syncthreads();
+      // list the slots with an owned apex whose other corners changed (the rest
+      // repeat absorbed candidates in the last sweep, see the sweep loop)
+      if (slist && sw + 1 == nsweeps - 1) {
+        if (tid == 0) s_nlist = 0;
+        __syncthreads();
+        for (int j = tid; j < ns; j += NT) {
+          const uint2 l = s.lv[j];
+          const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+          unsigned ch = 0, om = 0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const bool o = id[q] < nown;
+            const unsigned c = o ? (unsigned)s.vchg[id[q]] : ((unsigned)s.m0[j] >> q) & 1u;
+            ch |= c << q;
+            om |= (o ? 1u : 0u) << q;
+          }
+          unsigned need = 0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) need |= (((om >> q) & 1u) && (ch & ~(1u << q))) ? 1u : 0u;
+          const unsigned am = __activemask();
+          const unsigned bm = __ballot_sync(am, need != 0);
+          const int lane = tid & 31, leader = __ffs(am) - 1;
+          int base = 0;
+          if (lane == leader && bm) base = atomicAdd(&s_nlist, __popc(bm));
+          base = __shfl_sync(am, base, leader);
+          if (need) slist[base + __popc(bm & ((1u << lane) - 1u))] = j;
+        }
+        __syncthreads();
+      }
     }
     const int allc = __syncthreads_and(myconv);
     if (!kCheck)
