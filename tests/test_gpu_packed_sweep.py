@@ -1,0 +1,40 @@
+"""The 3D sweep kernel runs the last sweep of a visit from a packed list of the slots
+that can still change an owned vertex; the precision kernel keeps the plain loop over
+every slot.  With nothing flagged the precision kernel computes the FP32 updates, so
+the two must agree bit for bit for any number of sweeps per visit."""
+import numpy as np
+import pytest
+
+from conftest import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("sweeps", [1, 2, 3])
+def test_packed_last_sweep_equals_plain_loop(need_gpu, eik, mg, O, sweeps):
+    xyz, tets = mg.kuhn_cube(21, 0.2, seed=21)
+    sp = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=22)
+    metric = (1.0 / sp.astype(np.float64) ** 2).astype(np.float32)
+    out = []
+    for prec in (0, 1):
+        e = eik.Eikonal(False)
+        e.set_mesh(xyz, tets)
+        e.initSpeedMtxMultipliers(metric)
+        e.setSeeds([0, xyz.shape[0] - 1])
+        e.maxVertsPerBlock_ = 64
+        e.keepHistory_ = 0
+        e.fimSweeps_ = sweeps
+        e.precisionMode_ = prec
+        e.precisionKappa_ = 1e30  # nothing flagged: the FP32 path everywhere
+        e.solveEikonal()
+        assert e.stats()["flagged_tets"] == 0
+        out.append(e)
+    assert bits_equal(out[0].getFinalResult(), out[1].getFinalResult())
+    assert out[0].numIterations() == out[1].numIterations()
+    assert out[0].stats()["vertex_updates"] == out[1].stats()["vertex_updates"]
+    # and the scheme itself: the CPU restatement with the same sweep count
+    lab, nb = out[0].getPartition()
+    want = O.solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], metric), lab, nb,
+                     [0, xyz.shape[0] - 1], nsweeps=sweeps)["result"]
+    rel = np.abs(out[0].getFinalResult() - want) / np.maximum(np.abs(want), 1e-6)
+    assert np.median(rel) < 1e-6 and rel.max() < 1e-2
