@@ -8,6 +8,7 @@
 #include <cstring>
 #include <numeric>
 #include <set>
+#include <thread>
 
 namespace eikgb {
 
@@ -289,17 +290,28 @@ int metis_rule_blocks(int nv, int k, int dim) {
 }
 
 namespace {
-void rcb(const float* xyz, int* ids, int n, int nparts, int first, int* labels) {
+// A point carries its coordinates so the selections below read contiguous memory.
+struct RcbPoint {
+  float c[3];
+  int id;
+};
+
+// Recursive coordinate bisection: split the longest bounding-box axis at the
+// element that gives the left half its share of parts.  Points are ordered by
+// (coordinate, id), a total order, so each half is a fixed set whatever the
+// selection algorithm and the threads that run the halves; the labels are a
+// function of the coordinates alone.
+void rcb(RcbPoint* p, int n, int nparts, int first, int* labels, int depth) {
   if (nparts <= 1 || n <= 1) {
-    for (int i = 0; i < n; ++i) labels[ids[i]] = first;
+    for (int i = 0; i < n; ++i) labels[p[i].id] = first;
     return;
   }
-  float lo[3] = {xyz[3 * ids[0]], xyz[3 * ids[0] + 1], xyz[3 * ids[0] + 2]};
+  float lo[3] = {p[0].c[0], p[0].c[1], p[0].c[2]};
   float hi[3] = {lo[0], lo[1], lo[2]};
   for (int i = 1; i < n; ++i)
     for (int d = 0; d < 3; ++d) {
-      lo[d] = std::min(lo[d], xyz[3 * ids[i] + d]);
-      hi[d] = std::max(hi[d], xyz[3 * ids[i] + d]);
+      lo[d] = std::min(lo[d], p[i].c[d]);
+      hi[d] = std::max(hi[d], p[i].c[d]);
     }
   int ax = 0;
   for (int d = 1; d < 3; ++d)
@@ -307,20 +319,27 @@ void rcb(const float* xyz, int* ids, int n, int nparts, int first, int* labels) 
   const int pl = nparts / 2;
   // left half gets a share proportional to its part count; sizes stay within one
   const int nl = (int)(((long long)n * pl) / nparts);
-  std::nth_element(ids, ids + nl, ids + n, [&](int a, int b) {
-    const float xa = xyz[3 * a + ax], xb = xyz[3 * b + ax];
-    return xa < xb || (xa == xb && a < b);
+  std::nth_element(p, p + nl, p + n, [ax](const RcbPoint& a, const RcbPoint& b) {
+    return a.c[ax] < b.c[ax] || (a.c[ax] == b.c[ax] && a.id < b.id);
   });
-  rcb(xyz, ids, nl, pl, first, labels);
-  rcb(xyz, ids + nl, n - nl, nparts - pl, first + pl, labels);
+  // the two halves are independent: the first levels run them on two threads
+  if (depth < 4 && n >= 32768) {
+    std::thread left([=] { rcb(p, nl, pl, first, labels, depth + 1); });
+    rcb(p + nl, n - nl, nparts - pl, first + pl, labels, depth + 1);
+    left.join();
+  } else {
+    rcb(p, nl, pl, first, labels, depth + 1);
+    rcb(p + nl, n - nl, nparts - pl, first + pl, labels, depth + 1);
+  }
 }
 }  // namespace
 
 void partition_rcb(int nv, const float* xyz, int nparts, std::vector<int>& labels) {
   labels.assign(nv, 0);
-  std::vector<int> ids(nv);
-  std::iota(ids.begin(), ids.end(), 0);
-  rcb(xyz, ids.data(), nv, std::max(1, std::min(nparts, nv)), 0, labels.data());
+  if (nv <= 0) return;
+  std::vector<RcbPoint> pts(nv);
+  for (int v = 0; v < nv; ++v) pts[v] = RcbPoint{{xyz[3 * v], xyz[3 * v + 1], xyz[3 * v + 2]}, v};
+  rcb(pts.data(), nv, std::max(1, std::min(nparts, nv)), 0, labels.data(), 0);
 }
 
 std::string partition_square(int nv, int dim, int L, int W, int D, int bl, int bw, int bd,
