@@ -562,6 +562,19 @@ def main():
             print(json.dumps(res), flush=True)
         return 0
     xyz, tets, metric, seed = build_workload()
+    # load the library's kernels once (a small solve), so the first solve below
+    # times this mesh's setup rather than the process's module loading
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    for dev_setup in (1, 0):
+        wx, wt = mg.kuhn_cube(9, 0.2, seed=1)
+        w = E.Eikonal(False)
+        w.set_mesh(wx, wt)
+        w.setSeeds([0])
+        w.keepHistory_ = 0
+        w.deviceSetup_ = dev_setup
+        w.directLaunch_ = 1 if args.launch == "direct" else 0
+        w.solveEikonal()
+        del w
     e = E.Eikonal(False)
     e.set_mesh(xyz, tets)
     e.initSpeedMtxMultipliers(metric)
@@ -671,7 +684,9 @@ def main():
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
         "setup_s": setup_s,
         "first_solve_s": {"device_setup": setup_s, "host_setup": setup_host_s,
-                          "bitwise_equal": same_as_host},
+                          "bitwise_equal": same_as_host,
+                          "note": "first solve of this mesh (partition, layout, upload, graph, solve) in a "
+                                  "process whose kernels are loaded"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                      "kernel": "k_visit3d<false> (block sweeps)",
