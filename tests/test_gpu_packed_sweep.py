@@ -38,3 +38,26 @@ def test_packed_last_sweep_equals_plain_loop(need_gpu, eik, mg, O, sweeps):
                      [0, xyz.shape[0] - 1], nsweeps=sweeps)["result"]
     rel = np.abs(out[0].getFinalResult() - want) / np.maximum(np.abs(want), 1e-6)
     assert np.median(rel) < 1e-6 and rel.max() < 1e-2
+
+
+def test_cta_size_does_not_change_results(need_gpu, eik, mg):
+    """Blocks larger than the CTA run several slots per thread in every loop (the
+    packed list, the check memo, the copies); the results must not depend on it."""
+    xyz, tets = mg.kuhn_cube(25, 0.2, seed=31)
+    sp = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=32)
+    metric = (1.0 / sp.astype(np.float64) ** 2).astype(np.float32)
+    out = []
+    for threads in (0, 256, 128):
+        e = eik.Eikonal(False)
+        e.set_mesh(xyz, tets)
+        e.initSpeedMtxMultipliers(metric)
+        e.setSeeds([7])
+        e.maxVertsPerBlock_ = 64
+        e.keepHistory_ = 0
+        e.threadsPerBlock_ = threads
+        e.solveEikonal()
+        out.append(e)
+    for e in out[1:]:
+        assert bits_equal(out[0].getFinalResult(), e.getFinalResult())
+        assert out[0].numIterations() == e.numIterations()
+        assert out[0].stats()["check_visits"] == e.stats()["check_visits"]
