@@ -173,7 +173,9 @@ int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned 
  *   which = 3 / 4: each case is a triangle forming its own block (T0 T1 T2 LenAB
  *              (v0v1) LenBC (v1v2) LenCA (v2v0) speedInv), passed once through the
  *              2D block-sweep kernel (7 sweeps) / neighbour-check kernel (1 sweep);
- *              3 outputs per case. */
+ *              3 outputs per case;
+ *   which = 5: the precision mode's FP64 tet update (no reference counterpart),
+ *              inputs as for 0, the FP64 result rounded to FP32. */
 int eik_selftest_local_update(int which, const float* in, float* out, int n);
 
 /* Failure-path self-test (no counterpart in the reference, which has no bounded

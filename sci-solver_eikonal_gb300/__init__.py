@@ -521,7 +521,7 @@ class EikonalServer:
 
 def selftest_local_update(which, inputs):
     """Evaluates the device local updates element-wise (see eik_selftest_local_update)."""
-    nin, nout = {0: (9, 1), 1: (7, 1), 2: (2, 2), 3: (7, 3), 4: (7, 3)}[which]
+    nin, nout = {0: (9, 1), 1: (7, 1), 2: (2, 2), 3: (7, 3), 4: (7, 3), 5: (9, 1)}[which]
     a = np.ascontiguousarray(inputs, dtype=np.float32).reshape(-1, nin)
     out = np.empty((a.shape[0], nout), dtype=np.float32)
     rc = lib().eik_selftest_local_update(which, _fptr(a), _fptr(out), a.shape[0])

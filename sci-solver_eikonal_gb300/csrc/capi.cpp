@@ -579,7 +579,7 @@ int eik_selftest_wait_timeout(double* waited_ms) {
 }
 
 int eik_selftest_local_update(int which, const float* in, float* out, int n) {
-  if (which < 0 || which > 4 || n < 0 || (n > 0 && (!in || !out))) return EIK_ERR_ARG;
+  if (which < 0 || which > 5 || n < 0 || (n > 0 && (!in || !out))) return EIK_ERR_ARG;
   return selftest_device(which, in, out, n).empty() ? EIK_OK : EIK_ERR_CUDA;
 }
 

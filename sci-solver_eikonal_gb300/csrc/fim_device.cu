@@ -1270,6 +1270,15 @@ __global__ void k_selftest_tri(const float* in, float* out, int n) {
     out[i] = tri_update<false>(a[0], a[1], a[2], a[3], a[4], a[5], a[6], 0.f, 0.f);
   }
 }
+// precision mode's FP64 tet update from FP32 inputs (the Gram terms widened as the
+// kernel widens its FP64 products)
+__global__ void k_selftest_tet64(const float* in, float* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float* a = in + 9 * (size_t)i;
+    out[i] = (float)tet_update_f64(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
+  }
+}
 __global__ void k_selftest_quot(const float* in, float* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -2300,7 +2309,7 @@ std::string selftest_wait_timeout(int* status, double* waited_ms) {
 
 std::string selftest_device(int which, const float* in, float* out, int n) {
   if (which == 3 || which == 4) return selftest_tri_blocks(in, n, which == 4, out);
-  const int nin = (which == 0) ? 9 : (which == 1) ? 7 : 2;
+  const int nin = (which == 0 || which == 5) ? 9 : (which == 1) ? 7 : 2;
   const int nout = (which == 2) ? 2 : 1;
   float *din = nullptr, *dout = nullptr;
   CK(cudaMalloc((void**)&din, sizeof(float) * (size_t)nin * n + 16));
@@ -2309,6 +2318,7 @@ std::string selftest_device(int which, const float* in, float* out, int n) {
   const int grid = (n + 127) / 128;
   if (n > 0) {
     if (which == 0) k_selftest_tet<<<grid, 128>>>(din, dout, n);
+    else if (which == 5) k_selftest_tet64<<<grid, 128>>>(din, dout, n);
     else if (which == 1) k_selftest_tri<<<grid, 128>>>(din, dout, n);
     else k_selftest_quot<<<grid, 128>>>(din, dout, n);
   }

@@ -64,3 +64,25 @@ def test_precision_kernel_without_flags_is_the_fp32_kernel(need_gpu, eik, prec_c
     assert enf.stats()["flagged_tets"] == 0
     assert bits_equal(e32.getFinalResult(), enf.getFinalResult())
     assert e32.numIterations() == enf.numIterations()
+
+
+def test_fp64_update_matches_the_fp64_oracle(need_gpu, eik, O):
+    """The precision mode's FP64 tet update (FP32 roots of the candidate distances)
+    against the CPU restatement in FP64, on random tets over eight decades of size
+    with random arrival times."""
+    rng = np.random.default_rng(17)
+    n = 20000
+    P = rng.normal(size=(n, 4, 3)) * np.exp(rng.uniform(-4, 4, (n, 1, 1)))
+    T = rng.uniform(0, 2, (n, 3)) * np.abs(P[:, :1, 0])
+    AC, BC, CD = P[:, 2] - P[:, 0], P[:, 2] - P[:, 1], P[:, 3] - P[:, 2]
+    g = np.stack([(AC * AC).sum(1), (AC * BC).sum(1), (AC * CD).sum(1), (BC * BC).sum(1), (BC * CD).sum(1),
+                  (CD * CD).sum(1)], 1)
+    inp = np.concatenate([T, g], 1).astype(np.float32)
+    got = eik.selftest_local_update(5, inp).astype(np.float64)
+    f = O.lib().oracle_tet_update_f64
+    want = np.array([f(*map(float, row)) for row in inp])
+    rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-30)
+    # FP32 roots of the candidate distances: ~1e-7; a candidate whose barycentric
+    # test sits on its boundary may switch in rare cases
+    assert np.median(rel) < 1e-7
+    assert np.mean(rel < 1e-6) > 0.999
