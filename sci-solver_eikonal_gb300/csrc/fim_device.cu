@@ -52,9 +52,8 @@ struct Ctl {
   int nact;       // active blocks this iteration
   int nnew;       // newly activated blocks this iteration
   int nnext;      // active list being built for the next iteration
-  int work_a, work_b, work_c, work_d;
-  int done_c, done_d;
-  int conv_fail;  // 2D: a vertex failed the all-vertex test this iteration
+  int work_a, work_c;  // claim counters of the sweep and check visits
+  int done_d;     // 2D: CTAs of the all-vertex test finished (the last one closes)
   int error;
   int stop;       // set when the outer loop must end (read by the direct-launch loop)
   unsigned long long updates, fim_visits, chk_visits, slot_visits, halo_visits, owned_visits;
@@ -938,9 +937,8 @@ __device__ void finish_iteration_cta(const DevArgs& a, bool vertex_test) {
     c->nact = c->nnext;
     c->nnext = 0;
     c->nnew = 0;
-    c->work_a = c->work_b = c->work_c = c->work_d = 0;
-    c->done_c = c->done_d = 0;
-    c->conv_fail = 0;
+    c->work_a = c->work_c = 0;
+    c->done_d = 0;
     bool go = any && c->error == 0;
     if (a.serve && (fin || *a.pending != 0)) go = false;
     c->stop = go ? 0 : 1;
@@ -2360,9 +2358,8 @@ __global__ void k_close3d_noalloc(DevArgs a) {
   c->nact = c->nnext;
   c->nnext = 0;
   c->nnew = 0;
-  c->work_a = c->work_b = c->work_c = c->work_d = 0;
-  c->done_c = c->done_d = 0;
-  c->conv_fail = 0;
+  c->work_a = c->work_c = 0;
+  c->done_d = 0;
 }
 
 std::mutex g_noalloc_mutex;
