@@ -716,9 +716,47 @@ def main():
     return 0
 
 
+C2D_WORKLOAD = ("plain FIM 2D: 33x33 vertex grid on the unit square, cells split along one diagonal "
+                "(1089 verts, 2048 tris), uniform speed 1, seed at vertex 0, 16 verts/block")
+
+
+def c2d_summary(E):
+    """The reference's small 2D case: device solve time, and the result's error
+    against the FP64 run of the same scheme (same partition) and against the exact
+    Euclidean distance to the seed."""
+    from oracle import oracle as O
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    xyz, faces = mg.grid2d(33)
+    e = E.Eikonal(True)
+    e.set_mesh(xyz, faces)
+    e.maxVertsPerBlock_ = 16
+    e.setSeeds([0])
+    e.keepHistory_ = 0
+    e.solveEikonal()
+    ms = []
+    for _ in range(20):
+        e.solveEikonal()
+        ms.append(e.stats()["solve_ms"])
+    got = e.getFinalResult()
+    lab, nb = e.getPartition()
+    ff, obt, off, vfv = e.triPrep()
+    init = np.full(xyz.shape[0], 1e7, np.float32)
+    init[0] = 0
+    r64 = O.solve2d(xyz, ff, np.ones(ff.shape[0], np.float32), obt, off, vfv, lab, nb, [0], init, precision=64)
+    dist = np.linalg.norm(xyz.astype(np.float64) - xyz[0].astype(np.float64), axis=1)
+    return {"workload": C2D_WORKLOAD, "solve_ms_p50": statistics.median(ms), "iterations": e.numIterations(),
+            "blocks": int(nb), "error_vs_fp64": error_stats(got, r64["result"]),
+            "error_vs_exact_distance": error_stats(got, dist)}
+
+
 def pattern_summaries(args, E, torch, local):
-    """The batched, served and precision workloads, summarised on the same line."""
+    """The batched, served and precision workloads and the small 2D case,
+    summarised on the same line."""
     out = {}
+    try:
+        out["plain_2d"] = c2d_summary(E)
+    except Exception as ex:  # keep the headline line even if a pattern fails
+        out["plain_2d"] = {"error": repr(ex)}
     try:
         b = bench_batch(args, E, torch, 1, local)
         out["batched"] = {"workload": BATCH_WORKLOAD, "solves_per_s": b["value"],
