@@ -306,6 +306,20 @@ def bench_batch(args, E, torch, world, local):
     lat = sorted(times)
     peak, peak_src = measured_hbm_peak()
     achieved = fim_bytes / (fim_ms * 1e-3) / 1e9 if fim_ms > 0 else 0.0
+    # error against the FP64 run of the same scheme (same partition), on instances
+    # spread over the sizes
+    from oracle import oracle as O
+    order = sorted(range(n), key=lambda k: work[k][0].shape[0])
+    err = []
+    for k in sorted({order[0], order[n // 3], order[(2 * n) // 3], order[-1]}):
+        xyz, faces, speed, seeds = work[k]
+        f, obt, off, vfv = solvers[k].triPrep()
+        lab, nb = solvers[k].getPartition()
+        init = np.full(xyz.shape[0], 1e7, np.float32)
+        init[list(seeds)] = 0
+        r64 = O.solve2d(xyz, f, (np.float32(1) / speed).astype(np.float32), obt, off, vfv, lab, nb, list(seeds),
+                        init, max_iters=MAX_ITERS, precision=64)
+        err.append(dict(error_stats(res[k], r64["result"]), vertices=int(xyz.shape[0])))
     return {
         "metric": METRIC, "value": n / (batched_ms * 1e-3), "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms, "higher_is_better": True,
@@ -320,6 +334,7 @@ def bench_batch(args, E, torch, world, local):
                   "e2e_solves_per_s": n / sum(plain_wall) if plain_wall else float("nan")},
         "batched_over_plain": (n / (batched_ms * 1e-3)) / (n / (plain_total_ms * 1e-3)),
         "bitwise_mismatches_vs_plain": mismatch,
+        "error_vs_fp64_sample": err,
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
         "e2e": {"value": n / statistics.median(e2e), "unit": "solves/s",
                 "h2d_bytes_per_step": int(batch.stats()["h2d_bytes"]), "d2h_bytes_per_step": 4 * nv_total},
@@ -764,6 +779,7 @@ def pattern_summaries(args, E, torch, local):
                           "vertex_updates_per_s": b["vertex_updates_per_s"], "ms_per_batch": b["ms_per_step"],
                           "latency_ms": b["latency_ms"], "e2e_solves_per_s": b["e2e"]["value"],
                           "bitwise_mismatches_vs_plain": b["bitwise_mismatches_vs_plain"],
+                          "error_vs_fp64_sample": b["error_vs_fp64_sample"],
                           "verts_per_block": b["config"]["verts_per_block"], "clocks": b["clocks"]}
     except Exception as ex:  # keep the headline line even if a pattern fails
         out["batched"] = {"error": repr(ex)}
