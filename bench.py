@@ -706,7 +706,8 @@ def main():
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                      "kernel": "k_visit3d<false> (block sweeps)",
                      "kernel_ms_per_step": fim_ms / args.steps,
-                     "note": "the sweep kernel is FP32-issue bound (tet local solver), not HBM bound",
+                     "note": "the sweep kernel is bound by CTA barriers and instruction latency in the tet local "
+                             "solver, not by HBM",
                      "issue": issue_roofline("fim3d_visit_c3d.md")},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times)},
