@@ -1514,6 +1514,17 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, vthreads, vsmem));
     if (occ < 1) return "visit kernel cannot be resident (shared memory / registers)";
     P.grid_visit = std::min(occ * nsm, std::max(L.nb, 1));
+    // 3D checks: most slots are settled by the check memo, so a visit is mostly
+    // fixed latency (claim, copies, barriers); CTAs of half the size, two per SM,
+    // overlap two visits (several slots per thread where a block is larger)
+    int cthreads = vthreads, grid_chk = P.grid_visit;
+    if (L.dim == 3 && vthreads >= 1024) {
+      cthreads = vthreads / 2;
+      int occc = 0;
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occc, kv_chk, cthreads, vsmem));
+      if (occc >= 2) grid_chk = std::min(occc * nsm, std::max(L.nb, 1));
+      else cthreads = vthreads;
+    }
     P.grid_aux = nsm * 4;
     // start node
     void* args_ptr[] = {&P.args};
@@ -1545,7 +1556,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
     if (L.dim == 3) {
       if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, grid_chk, cthreads, vsmem, args_ptr)).empty()) return e;
       if (!(e = add((void*)k_close3d, 1, 256, 0, args_ptr)).empty()) return e;
     } else {
       if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
