@@ -206,24 +206,28 @@ struct Smem {
   unsigned char* vchg;  // max_owned
 };
 
-__device__ __forceinline__ Smem carve(unsigned char* sm, const DevArgs& a, int ncoef) {
+// `next` = false (single-sweep check visits): no second set of per-slot copies
+// and masks (h1, m1 alias h0, m0 and are never written)
+__device__ __forceinline__ Smem carve(unsigned char* sm, const DevArgs& a, int ncoef, bool next = true) {
   Smem s;
   const int np = a.max_slots_pad;
   s.coef = reinterpret_cast<float*>(sm);
   s.lv = reinterpret_cast<uint2*>(s.coef + (size_t)ncoef * np);
   s.h0 = reinterpret_cast<float*>(s.lv + np);
-  s.h1 = s.h0 + 4 * (size_t)np;
+  s.h1 = next ? s.h0 + 4 * (size_t)np : s.h0;
   s.m0 = reinterpret_cast<unsigned char*>(s.h1 + 4 * (size_t)np);
-  s.m1 = s.m0 + np;
+  s.m1 = next ? s.m0 + np : s.m0;
   s.vt = reinterpret_cast<float*>(s.m1 + np);
   s.vnew = reinterpret_cast<int*>(s.vt + a.max_local);
   s.vchg = reinterpret_cast<unsigned char*>(s.vnew + a.max_owned);
   return s;
 }
 
-__host__ __device__ inline size_t smem_bytes(int ncoef, int max_slots_pad, int max_local, int max_owned) {
-  size_t n = (size_t)ncoef * max_slots_pad * 4 + (size_t)max_slots_pad * 8 + 2 * 16 * (size_t)max_slots_pad +
-             2 * (size_t)max_slots_pad + 4 * (size_t)max_local + 4 * (size_t)max_owned + (size_t)max_owned;
+__host__ __device__ inline size_t smem_bytes(int ncoef, int max_slots_pad, int max_local, int max_owned,
+                                             bool next = true) {
+  const size_t sets = next ? 2 : 1;
+  size_t n = (size_t)ncoef * max_slots_pad * 4 + (size_t)max_slots_pad * 8 + sets * 16 * (size_t)max_slots_pad +
+             sets * (size_t)max_slots_pad + 4 * (size_t)max_local + 4 * (size_t)max_owned + (size_t)max_owned;
   return (n + 15) & ~(size_t)15;
 }
 
@@ -268,7 +272,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   __shared__ int s_item;
   __shared__ volatile int s_moved;  // check visits: some owned vertex drops by >= EPS
   __shared__ int s_nlist;
-  const Smem s0 = carve(sm, a, 6);
+  const Smem s0 = carve(sm, a, 6, !kCheck);
   // sweep visits: the slots the last sweep must recompute, packed into a list so
   // they fill few warps (the region behind the carve that check visits use for
   // memos; present whenever the check memo is).  Not in the precision kernel: there
@@ -279,7 +283,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
                          : nullptr;
   // check memos of the block's slots, staged behind the visit's carve
   uint4* const smemo = (kCheck && a.chk_memo)
-                           ? reinterpret_cast<uint4*>(sm + smem_bytes(6, a.max_slots_pad, a.max_local, a.max_owned))
+                           ? reinterpret_cast<uint4*>(sm + smem_bytes(6, a.max_slots_pad, a.max_local, a.max_owned, false))
                            : nullptr;
   const int tid = threadIdx.x, NT = blockDim.x;
   const Ctl* ctl = a.ctl;
@@ -1483,33 +1487,39 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     // to the reference); larger 2D blocks fall back to the slot-loop kernel
     const bool slot2d = (L.dim == 2) && P.max_slots_pad <= 1024;
     int vthreads = threads;
-    size_t vsmem = P.smem;
+    size_t vsmem = P.smem, vsmem_chk = P.smem;
     void* kv_fim;
     void* kv_chk;
     if (L.dim == 3) {
       kv_fim = P.prec ? (void*)k_visit3d<false, true> : (void*)k_visit3d<false>;
       kv_chk = P.prec ? (void*)k_visit3d<true, true> : (void*)k_visit3d<true>;
-      // the check kernel stages the block's check memos (16 B per slot) in shared memory
+      // check visits need one set of per-slot copies; they stage the block's check
+      // memos (16 B per slot) behind it, and sweep visits their packed slot list
+      // (4 B per slot) behind theirs
+      const size_t np = (size_t)P.max_slots_pad;
+      vsmem_chk = smem_bytes(6, P.max_slots_pad, P.max_local, P.max_owned, false);
       if (a.chk_memo) {
         int maxsm = 0;
         CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        const size_t with_memo = P.smem + sizeof(uint4) * (size_t)P.max_slots_pad;
-        if (with_memo + 64 <= (size_t)maxsm)
-          vsmem = with_memo;
-        else
+        const size_t fim_list = P.smem + sizeof(int) * np, chk_memo = vsmem_chk + sizeof(uint4) * np;
+        if (std::max(fim_list, chk_memo) + 64 <= (size_t)maxsm) {
+          vsmem = fim_list;
+          vsmem_chk = chk_memo;
+        } else {
           a.chk_memo = nullptr;
+        }
       }
     } else if (slot2d) {
       vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
-      vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
+      vsmem = vsmem_chk = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
       kv_fim = (sweeps == 7) ? (void*)k_visit2d_slot<false, 7> : (void*)k_visit2d_slot<false, 0>;
       kv_chk = (void*)k_visit2d_slot<true, 1>;
     } else {
       kv_fim = (void*)k_visit2d<false>;
       kv_chk = (void*)k_visit2d<true>;
     }
-    for (void* k : {kv_fim, kv_chk})
-      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    CK(cudaFuncSetAttribute(kv_fim, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    CK(cudaFuncSetAttribute(kv_chk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem_chk));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, vthreads, vsmem));
     if (occ < 1) return "visit kernel cannot be resident (shared memory / registers)";
@@ -1521,7 +1531,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     if (L.dim == 3 && vthreads >= 1024) {
       cthreads = vthreads / 2;
       int occc = 0;
-      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occc, kv_chk, cthreads, vsmem));
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occc, kv_chk, cthreads, vsmem_chk));
       if (occc >= 2) grid_chk = std::min(occc * nsm, std::max(L.nb, 1));
       else cthreads = vthreads;
     }
@@ -1556,7 +1566,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
     if (L.dim == 3) {
       if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, grid_chk, cthreads, vsmem, args_ptr)).empty()) return e;
+      if (!(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
       if (!(e = add((void*)k_close3d, 1, 256, 0, args_ptr)).empty()) return e;
     } else {
       if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
