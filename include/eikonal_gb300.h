@@ -53,7 +53,9 @@ typedef struct eik_options {
   int direct_launch;       /* 0 (default): a solve is one CUDA-graph launch; 1: the same kernels
                               launched one by one with a host check per iteration, for profilers
                               that cannot see kernels inside conditional graphs */
-  int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/512/1024); 0 = default */
+  int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/512/1024); 0 = default
+                              (one thread per slot of the largest block; the check kernel then
+                              runs CTAs of half that size at 1024) */
   int precision;           /* 0 (default): the reference's FP32 arithmetic, bit for bit.  1 (3D):
                               tets whose metric edge Gram matrix has condition number above
                               precision_kappa (slivers, strong anisotropy) run their local
