@@ -97,3 +97,28 @@ def test_single_triangle_and_2d_all_seeds(need_gpu, eik, mg):
     e.maxVertsPerBlock_ = 8
     e.solveEikonal()
     assert np.all(e.getFinalResult() == 0.0)
+
+
+def test_2d_blocks_above_1024_slots_use_the_slot_loop_kernel(need_gpu, eik, mg, O):
+    """2D blocks with more element slots than a CTA can hold one per thread run the
+    slot-loop kernel (an extension: the reference keeps 2D blocks at 64 vertices);
+    checked against the CPU restatement of the scheme on the same partition."""
+    xyz, faces = mg.icosphere(5)
+    e = eik.Eikonal(True)
+    e.set_mesh(xyz, faces)
+    e.setSeeds([0, 5000])
+    e.maxVertsPerBlock_ = 700
+    e.keepHistory_ = 0
+    e.solveEikonal()
+    st = e.stats()
+    assert st["max_slots_per_block"] > 1024 and st["device_error"] == 0
+    got = e.getFinalResult()
+    lab, nb = e.getPartition()
+    f, obt, off, vfv = e.triPrep()
+    init = np.full(xyz.shape[0], 1e7, np.float32)
+    init[[0, 5000]] = 0
+    want = O.solve2d(xyz, f, np.ones(f.shape[0], np.float32), obt, off, vfv, lab, nb, [0, 5000], init)["result"]
+    # (the scheme decides a 2D block's convergence on its first 32 vertices, as the
+    # reference does, so blocks this large can stop with vertices unreached; the
+    # restatement does the same)
+    assert np.max(relerr(got, want)) <= 1e-4
