@@ -53,9 +53,11 @@ typedef struct eik_options {
   int direct_launch;       /* 0 (default): a solve is one CUDA-graph launch; 1: the same kernels
                               launched one by one with a host check per iteration, for profilers
                               that cannot see kernels inside conditional graphs */
-  int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/512/1024); 0 = default
-                              (one thread per slot of the largest block; the check kernel then
-                              runs CTAs of half that size at 1024) */
+  int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/512/1024).  0 (default):
+                              chosen per handle over its first solves between one thread per slot
+                              of the largest block and 512 (two CTAs per SM), by measured speed;
+                              results do not depend on it.  The check kernel runs CTAs of half
+                              the size when this is 1024. */
   int precision;           /* 0 (default): the reference's FP32 arithmetic, bit for bit.  1 (3D):
                               tets whose metric edge Gram matrix has condition number above
                               precision_kappa (slivers, strong anisotropy) run their local

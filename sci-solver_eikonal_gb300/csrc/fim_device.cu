@@ -1295,16 +1295,21 @@ __global__ void k_selftest_quot(const float* in, float* out, int n) {
     if (e_ != cudaSuccess) return std::string(#x ": ") + cudaGetErrorString(e_);       \
   } while (0)
 
-// CTA size of the 3D visit kernels when the caller gives none: one thread per
-// element slot of the largest block, at most 512, so that two CTAs (64 registers
-// per thread) share an SM and overlap two block visits; threads of larger blocks
-// loop over several slots.  On the 65^3 workload (blocks of up to ~1000 slots) 512
-// measured 3.5% faster than 1024 and 256 14% slower.
-int auto_visit_threads(int max_slots_pad) {
+// CTA sizes of the 3D visit kernels when the caller gives none.  One thread per
+// element slot of the largest block (up to 1024) runs every slot's updates side by
+// side; 512 threads lets two CTAs (64 registers per thread) share an SM and overlap
+// two block visits, threads of larger blocks taking several slots.  Which is faster
+// depends on the updates' cost: on the isotropic 65^3 workload 512 measured 3.5%
+// faster, on the anisotropic sliver workload 1024 was 10% faster (36% in precision
+// mode, where flagged slots run FP64).  A handle's solves measure both (after one
+// warm-up solve) and keep the faster by sweep-kernel time per slot visit; results
+// do not depend on the CTA size.  The server uses 512.
+int full_visit_threads(int max_slots_pad) {
   int t = 256;
-  while (t < max_slots_pad && t < 512) t *= 2;
+  while (t < max_slots_pad && t < 1024) t *= 2;
   return t;
 }
+int auto_visit_threads(int max_slots_pad) { return std::min(full_visit_threads(max_slots_pad), 512); }
 
 template <typename T>
 std::string dev_alloc(T*& p, size_t n) {
@@ -1363,6 +1368,10 @@ struct DeviceSolve::Impl {
   int* inst_maxit = nullptr;
   int ninst = 1;
   size_t coef_n = 0;
+  // online choice of the 3D visit CTA size (FP32 / precision kernels): candidates
+  // measured so far and their sweep-kernel time per slot visit
+  int tune_n[2] = {0, 0};
+  float tune_cost[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
   uint4* chk_memo = nullptr;  // 3D: coef_n / 6 slots
   // host staging for the initial state
   std::vector<float> h_prev;  // caller's initial values (renumbered), empty when none
@@ -1437,6 +1446,7 @@ struct DeviceSolve::Impl {
     inst_vbeg = nullptr;
     chunks = nullptr;
     chk_memo = nullptr;
+    tune_n[0] = tune_n[1] = 0;
     nchunks = 0;
     prec = false;
     seed_ids = nullptr;
@@ -1817,9 +1827,21 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   const Layout& L = *L_;
   cudaStream_t st = (cudaStream_t)stream_;
   const int sweeps = (opt.fim_sweeps > 0) ? opt.fim_sweeps : (L.dim == 3 ? 2 : 7);
-  const int threads = (opt.threads == 128 || opt.threads == 256 || opt.threads == 512 || opt.threads == 1024)
-                          ? opt.threads
-                          : auto_visit_threads(P.max_slots_pad);
+  const bool given = opt.threads == 128 || opt.threads == 256 || opt.threads == 512 || opt.threads == 1024;
+  int threads = given ? opt.threads : full_visit_threads(P.max_slots_pad);
+  int tune_slot = -1;  // which candidate CTA size this solve measures
+  const int tq = P.prec ? 1 : 0;
+  if (!given && L.dim == 3) {
+    const int full = threads, half = auto_visit_threads(P.max_slots_pad);
+    if (half < full) {
+      if (P.tune_n[tq] < 3) {  // 0: warm-up at 512, 1: measure 512, 2: measure the full size
+        tune_slot = P.tune_n[tq];
+        threads = (tune_slot == 2) ? full : half;
+      } else {
+        threads = (P.tune_cost[tq][0] <= P.tune_cost[tq][1]) ? half : full;
+      }
+    }
+  }
   // per-instance iteration caps (one cap for all when not given)
   std::vector<int> cap(P.ninst, opt.max_iterations);
   if ((int)opt.inst_max_iterations.size() == P.ninst) cap = opt.inst_max_iterations;
@@ -1955,6 +1977,7 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   stats_.fim_slots = (long long)out.fim_slots;
   stats_.fim_halo = (long long)out.fim_halo;
   stats_.fim_owned = (long long)out.fim_owned;
+  const bool measured = tune_slot >= 0 && stats_.error == 0 && stats_.fim_slots > 0;
   {
     std::vector<unsigned long long> kt(4 * (size_t)P.ktime_cap);
     CK(cudaMemcpy(kt.data(), P.ktime, sizeof(unsigned long long) * kt.size(), cudaMemcpyDeviceToHost));
@@ -1965,6 +1988,10 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
       if (kt[4 * i + 3] > kt[4 * i + 2] && kt[4 * i + 2] != ~0ull) { chk += (double)(kt[4 * i + 3] - kt[4 * i + 2]); ++nc; }
     }
     stats_.fim_kernel_ms = (float)(fim * 1e-6);
+    if (measured && fim > 0) {  // sweep-kernel time per slot visit of this CTA size
+      if (tune_slot > 0) P.tune_cost[tq][tune_slot - 1] = (float)(fim / (double)stats_.fim_slots);
+      P.tune_n[tq] = tune_slot + 1;
+    }
     stats_.check_kernel_ms = (float)(chk * 1e-6);
     stats_.fim_launches = nf;
     stats_.check_launches = nc;
