@@ -66,6 +66,7 @@ def parse():
                    help="c3d only: skip the batched / served / precision summaries added to the line")
     p.add_argument("--launch", default="graph", choices=["graph", "direct"],
                    help="graph: one CUDA-graph launch per solve; direct: kernel by kernel (for ncu)")
+    p.add_argument("--prec-modes", default="fp32,mixed", help="prec: which of fp32 / mixed to run")
     return p.parse_args()
 
 
@@ -505,14 +506,16 @@ def bench_prec(args, E, torch):
     seeds = np.random.Generator(np.random.PCG64(9)).choice(xyz.shape[0], 4, replace=False).astype(np.int32)
     gen_s = time.perf_counter() - t0
     runs = {}
-    for name, prec in (("fp32", 0), ("mixed", 1)):
+    modes = [m for m in ("fp32", "mixed") if m in args.prec_modes.split(",")]
+    for name in modes:
         e = E.Eikonal(False)
         e.set_mesh(xyz, tets)
         e.initSpeedMtxMultipliers(M6.ravel())
         e.setSeeds(seeds)
         e.maxIterations_ = 1000
         e.keepHistory_ = 0
-        e.precisionMode_ = prec
+        e.precisionMode_ = 1 if name == "mixed" else 0
+        e.directLaunch_ = 1 if args.launch == "direct" else 0
         e.solveEikonal()
         for _ in range(args.warmup):
             e.solveEikonal()
@@ -522,7 +525,7 @@ def bench_prec(args, E, torch):
             ms.append(e.stats()["solve_ms"])
         st = e.stats()
         runs[name] = {"e": e, "ms": statistics.median(ms), "stats": st, "result": e.getFinalResult()}
-    lab, nb = runs["fp32"]["e"].getPartition()
+    lab, nb = runs[modes[0]]["e"].getPartition()
     # CPU baseline leg: the FP64 run of the same scheme, which is also the error reference
     c64 = cpu_sample(xyz, tets, M6.ravel(), seeds, lab, nb, 1000, precision=64)
     ref = c64["result"]
@@ -536,15 +539,15 @@ def bench_prec(args, E, torch):
            "config": {"workload": PREC_WORKLOAD, "vertices": int(xyz.shape[0]), "tets": int(tets.shape[0]),
                       "sliver_fraction": float(sl.mean()), "mesh_generation_s": round(gen_s, 1),
                       "kappa_threshold": 1e4}}
-    for name in ("fp32", "mixed"):
+    for name in modes:
         r = runs[name]
         st = r["stats"]
         out[name] = {"solve_ms": r["ms"], "iterations": st["iterations"],
                      "vertex_updates_per_s": st["vertex_updates"] / (r["ms"] * 1e-3),
                      "error_vs_fp64": err(r["result"]), "flagged_tets": st["flagged_tets"],
                      "residual_max_rel": st["residual_max_rel"], "residual_vertices": st["residual_vertices"]}
-    out["value"] = out["mixed"]["vertex_updates_per_s"]
-    out["ms_per_step"] = runs["mixed"]["ms"]
+    out["value"] = out[modes[-1]]["vertex_updates_per_s"]
+    out["ms_per_step"] = runs[modes[-1]]["ms"]
     out["fp64_oracle"] = {"seconds": c64["seconds"], "iterations": c64["iterations"], "threads": c64["cores"]}
     out["cpu_baseline"] = {k: c64[k] for k in ("value", "unit", "cores", "kind", "sample")}
     out["e2e"] = None
