@@ -115,6 +115,14 @@ class ClockSampler:
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        # let nvidia-smi finish its start-up (its first query) before the timed
+        # region: a solve that overlapped that start-up once took 60 ms instead of 10
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 1.5 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.05)
 
     def stop(self):
         if self.proc is None:
