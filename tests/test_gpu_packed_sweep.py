@@ -61,3 +61,23 @@ def test_cta_size_does_not_change_results(need_gpu, eik, mg):
         assert bits_equal(out[0].getFinalResult(), e.getFinalResult())
         assert out[0].numIterations() == e.numIterations()
         assert out[0].stats()["check_visits"] == e.stats()["check_visits"]
+
+
+def test_cta_size_choice_over_the_first_solves_keeps_the_bits(need_gpu, eik, mg):
+    """With no CTA size given, a handle's first solves run 512 and one thread per
+    slot to pick the faster; every solve gives the same bits."""
+    xyz, tets = mg.kuhn_cube(25, 0.2, seed=41)
+    sp = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=42)
+    metric = (1.0 / sp.astype(np.float64) ** 2).astype(np.float32)
+    e = eik.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.initSpeedMtxMultipliers(metric)
+    e.setSeeds([3])
+    e.maxVertsPerBlock_ = 64
+    e.keepHistory_ = 0
+    res = []
+    for _ in range(5):
+        e.solveEikonal()
+        res.append((e.getFinalResult().copy(), e.numIterations(), e.stats()["vertex_updates"]))
+    for r, it, upd in res[1:]:
+        assert bits_equal(res[0][0], r) and it == res[0][1] and upd == res[0][2]
