@@ -1834,9 +1834,11 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   if (!given && L.dim == 3) {
     const int full = threads, half = auto_visit_threads(P.max_slots_pad);
     if (half < full) {
-      if (P.tune_n[tq] < 3) {  // 0: warm-up at 512, 1: measure 512, 2: measure the full size
+      if (P.tune_n[tq] < 3) {  // 0: warm-up, 1: measure 512, 2: measure the full size
         tune_slot = P.tune_n[tq];
-        threads = (tune_slot == 2) ? full : half;
+        // the warm-up (often a handle's only solve) runs the size that usually wins:
+        // the full size where FP64 updates make slots long (precision mode)
+        threads = (tune_slot == 2 || (tune_slot == 0 && P.prec)) ? full : half;
       } else {
         threads = (P.tune_cost[tq][0] <= P.tune_cost[tq][1]) ? half : full;
       }
