@@ -159,14 +159,21 @@ def cpu_sample(xyz, tets, metric, seeds, labels, nb, sample_iters, nthreads=0, p
     from oracle import oracle as O  # CPU baseline only
     M = O.metrics_from_speeds(tets.shape[0], metric)
     threads = nthreads or O.num_threads()
+    sd = list(np.atleast_1d(seeds))
+    # the restatement builds its padded block layout on every call (as the
+    # reference's solveEikonal does); the rate counts only the outer iterations, as
+    # the device rate counts only the solve
     t0 = time.perf_counter()
-    r = O.solve3d(xyz, tets, M, labels, nb, list(np.atleast_1d(seeds)), max_iters=sample_iters, nthreads=threads,
-                  precision=precision)
+    r = O.solve3d(xyz, tets, M, labels, nb, sd, max_iters=sample_iters, nthreads=threads, precision=precision)
     dt = time.perf_counter() - t0
-    return {"value": r["vertex_updates"] / dt, "unit": "vertex-updates/s", "cores": threads, "kind": "port",
+    loop = max(O.last_loop_seconds(), 1e-9)
+    setup = dt - loop
+    return {"value": r["vertex_updates"] / loop, "unit": "vertex-updates/s", "cores": threads, "kind": "port",
             "sample": f"first {r['iterations']} outer iterations of the same solve "
-                      f"({r['vertex_updates']} vertex updates in {dt:.1f} s, FP{precision})",
-            "seconds": dt, "iterations": r["iterations"], "result": r["result"]}
+                      f"({r['vertex_updates']} vertex updates in {loop:.2f} s of iterations after "
+                      f"{setup:.2f} s of layout set-up, FP{precision})",
+            "seconds": dt, "loop_seconds": loop, "setup_seconds": setup, "iterations": r["iterations"],
+            "result": r["result"]}
 
 
 def error_stats(got, ref):

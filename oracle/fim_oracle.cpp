@@ -35,6 +35,8 @@
 
 using namespace oracle;
 
+static double g_last_loop_seconds = 0;
+
 extern "C" {
 
 // Local updates, exposed for unit tests (precision 32 or 64).
@@ -64,6 +66,7 @@ int oracle3d_solve(int nv, const float* xyz, int nt, const int* tets, const floa
     o.nv = nv; o.nt = nt; o.nb = nb; o.xyz = xyz; o.tets = tets; o.M = M; o.part = part;
     const int it = o.solve(seeds, nseeds, max_iters, nsweeps, nthreads, out_final, history, hist_cap, updates);
     if (max_tets) *max_tets = o.maxTets;
+    g_last_loop_seconds = o.loopSeconds;
     return it;
   };
   if (precision == 64) { Oracle3D<double> o; return run(o); }
@@ -98,5 +101,9 @@ int oracle2d_solve(int nv, const float* xyz, int nf, const int* faces, const flo
 }
 
 int oracle_num_threads(void) { return n_threads(0); }
+
+// Wall time of the outer iterations of the last oracle3d_solve (its layout set-up
+// excluded), for rates comparable with the device's solve time.
+double oracle_last_loop_seconds(void) { return g_last_loop_seconds; }
 
 }  // extern "C"

@@ -46,6 +46,7 @@ def lib():
                                         ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_int, _FP, _FP, ctypes.c_int, _LP, _IP]
         _lib.oracle_num_threads.restype = ctypes.c_int
+        _lib.oracle_last_loop_seconds.restype = ctypes.c_double
     return _lib
 
 
@@ -134,6 +135,11 @@ def solve2d(xyz, faces, speed_inv, obtuse, vf_off, vf_verts, labels, nblocks, se
 
 def num_threads():
     return lib().oracle_num_threads()
+
+
+def last_loop_seconds():
+    """Wall time of the outer iterations of the last solve3d (layout set-up excluded)."""
+    return lib().oracle_last_loop_seconds()
 
 
 # ---------------------------------------------------------------------------

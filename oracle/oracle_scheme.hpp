@@ -5,6 +5,7 @@
 #pragma once
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -424,6 +425,7 @@ struct Oracle3D {
           dst[inVerts[b][j]] = (float)vertT[(size_t)b * maxInVert + j];
     };
     size_t total = 0;
+    const auto loop0 = std::chrono::steady_clock::now();
     while (!act.empty()) {
       if (++total > (size_t)maxIters) break;
       const int na = (int)act.size();
@@ -462,11 +464,13 @@ struct Oracle3D {
       ++iters;
       if (history && iters <= hist_cap) snapshot(history + (size_t)(iters - 1) * nv);
     }
+    loopSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - loop0).count();
     snapshot(snap.data());
     if (out_final) std::memcpy(out_final, snap.data(), sizeof(float) * nv);
     if (updates) *updates = nupd;
     return iters;
   }
+  double loopSeconds = 0;  // wall time of the outer iterations (after the layout set-up)
 };
 
 // ===========================================================================
