@@ -257,18 +257,43 @@ void fill_stats(eik_stats& s, const SolveStats& st, const Layout& L, float setup
 // The 3D layout built on the device (build_layout3d_device), cached while the mesh
 // and partition inputs are unchanged; a speed change recomputes the metric terms
 // on the device.  The partition itself stays on the host (make_partition).
+// The tet metrics as the device build takes them (tet_metrics' rule without the
+// expansion to 6 entries): the caller's 6 entries or scalars as given, else 1 per
+// tet (identity); *mcomp receives the entries per tet.
+const float* compact_metrics(const eik_solver* h, std::vector<float>& ones, int* mcomp) {
+  if (h->speeds_set && h->speeds.size() == 6 * (size_t)h->ne) {
+    *mcomp = 6;
+    return h->speeds.data();
+  }
+  *mcomp = 1;
+  if (h->speeds_set && h->speeds.size() == (size_t)h->ne) return h->speeds.data();
+  ones.assign((size_t)h->ne, 1.0f);
+  return ones.data();
+}
+
 int device_prepare(eik_solver* h) {
   if (int rc = check_speeds(h)) return rc;
   const std::string key = partition_key(h);
   if (!h->dev) h->dev.reset(new DeviceSolve);
   if (h->dlay_mesh != h->mesh_ver || h->dlay_key != key || !h->dev->layout_built_on_device()) {
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
     int rc = make_partition(h);
     if (rc) return rc;
-    std::vector<float> M;
-    tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), M);
+    const auto t1 = clk::now();
+    std::vector<float> ones;
+    int mcomp = 6;
+    const float* M = compact_metrics(h, ones, &mcomp);
+    const auto t2 = clk::now();
     Built3D b;
-    std::string e = build_layout3d_device(h->nv, h->xyz.data(), h->ne, h->elems.data(), M.data(), h->labels.data(),
+    std::string e = build_layout3d_device(h->nv, h->xyz.data(), h->ne, h->elems.data(), M, mcomp, h->labels.data(),
                                           h->nb, (cudaStream_t)h->dev->stream(), b, h->dlayout);
+    if (h->opt.verbose) {
+      const auto t3 = clk::now();
+      auto ms = [](clk::time_point a, clk::time_point z) { return std::chrono::duration<double, std::milli>(z - a).count(); };
+      std::printf("Eikonal GB300: device setup: partition %.2f ms, metrics %.2f ms, layout build %.2f ms\n",
+                  ms(t0, t1), ms(t1, t2), ms(t2, t3));
+    }
     if (!e.empty()) {
       b.release();
       h->dlay_mesh = ~0u;
@@ -285,9 +310,10 @@ int device_prepare(eik_solver* h) {
     h->dlay_key = key;
     h->dlay_speed = h->speed_ver;
   } else if (h->dlay_speed != h->speed_ver) {
-    std::vector<float> M;
-    tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), M);
-    std::string e = h->dev->refresh_coef_built(M.data());
+    std::vector<float> ones;
+    int mcomp = 6;
+    const float* M = compact_metrics(h, ones, &mcomp);
+    std::string e = h->dev->refresh_coef_built(M, mcomp);
     if (!e.empty()) return fail(h, EIK_ERR_CUDA, e);
     h->dlay_speed = h->speed_ver;
   }

@@ -89,7 +89,8 @@ struct Built3D {
   int* slot_elem = nullptr;
   float* xyz = nullptr;
   int* tets = nullptr;
-  float* M6 = nullptr;
+  float* M6 = nullptr;          // metric per tet: mcomp entries (6: full, 1: scalar times I)
+  int mcomp = 6;
   int total_slots = 0, nhalo = 0, nnbr = 0;
   void release();
 };
@@ -97,7 +98,9 @@ struct Built3D {
 // Builds the 3D layout of build_layout3d on the device (same arrays).  L receives
 // the host-side part: block descriptors, renumbering, statistics (no coefficient,
 // corner-id, halo or neighbour arrays).
-std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M6,
+// M holds mcomp metric entries per tet: 6 (M00 M01 M02 M11 M12 M22) or 1 (a scalar
+// s standing for s*I, which gives the same products as the 6 entries s 0 0 s 0 s).
+std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M, int mcomp,
                                   const int* labels, int nb, cudaStream_t st, Built3D& out, Layout& L);
 
 // Device bytes one instance of this layout occupies (layout arrays + state).
@@ -118,7 +121,7 @@ class DeviceSolve {
   std::string upload_built(const Layout& L, Built3D& b);
   // Device-built layouts: recompute the per-slot coefficients on the device from
   // a new per-tet metric (6 entries per tet, host array).
-  std::string refresh_coef_built(const float* M6);
+  std::string refresh_coef_built(const float* M, int mcomp);
   bool layout_built_on_device() const;
   // Seeds are original vertex ids.  init_vals (2D only, may be null) are the
   // vertex values the reference's all-vertex convergence test starts from.

@@ -1165,7 +1165,7 @@ __device__ __forceinline__ float uMw_rn(const float* u, const float* m, const fl
 
 // `memo` (optional): check memos of the same slots, cleared with the new coefficients
 __global__ void k_admit_coef3d(const BlockDesc* blocks, int nb, float* coef, const int* slot_elem, const float* xyz,
-                               const int* tets, const float* M6, float k, uint4* memo) {
+                               const int* tets, const float* M, int mcomp, float k, uint4* memo) {
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const BlockDesc d = blocks[b];
     for (int j = threadIdx.x; j < d.nslots; j += blockDim.x) {
@@ -1176,7 +1176,12 @@ __global__ void k_admit_coef3d(const BlockDesc* blocks, int nb, float* coef, con
         const int v = tets[4 * (size_t)t + q];
         for (int c = 0; c < 3; ++c) P[q][c] = xyz[3 * (size_t)v + c];
       }
-      for (int q = 0; q < 6; ++q) m[q] = __fmul_rn(M6[6 * (size_t)t + q], k);
+      if (mcomp == 6) {
+        for (int q = 0; q < 6; ++q) m[q] = __fmul_rn(M[6 * (size_t)t + q], k);
+      } else {  // s*I: the entries s 0 0 s 0 s, each times k
+        const float sk = __fmul_rn(M[t], k), zk = __fmul_rn(0.0f, k);
+        m[0] = sk; m[1] = zk; m[2] = zk; m[3] = sk; m[4] = zk; m[5] = sk;
+      }
       float AC[3], AD[3], BC[3], CD[3], BD[3];
       for (int c = 0; c < 3; ++c) {
         AC[c] = __fsub_rn(P[2][c], P[0][c]);
@@ -1399,7 +1404,8 @@ struct DeviceSolve::Impl {
   struct Source {
     float* xyz = nullptr;
     int* tets = nullptr;
-    float* M6 = nullptr;
+    float* M6 = nullptr;  // mcomp metric entries per tet
+    int mcomp = 6;
     float* speed = nullptr;
   };
   std::vector<Source> src;         // per pool mesh
@@ -1683,6 +1689,7 @@ std::string DeviceSolve::upload_built(const Layout& L, Built3D& b) {
   P.src[0].xyz = b.xyz;
   P.src[0].tets = b.tets;
   P.src[0].M6 = b.M6;
+  P.src[0].mcomp = b.mcomp;
   P.coef_n = 6 * (size_t)b.total_slots;
   P.built = true;
   b = Built3D();
@@ -1691,15 +1698,22 @@ std::string DeviceSolve::upload_built(const Layout& L, Built3D& b) {
 
 bool DeviceSolve::layout_built_on_device() const { return p_->built; }
 
-std::string DeviceSolve::refresh_coef_built(const float* M6) {
+std::string DeviceSolve::refresh_coef_built(const float* M, int mcomp) {
   Impl& P = *p_;
   if (!L_ || !P.built || P.src.empty()) return "no device-built layout";
+  if (mcomp != 1 && mcomp != 6) return "metric entries per tet must be 1 or 6";
   const Layout& L = *L_;
   cudaStream_t st = (cudaStream_t)stream_;
-  CK(cudaMemcpyAsync(P.src[0].M6, M6, sizeof(float) * 6 * (size_t)L.ne, cudaMemcpyHostToDevice, st));
-  k_admit_coef3d<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.slot_elem,
-                                                                    P.src[0].xyz, P.src[0].tets, P.src[0].M6, 1.0f,
-                                                                    nullptr);
+  Impl::Source& src = P.src[0];
+  if (src.mcomp != mcomp) {  // the kept metric changes shape
+    CK(cudaStreamSynchronize(st));
+    std::string e = dev_alloc(src.M6, (size_t)mcomp * L.ne);
+    if (!e.empty()) return e;
+    src.mcomp = mcomp;
+  }
+  CK(cudaMemcpyAsync(src.M6, M, sizeof(float) * mcomp * (size_t)L.ne, cudaMemcpyHostToDevice, st));
+  k_admit_coef3d<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.slot_elem, src.xyz,
+                                                                    src.tets, src.M6, src.mcomp, 1.0f, nullptr);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   return "";
@@ -2262,7 +2276,7 @@ std::string DeviceSolve::serve_admit(const std::vector<Admission>& adm) {
     const int g = std::max(1, std::min(nbi, 4096));
     if (L.dim == 3)
       k_admit_coef3d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.xyz, src.tets, src.M6,
-                                        x.coef_scale, P.chk_memo);
+                                        src.mcomp, x.coef_scale, P.chk_memo);
     else
       k_admit_coef2d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.speed, x.coef_scale);
     k_admit_seeds<<<1, 256, 0, st>>>(P.args, i, P.seed_ids + off[q], nsd[q], P.seed_ids + boff[q], nbk[q],

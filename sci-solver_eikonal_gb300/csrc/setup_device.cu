@@ -180,10 +180,20 @@ __device__ __forceinline__ float uMw_host(const float* u, const float* m, const 
   return __fadd_rn(__fadd_rn(__fmul_rn(x, w[0]), __fmul_rn(y, w[1])), __fmul_rn(z, w[2]));
 }
 
+// the six metric entries of tet t from mcomp stored per tet (a scalar s is s*I)
+__device__ __forceinline__ void metric_entries(const float* M, int mcomp, int t, float* m) {
+  if (mcomp == 6) {
+    for (int q = 0; q < 6; ++q) m[q] = M[6 * (size_t)t + q];
+  } else {
+    const float s = M[t];
+    m[0] = s; m[1] = 0.0f; m[2] = 0.0f; m[3] = s; m[4] = 0.0f; m[5] = s;
+  }
+}
+
 // corner local ids and the six metric edge products of every slot
 __global__ void k_slot_fill(const unsigned* key, const int* val, const int* slot_of, int np, const BlockDesc* bd,
                             const int* tets, const int* lab, const int* perm, const int* halo, const float* xyz,
-                            const float* M6, uint16_t* lv, float* coef) {
+                            const float* M, int mcomp, uint16_t* lv, float* coef) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
     const int b = (int)(key[p] >> 1);
     const int t = val[p];
@@ -210,7 +220,7 @@ __global__ void k_slot_fill(const unsigned* key, const int* val, const int* slot
       for (int c = 0; c < 3; ++c) P[k][c] = xyz[3 * (size_t)v + c];
     }
     float m[6];
-    for (int q = 0; q < 6; ++q) m[q] = M6[6 * (size_t)t + q];
+    metric_entries(M, mcomp, t, m);
     float AC[3], AD[3], BC[3], CD[3], BD[3];
     for (int c = 0; c < 3; ++c) {
       AC[c] = __fsub_rn(P[2][c], P[0][c]);
@@ -318,7 +328,7 @@ void Built3D::release() {
   *this = Built3D();
 }
 
-std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M6,
+std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M, int mcomp,
                                   const int* labels, int nb, cudaStream_t st, Built3D& out, Layout& L) {
   struct Range {
     Range() { nvtxRangePushA("eikonal: device setup"); }
@@ -327,19 +337,21 @@ std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* t
   out.release();
   L = Layout();
   if (nv <= 0 || nt <= 0 || nb <= 0) return "empty mesh";
+  if (mcomp != 1 && mcomp != 6) return "metric entries per tet must be 1 or 6";
   for (int v = 0; v < nv; ++v)
     if (labels[v] < 0 || labels[v] >= nb) return "partition label out of range";
   Scratch S;
   std::string e;
   // inputs, kept: a speed change recomputes the metric terms from them
   if (!(e = keep(out.xyz, 3 * (size_t)nv)).empty() || !(e = keep(out.tets, 4 * (size_t)nt)).empty() ||
-      !(e = keep(out.M6, 6 * (size_t)nt)).empty())
+      !(e = keep(out.M6, (size_t)mcomp * nt)).empty())
     return e;
+  out.mcomp = mcomp;
   int* d_lab;
   if (!(e = S.get(d_lab, nv)).empty()) return e;
   CKS(cudaMemcpyAsync(out.xyz, xyz, sizeof(float) * 3 * (size_t)nv, cudaMemcpyHostToDevice, st));
   CKS(cudaMemcpyAsync(out.tets, tets, sizeof(int) * 4 * (size_t)nt, cudaMemcpyHostToDevice, st));
-  CKS(cudaMemcpyAsync(out.M6, M6, sizeof(float) * 6 * (size_t)nt, cudaMemcpyHostToDevice, st));
+  CKS(cudaMemcpyAsync(out.M6, M, sizeof(float) * mcomp * (size_t)nt, cudaMemcpyHostToDevice, st));
   CKS(cudaMemcpyAsync(d_lab, labels, sizeof(int) * nv, cudaMemcpyHostToDevice, st));
 
   // 1. owned-vertex renumbering
@@ -430,7 +442,8 @@ std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* t
 
   // 4. corner local ids and metric edge products
   k_slot_fill<<<grid_for(np), kThreads, 0, st>>>(d_key_s, d_val_s, d_slot_of, np, out.blocks, out.tets, d_lab,
-                                                 out.perm, out.halo, out.xyz, out.M6, out.lv, out.coef);
+                                                 out.perm, out.halo, out.xyz, out.M6, out.mcomp, out.lv,
+                                                 out.coef);
 
   // 5. block-neighbour graph (sorted unique pairs -> CSR)
   int nn = 0;
