@@ -9,6 +9,7 @@
 //   k_activate2d      host activation   src/core2d/cuda/meshFIM2d_eikonal.cu:734-756
 //   k_visit2d<true>   run_check_neighbor CUDA_kernels.cu:415-799                   (1 sweep, writes values)
 //   k_vertex_test2d   all-vertex convergence test, meshFIM2d_eikonal.cu:801-815
+//   k_close3d         end of the 3D host loop iteration, meshFIM3dEikonal.cu:411-417
 //   run_reduction (both dims) is a __syncthreads_and inside the visit kernels.
 //
 // Design (GB300-first, not a translation):
@@ -26,7 +27,11 @@
 //     per-slot storage does, and the per-vertex minimum is a shared-memory atomic.
 //   * Sweeps after the first recompute a slot only when one of its values changed
 //     in the previous sweep; unchanged inputs reproduce the previous candidates
-//     bit for bit, so skipping them cannot change any result.
+//     bit for bit, so skipping them cannot change any result.  The last sweep of a
+//     3D visit runs only slots that can still lower an owned vertex, from a packed
+//     list, and 3D checks skip slots whose inputs an earlier check found settled.
+//   * 3D visit CTAs are 512 threads (two per SM, overlapping two visits) or one
+//     thread per slot, whichever a handle's first solves measure faster.
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
