@@ -58,6 +58,7 @@ class Eikonal {
     precisionMode_ = o.precision;
     precisionKappa_ = o.precision_kappa;
     deviceSetup_ = o.device_setup;
+    partitioner_ = o.partitioner;
     if (eik_create(isTriMesh ? 1 : 0, &h_) != EIK_OK) throw std::runtime_error("eik_create failed");
   }
   virtual ~Eikonal() { eik_destroy(h_); }
@@ -182,6 +183,9 @@ class Eikonal {
   float precisionKappa_;
   // 1: 3D block layouts are built on the GPU; 0: on the host
   int deviceSetup_;
+  // EIK_PARTITION_RCB (default) or EIK_PARTITION_METIS (the reference's partitioner
+  // kind; METIS 5 here, METIS 4 in the reference)
+  int partitioner_;
 
  private:
   // the reference's exit codes for the failures it exits on (src/Eikonal.cu:71-88,
@@ -219,6 +223,7 @@ class Eikonal {
     o.precision = precisionMode_;
     o.precision_kappa = precisionKappa_;
     o.device_setup = deviceSetup_;
+    o.partitioner = partitioner_;
     check(eik_set_options(h_, &o));
   }
   eik_solver* h_ = nullptr;

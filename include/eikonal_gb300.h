@@ -34,6 +34,10 @@ extern "C" {
 
 #define EIK_SPEED_ONE 1 /* the reference's speedType_ ONE (src/core2d/include/TriMesh.h:15-16) */
 
+#define EIK_PARTITION_RCB 0   /* recursive coordinate bisection (default) */
+#define EIK_PARTITION_METIS 1 /* METIS k-way on the vertex graph, as GraphPartition_METIS2
+                                 (meshFIM3dEikonal.cu:153-237, meshFIM2d_eikonal.cu:111-204) */
+
 typedef struct eik_solver eik_solver;
 
 /* Public fields of the reference's Eikonal class (src/Eikonal.h:43-60) with its
@@ -68,6 +72,11 @@ typedef struct eik_options {
                               halo lists, metric edge products, neighbour graph) on the GPU;
                               0: on the host.  Same layout, same results; precision mode,
                               batches and the server use the host build. */
+  int partitioner;         /* EIK_PARTITION_RCB (default) or EIK_PARTITION_METIS: the reference's
+                              partitioner kind, here METIS 5 from the CUDA toolkit where the
+                              reference calls METIS 4 (so labels differ from the reference's);
+                              EIK_ERR_ARG when the library was built without it.  Ignored when
+                              is_structured is set or labels are given (eik_set_partition). */
 } eik_options;
 
 typedef struct eik_stats {

@@ -19,6 +19,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libeikonal_gb300.so")
 
 EIK_OK = 0
+PARTITION_RCB = 0    # recursive coordinate bisection (default)
+PARTITION_METIS = 1  # METIS k-way on the vertex graph (the reference's partitioner kind)
+
 ERRORS = {1: "EIK_ERR_ARG", 2: "EIK_ERR_STATE", 3: "EIK_ERR_MESH", 4: "EIK_ERR_CUDA",
           5: "EIK_ERR_LIMIT", 6: "EIK_ERR_DEVICE", 7: "EIK_ERR_IO", 8: "EIK_ERR_CANCELLED"}
 ONE = 1  # speed type ONE
@@ -35,6 +38,7 @@ class EikOptions(ctypes.Structure):
         ("max_iterations", ctypes.c_int), ("verbose", ctypes.c_int), ("keep_history", ctypes.c_int),
         ("fim_sweeps", ctypes.c_int), ("direct_launch", ctypes.c_int), ("threads_per_block", ctypes.c_int),
         ("precision", ctypes.c_int), ("precision_kappa", ctypes.c_float), ("device_setup", ctypes.c_int),
+        ("partitioner", ctypes.c_int),
     ]
 
 
@@ -194,6 +198,7 @@ class Eikonal:
         "verbose_": "verbose", "keepHistory_": "keep_history", "fimSweeps_": "fim_sweeps",
         "directLaunch_": "direct_launch", "threadsPerBlock_": "threads_per_block",
         "precisionMode_": "precision", "precisionKappa_": "precision_kappa", "deviceSetup_": "device_setup",
+        "partitioner_": "partitioner",
     }
 
     def __init__(self, isTriMesh, fname="../src/test/test_data/sphere_74verts.ply", verbose=False):

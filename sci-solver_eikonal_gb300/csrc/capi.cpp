@@ -70,9 +70,10 @@ int fail(eik_solver* h, int code, const std::string& msg) {
 
 std::string partition_key(const eik_solver* h) {
   char buf[256];
-  std::snprintf(buf, sizeof(buf), "%u|%d|%d|%d|%d,%d,%d|%d,%d,%d", h->part_ver, h->opt.is_structured,
+  std::snprintf(buf, sizeof(buf), "%u|%d|%d|%d|%d,%d,%d|%d,%d,%d|%d", h->part_ver, h->opt.is_structured,
                 h->opt.max_verts_per_block, h->dim, h->opt.square_length, h->opt.square_width, h->opt.square_depth,
-                h->opt.square_block_length, h->opt.square_block_width, h->opt.square_block_depth);
+                h->opt.square_block_length, h->opt.square_block_width, h->opt.square_block_depth,
+                h->opt.partitioner);
   return buf;
 }
 
@@ -85,6 +86,10 @@ int make_partition(eik_solver* h) {
     std::string e = partition_square(h->nv, h->dim, h->opt.square_length, h->opt.square_width, h->opt.square_depth,
                                      h->opt.square_block_length, h->opt.square_block_width,
                                      h->opt.square_block_depth, h->labels, h->nb);
+    if (!e.empty()) return fail(h, EIK_ERR_ARG, e);
+  } else if (h->opt.partitioner == EIK_PARTITION_METIS) {
+    const int want = metis_rule_blocks(h->nv, h->opt.max_verts_per_block, h->dim);
+    std::string e = partition_metis(h->nv, h->ne, h->dim == 3 ? 4 : 3, h->elems.data(), want, h->labels, h->nb);
     if (!e.empty()) return fail(h, EIK_ERR_ARG, e);
   } else {
     h->nb = metis_rule_blocks(h->nv, h->opt.max_verts_per_block, h->dim);
@@ -346,6 +351,7 @@ void eik_default_options(eik_options* o) {
   o->precision = 0;
   o->precision_kappa = 1e4f;
   o->device_setup = DEVICE_SETUP_DEFAULT;
+  o->partitioner = EIK_PARTITION_RCB;
 }
 
 int eik_create(int is_tri_mesh, eik_solver** out) {
@@ -371,6 +377,10 @@ int eik_set_options(eik_solver* h, const eik_options* o) {
   if (o->precision != 0 && o->precision != 1) return fail(h, EIK_ERR_ARG, "precision must be 0 or 1");
   if (!(o->precision_kappa >= 1.0f)) return fail(h, EIK_ERR_ARG, "precision_kappa must be at least 1");
   if (o->device_setup != 0 && o->device_setup != 1) return fail(h, EIK_ERR_ARG, "device_setup must be 0 or 1");
+  if (o->partitioner != EIK_PARTITION_RCB && o->partitioner != EIK_PARTITION_METIS)
+    return fail(h, EIK_ERR_ARG, "partitioner must be EIK_PARTITION_RCB or EIK_PARTITION_METIS");
+  if (o->partitioner == EIK_PARTITION_METIS && !metis_available())
+    return fail(h, EIK_ERR_ARG, "this build has no METIS (libmetis_static.a was not found at build time)");
   h->opt = *o;
   return EIK_OK;
 }

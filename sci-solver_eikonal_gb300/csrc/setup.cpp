@@ -342,6 +342,73 @@ void partition_rcb(int nv, const float* xyz, int nparts, std::vector<int>& label
   rcb(pts.data(), nv, std::max(1, std::min(nparts, nv)), 0, labels.data(), 0);
 }
 
+// METIS 5 (libmetis_static.a of the CUDA toolkit, linked when the build finds it):
+// its two entry points, declared here because the toolkit ships no metis.h.  The
+// library's integer type is 64-bit; the real-valued arguments are passed as null.
+#ifdef EIK_HAVE_METIS
+extern "C" {
+int METIS_PartGraphKway(int64_t* nvtxs, int64_t* ncon, int64_t* xadj, int64_t* adjncy, int64_t* vwgt,
+                        int64_t* vsize, int64_t* adjwgt, int64_t* nparts, void* tpwgts, void* ubvec,
+                        int64_t* options, int64_t* edgecut, int64_t* part);
+}
+bool metis_available() { return true; }
+#else
+bool metis_available() { return false; }
+#endif
+
+std::string partition_metis(int nv, int ne, int nodes_per_elem, const int* elems, int nparts,
+                            std::vector<int>& labels, int& nb) {
+#ifndef EIK_HAVE_METIS
+  (void)nv; (void)ne; (void)nodes_per_elem; (void)elems; (void)nparts; (void)labels; (void)nb;
+  return "this build has no METIS (libmetis_static.a was not found at build time)";
+#else
+  labels.assign(nv, 0);
+  nb = 1;
+  if (nv <= 0) return "";
+  if (nparts <= 1 || nv < 2) return "";
+  // vertex graph: vertices sharing an element are adjacent (CSR, sorted, unique)
+  std::vector<int64_t> deg(nv + 1, 0);
+  for (int e = 0; e < ne; ++e)
+    for (int i = 0; i < nodes_per_elem; ++i) deg[elems[(size_t)e * nodes_per_elem + i] + 1] += nodes_per_elem - 1;
+  for (int v = 0; v < nv; ++v) deg[v + 1] += deg[v];
+  std::vector<int64_t> nbr((size_t)deg[nv]);
+  std::vector<int64_t> fill(deg.begin(), deg.end() - 1);
+  for (int e = 0; e < ne; ++e) {
+    const int* t = elems + (size_t)e * nodes_per_elem;
+    for (int i = 0; i < nodes_per_elem; ++i)
+      for (int j = 0; j < nodes_per_elem; ++j)
+        if (i != j) nbr[(size_t)fill[t[i]]++] = t[j];
+  }
+  std::vector<int64_t> xadj(nv + 1, 0), adj;
+  adj.reserve(nbr.size() / 2);
+  for (int v = 0; v < nv; ++v) {
+    auto b0 = nbr.begin() + deg[v], b1 = nbr.begin() + deg[v + 1];
+    std::sort(b0, b1);
+    b1 = std::unique(b0, b1);
+    for (auto it = b0; it != b1; ++it)
+      if (*it != v) adj.push_back(*it);
+    xadj[v + 1] = (int64_t)adj.size();
+  }
+  int64_t n = nv, ncon = 1, np = std::min(nparts, nv), cut = 0;
+  std::vector<int64_t> part(nv, 0);
+  const int rc = METIS_PartGraphKway(&n, &ncon, xadj.data(), adj.data(), nullptr, nullptr, nullptr, &np, nullptr,
+                                     nullptr, nullptr, &cut, part.data());
+  if (rc != 1) return "METIS_PartGraphKway failed (status " + std::to_string(rc) + ")";
+  // number the non-empty parts 0..nb-1 in order
+  std::vector<int> id((size_t)np, -1);
+  nb = 0;
+  for (int v = 0; v < nv; ++v) {
+    const int64_t q = part[v];
+    if (q < 0 || q >= np) return "METIS returned a part out of range";
+    if (id[(size_t)q] < 0) id[(size_t)q] = 0;
+  }
+  for (int64_t q = 0; q < np; ++q)
+    if (id[(size_t)q] >= 0) id[(size_t)q] = nb++;
+  for (int v = 0; v < nv; ++v) labels[v] = id[(size_t)part[v]];
+  return "";
+#endif
+}
+
 std::string partition_square(int nv, int dim, int L, int W, int D, int bl, int bw, int bd,
                              std::vector<int>& labels, int& nb) {
   if (bl <= 0 || bw <= 0 || (dim == 3 && bd <= 0)) return "block dimensions must be positive";

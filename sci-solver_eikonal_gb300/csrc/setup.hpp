@@ -64,6 +64,14 @@ int metis_rule_blocks(int nv, int max_verts_per_block, int dim);
 // Recursive coordinate bisection into exactly `nparts` parts whose sizes differ by
 // at most one vertex.  Deterministic (ties broken by vertex id).
 void partition_rcb(int nv, const float* xyz, int nparts, std::vector<int>& labels);
+
+// METIS k-way partition of the vertex graph (vertices adjacent when they share an
+// element), the partitioner kind of the reference's GraphPartition_METIS2.  Parts
+// METIS leaves empty are dropped: nb receives the number of non-empty blocks.
+// Returns an error message when the build has no METIS.
+std::string partition_metis(int nv, int ne, int nodes_per_elem, const int* elems, int nparts,
+                            std::vector<int>& labels, int& nb);
+bool metis_available();
 // Structured tiling of a lexicographic grid (dims L x W [x D], tiles l x w [x d]).
 std::string partition_square(int nv, int dim, int L, int W, int D, int bl, int bw, int bd,
                              std::vector<int>& labels, int& nblocks);

@@ -247,3 +247,39 @@ def test_server_rejects_pool_over_budget(eik, mg):
         srv.start()  # fails on the budget before touching a GPU
     assert ei.value.code == 5 and "budget" in str(ei.value)
     srv.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_metis_partition(eik, mg, dim):
+    """partitioner = METIS: k-way on the vertex graph (METIS 5 from the CUDA toolkit,
+    the reference's partitioner kind).  Every vertex labelled, no empty block, about
+    the reference's block count, connected blocks dominate, same labels every time."""
+    if dim == 2:
+        xyz, el = mg.grid2d(33)
+        k = 16
+    else:
+        xyz, el = mg.kuhn_cube(17, 0.2, seed=3)
+        k = 64
+    labs = []
+    for _ in range(2):
+        e = eik.Eikonal(dim == 2)
+        e.set_mesh(xyz, el)
+        e.maxVertsPerBlock_ = k
+        e.partitioner_ = eik.PARTITION_METIS
+        e.prepare()
+        lab, nb = e.getPartition()
+        labs.append(lab.copy())
+        want = xyz.shape[0] // k if dim == 2 else -(-xyz.shape[0] // k)
+        assert 0.9 * want <= nb <= want and nb == e.maxBlocks_
+        sizes = np.bincount(lab, minlength=nb)
+        assert sizes.min() > 0 and lab.min() == 0 and lab.max() == nb - 1
+        assert sizes.max() <= 1.2 * xyz.shape[0] / nb  # METIS keeps parts within its imbalance
+    assert np.array_equal(labs[0], labs[1])
+    # RCB stays the default; an unknown partitioner is rejected
+    assert eik.Eikonal(dim == 2).partitioner_ == eik.PARTITION_RCB
+    e = eik.Eikonal(dim == 2)
+    e.set_mesh(xyz, el)
+    e.partitioner_ = 7
+    with pytest.raises(eik.EikonalError) as ex:
+        e.prepare()
+    assert ex.value.code == 1

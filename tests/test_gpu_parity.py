@@ -408,3 +408,31 @@ def test_2d_grid_against_cpu_oracle_and_distance(need_gpu, eik, O, mg):
     assert relerr(got, r64["result"]).max() < 1e-5
     d = np.linalg.norm(xyz.astype(np.float64), axis=1)
     assert relerr(got, d, 1e-3).max() < 0.05
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_metis_partition_solves_bitwise_like_the_reference_kernels(need_gpu, eik, mg, O, dim):
+    """With partitioner = METIS (the reference's partitioner kind) the solve still
+    equals the reference's kernels on the same labels, bit for bit."""
+    need_ref(O)
+    if dim == 3:
+        xyz, tets, M, seed = cube(mg, 17)
+        e = eik.Eikonal(False)
+        e.set_mesh(xyz, tets)
+        e.initSpeedMtxMultipliers(M)
+        e.setSeeds([seed])
+        e.partitioner_ = eik.PARTITION_METIS
+        e.solveEikonal()
+        lab, nb = e.getPartition()
+        r = O.ref_gpu_solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], M), lab, nb, [seed])
+        assert bits_equal(e.getFinalResult(), r["result"]) and r["iterations"] == e.numIterations()
+    else:
+        xyz, f = mg.icosphere(4)
+        e = eik.Eikonal(True)
+        e.set_mesh(xyz, f)
+        e.setSeeds([0])
+        e.maxVertsPerBlock_ = 32
+        e.partitioner_ = eik.PARTITION_METIS
+        e.solveEikonal()
+        r = _tri_ref(eik, O, e, xyz, None, [0])
+        assert bits_equal(e.getFinalResult(), r["result"]) and r["iterations"] == e.numIterations()
