@@ -783,10 +783,48 @@ def c2d_summary(E):
             "error_vs_exact_distance": error_stats(got, dist)}
 
 
+def metis_summary(E, torch):
+    """The headline workload on a METIS k-way partition (the reference's partitioner
+    kind; the headline uses coordinate bisection): partition time, device solve
+    time, vertex updates, and the error against the FP64 run of the scheme on that
+    partition."""
+    xyz, tets, metric, seed = build_workload()
+    e = E.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.initSpeedMtxMultipliers(metric)
+    e.setSeeds([seed])
+    e.maxVertsPerBlock_ = 64
+    e.maxIterations_ = MAX_ITERS
+    e.keepHistory_ = 0
+    e.partitioner_ = E.PARTITION_METIS
+    t0 = time.perf_counter()
+    e.solveEikonal()  # METIS on the host, layout on the device, first solve
+    first_s = time.perf_counter() - t0
+    for _ in range(3):  # the CTA-size choice
+        e.solveEikonal()
+    ms = []
+    for _ in range(10):
+        e.solveEikonal()
+        ms.append(e.stats()["solve_ms"])
+    st = e.stats()
+    med = statistics.median(ms)
+    lab, nb = e.getPartition()
+    f64 = cpu_sample(xyz, tets, metric, seed, lab, nb, MAX_ITERS, precision=64)
+    return {"partition": "METIS 5 k-way on the vertex graph", "first_solve_s": round(first_s, 2),
+            "solve_ms": med, "solves_per_s": 1e3 / med, "vertex_updates": st["vertex_updates"],
+            "vertex_updates_per_s": st["vertex_updates"] / (med * 1e-3), "iterations": st["iterations"],
+            "mean_slots_per_block": st["mean_slots_per_block"], "mean_halo_per_block": st["mean_halo_per_block"],
+            "error_vs_fp64": error_stats(e.getFinalResult(), f64["result"])}
+
+
 def pattern_summaries(args, E, torch, local):
-    """The batched, served and precision workloads and the small 2D case,
-    summarised on the same line."""
+    """The batched, served and precision workloads, the small 2D case and the
+    headline on a METIS partition, summarised on the same line."""
     out = {}
+    try:
+        out["metis_partition"] = metis_summary(E, torch)
+    except Exception as ex:  # keep the headline line even if a pattern fails
+        out["metis_partition"] = {"error": repr(ex)}
     try:
         out["plain_2d"] = c2d_summary(E)
     except Exception as ex:  # keep the headline line even if a pattern fails
