@@ -663,7 +663,8 @@ def main():
         fim_ms += st["fim_kernel_ms"]
         fim_bytes += algorithmic_bytes(st)
         iters.append(st["iterations"])
-        launches += 1 + 4 * st["iterations"]
+        # start + 4 kernels per iteration, the graph body running 4 iterations a pass
+        launches += 1 + 4 * 4 * ((st["iterations"] + 3) // 4)
     barrier()
     clocks = sampler.stop()
     total_ms, upd_all = aggregate_replicas(torch, sum(times), upd, world, "cuda")

@@ -123,6 +123,7 @@ struct DevArgs {
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
 constexpr float kEps2D = 1e-5f;
+constexpr int kBodyCopies3D = 4;  // 3D iterations per pass of the graph's loop body
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + 1D bulk copy (TMA engine)
@@ -1008,8 +1009,13 @@ __global__ void k_vertex_test2d(DevArgs a) {
   if (last_cta(&a.ctl->done_d)) finish_iteration_cta(a, true);
 }
 
-// 3D close: a tiny single-CTA kernel after the check visits.
-__global__ void k_close3d(DevArgs a) { finish_iteration_cta(a, false); }
+// 3D close: a tiny single-CTA kernel after the check visits.  The graph body holds
+// several copies of the iteration; the close of a later copy finds the loop already
+// stopped when an earlier copy ended it, and leaves the state alone.
+__global__ void k_close3d(DevArgs a, int copy) {
+  if (copy > 0 && a.ctl->stop) return;
+  finish_iteration_cta(a, false);
+}
 
 // start of a solve: set the while-condition from the initial active list
 // initial travel times: LARGENUM everywhere (prev too unless the caller's initial
@@ -1584,8 +1590,9 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     cudaGraphNode_t prevn = nullptr, n;
     P.body.clear();
+    bool record = true;  // the direct-launch loop replays the body's first copy
     auto add = [&](void* f, int grid, int block, size_t sm, void** params) -> std::string {
-      P.body.push_back(Impl::Launch{f, grid, block, sm, (f == (void*)k_snapshot) ? L.dim : 0});
+      if (record) P.body.push_back(Impl::Launch{f, grid, block, sm, (f == (void*)k_snapshot) ? L.dim : 0});
       cudaKernelNodeParams q{};
       q.func = f; q.gridDim = dim3(grid); q.blockDim = dim3(block); q.sharedMemBytes = (unsigned)sm;
       q.kernelParams = params;
@@ -1596,18 +1603,30 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     static int dim3v = 3, dim2v = 2;
     void* snap_args[] = {&P.args, (L.dim == 3) ? (void*)&dim3v : (void*)&dim2v};
     std::string e;
-    if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-    if (L.dim == 3) {
-      if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
-      if (!(e = add((void*)k_close3d, 1, 256, 0, args_ptr)).empty()) return e;
-    } else {
-      if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-      if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-      if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+    // 3D solves: the body holds kBodyCopies3D iterations, so the loop's condition
+    // node (which costs about as much as a kernel launch) runs once per that many
+    // iterations.  Copies after the loop stopped find nothing to do: their lists are
+    // empty or hold only finished instances' blocks, which every kernel skips, and
+    // their close leaves the state alone.
+    static int copy_idx[kBodyCopies3D];
+    const int copies = (L.dim == 3 && !serve) ? kBodyCopies3D : 1;
+    for (int u = 0; u < copies; ++u) {
+      record = (u == 0);
+      copy_idx[u] = u;
+      void* close_args[] = {&P.args, &copy_idx[u]};
+      if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
+      if (L.dim == 3) {
+        if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+        if (!(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
+        if (!(e = add((void*)k_close3d, 1, 256, 0, close_args)).empty()) return e;
+      } else {
+        if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+        if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
+        if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+      }
+      if (want_hist)
+        if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
     }
-    if (want_hist)
-      if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
     CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
     P.g_sweeps = sweeps;
     P.g_threads = threads;
