@@ -360,7 +360,8 @@ def bench_batch(args, E, torch, world, local):
                      "kernel_ms_per_step": fim_ms / args.steps,
                      "issue": issue_roofline("fim2d_slot_batch.md")},
         "clocks": clocks,
-        "gpu_launches": int(1 + 4 * sum(iters)),
+        # start + 4 kernels per iteration, the graph body running 4 iterations a pass
+        "gpu_launches": int(sum(1 + 4 * 4 * ((i + 3) // 4) for i in iters)),
     }
 
 

@@ -123,7 +123,7 @@ struct DevArgs {
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
 constexpr float kEps2D = 1e-5f;
-constexpr int kBodyCopies3D = 4;  // 3D iterations per pass of the graph's loop body
+constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + 1D bulk copy (TMA engine)
@@ -972,7 +972,9 @@ __device__ __forceinline__ bool last_cta(int* counter) {
 // 2D all-vertex convergence test (meshFIM2d_eikonal.cu:804-815) + iteration close
 constexpr int kVertexChunk = 2048;  // vertices per chunk of the 2D all-vertex test
 
-__global__ void k_vertex_test2d(DevArgs a) {
+__global__ void k_vertex_test2d(DevArgs a, int copy) {
+  // a later copy of the iteration in the graph body, after the loop stopped
+  if (copy > 0 && a.ctl->stop) return;
   // chunks of the running instances only (a server's idle slots and finished
   // batch members cost one flag read per chunk)
   for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
@@ -1011,7 +1013,8 @@ __global__ void k_vertex_test2d(DevArgs a) {
 
 // 3D close: a tiny single-CTA kernel after the check visits.  The graph body holds
 // several copies of the iteration; the close of a later copy finds the loop already
-// stopped when an earlier copy ended it, and leaves the state alone.
+// stopped when an earlier copy ended it, and leaves the state alone.  (A copy's close
+// returns only after an earlier copy of the same pass set the loop's condition to 0.)
 __global__ void k_close3d(DevArgs a, int copy) {
   if (copy > 0 && a.ctl->stop) return;
   finish_iteration_cta(a, false);
@@ -1603,13 +1606,14 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     static int dim3v = 3, dim2v = 2;
     void* snap_args[] = {&P.args, (L.dim == 3) ? (void*)&dim3v : (void*)&dim2v};
     std::string e;
-    // 3D solves: the body holds kBodyCopies3D iterations, so the loop's condition
-    // node (which costs about as much as a kernel launch) runs once per that many
-    // iterations.  Copies after the loop stopped find nothing to do: their lists are
-    // empty or hold only finished instances' blocks, which every kernel skips, and
-    // their close leaves the state alone.
-    static int copy_idx[kBodyCopies3D];
-    const int copies = (L.dim == 3 && !serve) ? kBodyCopies3D : 1;
+    // Solves and batches: the body holds kBodyCopies iterations, so the loop's
+    // condition node (which costs about as much as a kernel launch) runs once per
+    // that many iterations.  Copies after the loop stopped find nothing to do: their
+    // lists are empty or hold only finished instances' blocks, which every kernel
+    // skips, and their close (3D) or vertex test (2D) returns at once.  The server
+    // keeps one copy: it admits requests between passes.
+    static int copy_idx[kBodyCopies];
+    const int copies = serve ? 1 : kBodyCopies;
     for (int u = 0; u < copies; ++u) {
       record = (u == 0);
       copy_idx[u] = u;
@@ -1622,7 +1626,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
       } else {
         if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
         if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-        if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+        if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, close_args)).empty()) return e;
       }
       if (want_hist)
         if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
