@@ -311,6 +311,37 @@ def test_direct_launch_matches_graph_launch(need_gpu, eik, mg):
     assert res[0][0] == res[1][0] and bits_equal(res[0][1], res[1][1])
 
 
+@pytest.mark.parametrize("dim", [3, 2])
+def test_loop_body_copies_stop_where_the_direct_loop_stops(need_gpu, eik, mg, dim):
+    """The graph's loop body runs four outer iterations a pass; the kernel-by-kernel
+    loop checks the stop flag after each one.  Iteration caps at every position
+    within a pass, and the uncapped solve, give the same iterations, updates and bits
+    in both."""
+    if dim == 3:
+        xyz, elems, sp, seed = cube(mg, 17)
+        speed, seeds = sp, [seed]
+    else:
+        xyz, elems = mg.icosphere(4)
+        speed, seeds = mg.batch_speed(xyz, elems), [0]
+    for cap in (1, 2, 3, 4, 5, 6, 7, 1000):
+        res = []
+        for direct in (0, 1):
+            e = eik.Eikonal(dim == 2)
+            e.set_mesh(xyz, elems)
+            e.initSpeedMtxMultipliers(speed)
+            e.setSeeds(seeds)
+            e.maxVertsPerBlock_ = 32
+            e.maxIterations_ = cap
+            e.directLaunch_ = direct
+            e.solveEikonal()
+            res.append(e)
+        g, d = res
+        assert g.numIterations() == d.numIterations() == min(cap, d.numIterations())
+        assert g.stats()["vertex_updates"] == d.stats()["vertex_updates"]
+        assert bits_equal(g.getFinalResult(), d.getFinalResult())
+    assert d.numIterations() > 4  # the uncapped solve ends on its own, after the first pass
+
+
 def test_write_vtk(need_gpu, eik, golden, tmp_path):
     e = eik.Eikonal(False)
     e.set_mesh(golden["sphere334_xyz"], golden["sphere334_tets"])
