@@ -1612,11 +1612,11 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     // lists are empty or hold only finished instances' blocks, which every kernel
     // skips, and their close (3D) or vertex test (2D) returns at once.  The server
     // keeps one copy: it admits requests between passes.
-    static int copy_idx[kBodyCopies];
+    static int copy_idx[kBodyCopies] = {0, 1, 2, 3};  // read-only kernel arguments
+    static_assert(kBodyCopies == 4, "copy_idx lists every copy");
     const int copies = serve ? 1 : kBodyCopies;
     for (int u = 0; u < copies; ++u) {
       record = (u == 0);
-      copy_idx[u] = u;
       void* close_args[] = {&P.args, &copy_idx[u]};
       if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
       if (L.dim == 3) {
