@@ -16,7 +16,8 @@
 //   * One CTA visits one block at a time and pulls blocks from a device work
 //     counter; grids are sized by occupancy x 152 SMs and stay fixed so the whole
 //     iteration is a CUDA-graph body.  A conditional while-node repeats the body
-//     until no block is active: no host round trip per iteration.
+//     (four iterations a pass outside the server) until no block is active: no
+//     host round trip per iteration.
 //   * A block's metric terms and corner ids are contiguous in HBM (block-major
 //     slots, SoA coefficient runs, 16-byte aligned) and arrive in shared memory by
 //     two cp.async.bulk copies completing on an mbarrier, while the threads gather
@@ -1451,7 +1452,7 @@ struct DeviceSolve::Impl {
     size_t smem;
     int extra;  // second kernel argument (k_snapshot's dimension), unused otherwise
   };
-  std::vector<Launch> body;  // the loop body, in graph order
+  std::vector<Launch> body;  // one iteration of the loop body, in graph order
 
   void free_all() {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
