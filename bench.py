@@ -18,10 +18,16 @@ solve (seed -> every block converged).
   cpu_baseline  the CPU restatement of the reference scheme (oracle/) with all
          host threads on a bounded sample of the same solve
 
+  reference_gpu  the reference's own kernels (built from its sources into
+         oracle/_ref/ref3d.cubin) under a restatement of its host loop, on the same
+         mesh and partition: the outer loop's wall time and rate
+
 --impl reference times that CPU restatement alone (the reference has no CPU
-driver of its own, and its CUDA build needs METIS 4 and cusp).  With N > 1 ranks every rank runs its own
-replica (no collective in the solve path); value sums all ranks' updates over
-the slowest rank's time.
+driver of its own, and its CUDA build needs METIS 4 and cusp), with the
+partition from the oracle's restatement of the default bisection: that arm loads
+no product code.  With N > 1 ranks every rank runs its own replica (no
+collective in the solve path); value sums all ranks' updates over the slowest
+rank's time.
 """
 import argparse
 import importlib
@@ -43,6 +49,7 @@ WORKLOAD = ("plain FIM 3D at scale: 65^3 jittered Kuhn cube (274,625 verts, 1,57
             "log-uniform per-tet speed [0.5, 2] as metric 1/v^2, seed at the centre vertex, 64 verts/block")
 N_GRID = 65
 MAX_ITERS = 100  # the reference default (src/Eikonal.cu:19); the workload converges in 81
+DRAM_PROFILE = "fim3d_visit_dram_c3d.txt"  # per-launch DRAM bytes of the visit kernels over one solve
 
 
 def parse():
@@ -53,6 +60,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-sample-iters", type=int, default=0, help="0 = choose automatically")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-reference-gpu", action="store_true",
+                   help="skip the reference kernels' solve of the headline workload (reference_gpu)")
     p.add_argument("--workload", default="c3d", choices=["c3d", "batch", "serve", "prec"],
                    help="c3d: the 65^3 tet solve (headline); batch: 256 icospheres, batched vs plain; "
                         "serve: Poisson request stream over a resident mesh pool; "
@@ -77,21 +86,35 @@ def dist_env():
     return rank, world, local
 
 
+def load_meshgen():
+    """The synthetic-mesh module, loaded from its file so that importing it does not
+    import the product package (the reference arm must not load product code)."""
+    import importlib.util
+    name = "eikonal_bench_meshgen"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, "sci-solver_eikonal_gb300", "meshgen.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def bench_config(world):
+    """`config` of the headline line, the same dict on both arms."""
+    return {"workload": WORKLOAD, "partition": "recursive coordinate bisection", "verts_per_block": 64,
+            "max_iterations": MAX_ITERS, "parallelism": f"replicas x{world}",
+            "l2": "GPU arm: flushed before every timed solve (512 MB write, outside the timed events); "
+                  "CPU arm: the padded block layout (about 170 MB of slot data) exceeds the host caches"}
+
+
 def build_workload():
-    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    mg = load_meshgen()
     xyz, tets = mg.kuhn_cube(N_GRID, 0.2, seed=1)
     speed = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=2)
     metric = (1.0 / (speed.astype(np.float64) ** 2)).astype(np.float32)
     seed = mg.center_vertex(N_GRID)
     return xyz, tets, metric, seed
-
-
-def algorithmic_bytes(st):
-    """Bytes the block-sweep kernel must move: per visited slot 6 float metric terms +
-    4 u16 corner ids (32 B), owned + halo travel times read (4 B each), owned times
-    written (4 B), one block flag (4 B)."""
-    return (32 * st["fim_slots"] + 4 * (st["fim_owned"] + st["fim_halo"]) + 4 * st["fim_owned"]
-            + 4 * st["fim_visits"])
 
 
 class ClockSampler:
@@ -187,11 +210,11 @@ def error_stats(got, ref):
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    E = importlib.import_module("sci-solver_eikonal_gb300")
     xyz, tets, metric, seed = build_workload()
-    # the same partition as the product's arm (recursive coordinate bisection)
-    labels, nb = partition_host(E, xyz, tets, metric)
+    # the same partition as the product's arm (recursive coordinate bisection),
+    # from the oracle's restatement of it
     from oracle import oracle as O
+    labels, nb = O.partition_rcb(xyz, 64, 3)
     sample_iters = args.cpu_sample_iters or MAX_ITERS
     vals = []
     for i in range(args.warmup + args.steps):
@@ -203,8 +226,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "vertex-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "partition": f"recursive coordinate bisection, {nb} blocks",
-                       "step": vals[0]["sample"]},
+            "config": bench_config(world), "blocks": nb, "step": vals[0]["sample"],
             "cpu_baseline": {"value": v, "unit": "vertex-updates/s", "cores": vals[0]["cores"], "kind": "port",
                              "sample": vals[0]["sample"]},
             "e2e": {"value": v, "unit": "vertex-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -223,16 +245,6 @@ def aggregate_replicas(torch, total_ms, updates, world, device):
     sm = tt.clone()
     torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
     return float(mx[0]), float(sm[1])
-
-
-def partition_host(E, xyz, tets, metric):
-    """Labels from the product's partitioner (host-only call, no GPU work)."""
-    e = E.Eikonal(False)
-    e.set_mesh(xyz, tets)
-    e.initSpeedMtxMultipliers(metric)
-    e.maxVertsPerBlock_ = 64
-    e.prepare()
-    return e.getPartition()
 
 
 BATCH_WORKLOAD = ("batching: 256 unit icospheres, subdivision level U{2..6} (162-40,962 verts; seed 3), "
@@ -355,10 +367,9 @@ def bench_batch(args, E, torch, world, local):
         "e2e": {"value": n / statistics.median(e2e), "unit": "solves/s",
                 "h2d_bytes_per_step": int(batch.stats()["h2d_bytes"]), "d2h_bytes_per_step": 4 * nv_total},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": profile_traffic("fim2d_slot_batch.md"), "peak_source": peak_src,
+                     "traffic": None, "peak_source": peak_src,
                      "kernel": "k_visit2d_slot<false,7> (block sweeps)",
-                     "kernel_ms_per_step": fim_ms / args.steps,
-                     "issue": issue_roofline("fim2d_slot_batch.md")},
+                     "kernel_ms_per_step": fim_ms / args.steps},
         "clocks": clocks,
         # start + 4 kernels per iteration, the graph body running 4 iterations a pass
         "gpu_launches": int(sum(1 + 4 * 4 * ((i + 3) // 4) for i in iters)),
@@ -372,27 +383,54 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def profile_value(name, key):
-    """A `key: value` figure of a committed ncu summary (None when absent)."""
+def launch_dram(name):
+    """DRAM bytes (read + write) per launch of the sweep and check kernels over one
+    solve, by outer iteration, from a committed ncu summary (data lines
+    `iteration sweep_bytes check_bytes`); None when the summary is absent."""
     path = os.path.join(ROOT, "profiles", name)
-    if os.path.exists(path):
-        for line in open(path):
-            if line.startswith(key + ":"):
-                return float(line.split(":")[1])
-    return None
+    if not os.path.exists(path):
+        return None
+    rows = {}
+    for line in open(path):
+        f = line.split()
+        if len(f) >= 3 and f[0].isdigit():
+            rows[int(f[0])] = (float(f[1]), float(f[2]))
+    return rows or None
 
 
-def profile_traffic(name):
-    """DRAM bytes per launch of a kernel, from its committed ncu summary."""
-    return profile_value(name, "traffic_bytes_per_launch")
+def sweep_bytes(it):
+    """Algorithmic bytes of one sweep-kernel launch from its iteration's counters
+    (Eikonal.iterationStats columns): per slot 6 float metric terms + 4 u16 corner
+    ids (32 B), owned + halo travel times read (4 B each), owned times written (4 B),
+    one block flag (4 B) per visit."""
+    return 32 * it[3] + 4 * (it[5] + it[4]) + 4 * it[5] + 4 * it[2]
 
 
-def issue_roofline(name):
-    """The sweep kernels are bound by instruction issue, not HBM: the issue-slot
-    utilisation ncu measured for the kernel (from its committed summary)."""
-    v = profile_value(name, "issue_active_pct")
-    return None if v is None else {"issue_active_frac_of_peak": v / 100.0,
-                                   "source": f"ncu --set full capture in profiles/{name}"}
+def check_bytes(it):
+    """Algorithmic bytes of one check-kernel launch: per slot the metric terms and
+    ids (32 B) and its check memo (16 B), owned + halo times read, one list entry."""
+    return 48 * it[7] + 4 * (it[9] + it[8]) + 4 * it[6]
+
+
+def traffic_vs_algorithmic(its, profile):
+    """Mean DRAM bytes per launch from the capture beside the mean algorithmic bytes
+    of the same launches (same iterations of the same deterministic solve) in this
+    run, for the sweep and the check kernel."""
+    rows = launch_dram(profile)
+    out = {}
+    for k, (col, fn, name) in enumerate(((0, sweep_bytes, "sweep"), (1, check_bytes, "check"))):
+        alg = [fn(its[i]) for i in range(len(its))]
+        if rows:
+            common = [i for i in sorted(rows) if i < len(its) and rows[i][col] > 0]
+            if common:
+                dram = sum(rows[i][col] for i in common) / len(common)
+                a = sum(alg[i] for i in common) / len(common)
+                out[name] = {"traffic": dram, "algorithmic": a, "traffic_over_algorithmic": dram / a if a else None,
+                             "launches": len(common)}
+                continue
+        out[name] = {"traffic": None, "algorithmic": sum(alg) / max(1, sum(1 for x in alg if x > 0)),
+                     "traffic_over_algorithmic": None, "launches": 0}
+    return out
 
 
 SERVE_WORKLOAD = ("serving: resident pool of icospheres L5, L6, L7 and L6 with other speeds (2D) and jittered "
@@ -647,7 +685,7 @@ def main():
         e.solveEikonal()
     sampler = ClockSampler(local)
     sampler.start()
-    times, upd, fim_ms, fim_bytes, iters, launches = [], 0, 0.0, 0, [], 0
+    times, upd, fim_ms, chk_ms, fim_bytes, iters, launches = [], 0, 0.0, 0.0, 0, [], 0
     barrier()
     for _ in range(args.steps):
         flush.zero_()
@@ -662,7 +700,9 @@ def main():
         st = e.stats()
         upd += st["vertex_updates"]
         fim_ms += st["fim_kernel_ms"]
-        fim_bytes += algorithmic_bytes(st)
+        chk_ms += st["check_kernel_ms"]
+        its = e.iterationStats()
+        fim_bytes += sum(sweep_bytes(it) for it in its)
         iters.append(st["iterations"])
         # start + 4 kernels per iteration, the graph body running 4 iterations a pass
         launches += 1 + 4 * 4 * ((st["iterations"] + 3) // 4)
@@ -688,7 +728,8 @@ def main():
     st = e.stats()
     e2e_value = st["vertex_updates"] * len(e2e_times) / sum(e2e_times)
     h2d = st["h2d_bytes"] + seeds.nbytes
-    d2h = 4 * nv + 8 * 4 * (MAX_ITERS + 1) + 256
+    # results, the per-iteration telemetry (12 words per iteration) and the control block
+    d2h = 4 * nv + 8 * 12 * (MAX_ITERS + 1) + 256
 
     if rank != 0:
         return 0
@@ -699,22 +740,15 @@ def main():
     else:
         peak, peak_src = 6800.0, "fallback"
     achieved = fim_bytes / (fim_ms * 1e-3) / 1e9 if fim_ms > 0 else 0.0
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "fim3d_visit_c3d.md")
-    if os.path.exists(prof):
-        for line in open(prof):
-            if line.startswith("traffic_bytes_per_launch:"):
-                traffic = float(line.split(":")[1])
+    tva = traffic_vs_algorithmic(its, DRAM_PROFILE)
     lat = sorted(times)
     res = {
         "metric": METRIC, "value": value, "unit": "vertex-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "blocks": st0["num_blocks"], "iterations_per_solve": iters[0],
-                   "vertex_updates_per_solve": upd // args.steps, "max_iterations": MAX_ITERS,
-                   "l2": "flushed before every timed solve (512 MB write, outside the timed events)",
-                   "partition": "recursive coordinate bisection", "parallelism": f"replicas x{world}",
-                   "launch": args.launch},
+        "config": bench_config(world),
+        "blocks": st0["num_blocks"], "iterations_per_solve": iters[0], "vertex_updates_per_solve": upd // args.steps,
+        "launch": args.launch,
         "solves_per_s": world * args.steps / (total_ms * 1e-3),
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
         "setup_s": setup_s,
@@ -723,14 +757,24 @@ def main():
                           "note": "first solve of this mesh (partition, layout, upload, graph, solve) in a "
                                   "process whose kernels are loaded"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                     "frac": achieved / peak, "traffic": tva["sweep"]["traffic"], "peak_source": peak_src,
                      "kernel": "k_visit3d<false> (block sweeps)",
                      "kernel_ms_per_step": fim_ms / args.steps,
+                     "algorithmic_bytes_per_launch": tva["sweep"]["algorithmic"],
+                     "traffic_over_algorithmic": tva["sweep"]["traffic_over_algorithmic"],
+                     "check_kernel": dict(tva["check"], kernel_ms_per_step=chk_ms / args.steps),
+                     "traffic_source": f"profiles/{DRAM_PROFILE}: ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                                       "of every sweep and check launch of one solve of this workload (kernel by "
+                                       "kernel; cold caches), set beside this run's algorithmic bytes of the same "
+                                       "iterations",
                      "note": "the sweep kernel is bound by CTA barriers and instruction latency in the tet local "
-                             "solver, not by HBM",
-                     "issue": issue_roofline("fim3d_visit_c3d.md")},
+                             "solver, not by HBM"},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times)},
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times),
+                "note": "each step re-solves the resident mesh through the C ABI: seeds copied in, the solve, the "
+                        "travel times copied out; the partition and block layout built by the first solve "
+                        "(first_solve_s) are kept, whereas the reference's solveEikonal rebuilds them on every "
+                        "call"},
         "clocks": clocks,
         "gpu_launches": launches,
     }
@@ -746,10 +790,36 @@ def main():
         f64 = cpu_sample(xyz, tets, metric, seed, labels, nb, MAX_ITERS, precision=64)
         res["error_vs_fp64"] = error_stats(out, f64["result"])
         res["error_vs_fp64"]["fp64_run_s"] = round(f64["seconds"], 2)
+    if world == 1 and not args.no_reference_gpu:
+        labels, nb = e.getPartition()
+        res["reference_gpu"] = reference_gpu_summary(xyz, tets, metric, seed, labels, nb, out)
     if world == 1 and not args.no_patterns:
         res.update(pattern_summaries(args, E, torch, local))
     print(json.dumps(res), flush=True)
     return 0
+
+
+def reference_gpu_summary(xyz, tets, metric, seed, labels, nb, ours):
+    """The reference's own kernels (FIMCuda, CopyOutBack, run_check_neghbor,
+    run_reduction built from its sources) under a restatement of its host loop
+    (meshFIM3dEikonal.cu:411-542) on the same mesh, metric, seed and partition: one
+    solve, its outer loop timed on the host clock (kernels plus the reference's
+    per-iteration host round trips; the padded layout set-up timed apart)."""
+    from oracle import oracle as O  # reference baseline only
+    if O.ref_gpu() is None:
+        return {"unavailable": "the reference's kernels were not built (oracle/_ref/ref3d.cubin)"}
+    M = O.metrics_from_speeds(tets.shape[0], metric)
+    t0 = time.perf_counter()
+    r = O.ref_gpu_solve3d(xyz, tets, M, labels, nb, [seed], max_iters=MAX_ITERS)
+    total = time.perf_counter() - t0
+    loop_s = r["loop_ms"] * 1e-3
+    return {"ms_per_solve": r["loop_ms"], "solves_per_s": 1.0 / loop_s,
+            "vertex_updates_per_s": r["vertex_updates"] / loop_s, "vertex_updates": r["vertex_updates"],
+            "iterations": r["iterations"], "layout_setup_s": round(total - loop_s, 3),
+            "bitwise_equal_to_ours": bool(np.array_equal(np.asarray(r["result"]).view(np.uint32),
+                                                         np.asarray(ours, np.float32).view(np.uint32))),
+            "what": "the reference's CUDA kernels compiled from its sources for sm_103a, one CUDA block per active "
+                    "mesh block with one thread per element slot, host round trips every iteration"}
 
 
 C2D_WORKLOAD = ("plain FIM 2D: 33x33 vertex grid on the unit square, cells split along one diagonal "

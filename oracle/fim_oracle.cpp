@@ -100,6 +100,56 @@ int oracle2d_solve(int nv, const float* xyz, int nf, const int* faces, const flo
   return run(o);
 }
 
+// Recursive coordinate bisection, restated so the CPU baseline and the reference
+// arm of the benchmark run on the product's default partition without loading the
+// product.  The reference partitions with METIS (meshFIM3dEikonal.cu:153-237); the
+// product's default is this bisection: split the longest bounding-box axis of the
+// point set so the lower part gets floor(n * floor(k/2) / k) points, points ordered
+// by (coordinate, vertex id), parts [first, first + floor(k/2)) below and the rest
+// above.  Same labels as the product's partitioner (a test holds them equal); this
+// version sorts each level instead of selecting, and runs on one thread.
+static void rcb_split(std::vector<int>& ids, size_t lo, size_t hi, int nparts, int first, const float* xyz,
+                      int* labels) {
+  const size_t n = hi - lo;
+  if (nparts <= 1 || n <= 1) {
+    for (size_t i = lo; i < hi; ++i) labels[ids[i]] = first;
+    return;
+  }
+  float mn[3], mx[3];
+  for (int d = 0; d < 3; ++d) mn[d] = mx[d] = xyz[3 * (size_t)ids[lo] + d];
+  for (size_t i = lo + 1; i < hi; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const float c = xyz[3 * (size_t)ids[i] + d];
+      mn[d] = std::min(mn[d], c);
+      mx[d] = std::max(mx[d], c);
+    }
+  int ax = 0;
+  for (int d = 1; d < 3; ++d)
+    if (mx[d] - mn[d] > mx[ax] - mn[ax]) ax = d;
+  std::sort(ids.begin() + lo, ids.begin() + hi, [&](int a, int b) {
+    const float ca = xyz[3 * (size_t)a + ax], cb = xyz[3 * (size_t)b + ax];
+    return ca < cb || (ca == cb && a < b);
+  });
+  const int pl = nparts / 2;
+  const size_t nl = (size_t)(((long long)n * pl) / nparts);
+  rcb_split(ids, lo, lo + nl, pl, first, xyz, labels);
+  rcb_split(ids, lo + nl, hi, nparts - pl, first + pl, xyz, labels);
+}
+
+// Block count of the product's partition rule: the reference's METIS block counts
+// (2D nv / k, meshFIM2d_eikonal.cu; 3D ceil(nv / k), meshFIM3dEikonal.cu), at least
+// 2 and at most nv.  Labels go to `labels` (nv ints); returns the block count.
+int oracle_partition_rcb(int nv, const float* xyz, int verts_per_block, int dim, int* labels) {
+  if (nv <= 0 || !xyz || !labels) return -1;
+  const long long k = verts_per_block > 0 ? verts_per_block : 1;
+  long long nb = (dim == 2) ? (long long)nv / k : ((long long)nv + k - 1) / k;
+  nb = std::max(2ll, std::min(nb, (long long)nv));
+  std::vector<int> ids(nv);
+  for (int v = 0; v < nv; ++v) ids[v] = v;
+  rcb_split(ids, 0, (size_t)nv, (int)nb, 0, xyz, labels);
+  return (int)nb;
+}
+
 int oracle_num_threads(void) { return n_threads(0); }
 
 // Wall time of the outer iterations of the last oracle3d_solve (its layout set-up

@@ -2,8 +2,9 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
 module, and only as the checker.  It wraps liboracle.so (fim_oracle.cpp, the CPU
-restatement of the reference scheme) and, where built, the reference's own tet
-local solver compiled for the host (_ref/libref_tet.so).
+restatement of the reference scheme) and, where built, the reference's own host
+code compiled here from its sources (_ref/: the tet local solver, the 2D mesh
+preparation, the 3D metric set-up).
 """
 import ctypes
 import os
@@ -46,6 +47,8 @@ def lib():
                                         ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_int, _FP, _FP, ctypes.c_int, _LP, _IP]
         _lib.oracle_num_threads.restype = ctypes.c_int
+        _lib.oracle_partition_rcb.restype = ctypes.c_int
+        _lib.oracle_partition_rcb.argtypes = [ctypes.c_int, _FP, ctypes.c_int, ctypes.c_int, _IP]
         _lib.oracle_last_loop_seconds.restype = ctypes.c_double
     return _lib
 
@@ -59,6 +62,71 @@ def ref_lib():
         _ref.ref_tet_local_solver.restype = ctypes.c_float
         _ref.ref_tet_local_solver.argtypes = [ctypes.c_float] * 9
     return _ref
+
+
+_hostlibs = {}
+
+
+def ref_host_lib(name):
+    """A reference host build from _ref/ (libref_tri.so: the reference's trimesh
+    preparation; libref_host3d.so: TetMesh::init + gettetmem), or None."""
+    path = os.path.join(HERE, "_ref", f"lib{name}.so")
+    if name not in _hostlibs:
+        if not os.path.exists(path):
+            return None
+        lib = ctypes.CDLL(path)
+        if name == "ref_tri":
+            lib.ref_tri_setup.restype = ctypes.c_int
+            lib.ref_tri_setup.argtypes = [ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, ctypes.c_int, _IP, _FP, _FP, _IP,
+                                          ctypes.c_int, _IP, _FP, _FP]
+        else:
+            lib.ref_tet_gram.restype = ctypes.c_int
+            lib.ref_tet_gram.argtypes = [ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, ctypes.c_int, _FP, _FP]
+        _hostlibs[name] = lib
+    return _hostlibs[name]
+
+
+def ref_tri_setup(xyz, faces, speeds=None):
+    """The reference's own 2D mesh preparation (meshFIM2dEikonal::SetMesh on a
+    TriMesh, compiled from its sources): oriented faces, edge lengths, inverse
+    speeds and virtual faces, as a dict of arrays."""
+    lib = ref_host_lib("ref_tri")
+    xyz, faces = _f(xyz), _i(faces)
+    nv, nf = xyz.shape[0], faces.shape[0]
+    sp = None if speeds is None else _f(speeds)
+    cap = 8 * nf + 16
+    while True:
+        fo = np.empty((nf, 3), np.int32)
+        eo = np.empty((nf, 3), np.float32)
+        so = np.empty(nf, np.float32)
+        vc = np.empty(nf, np.int32)
+        vv = np.empty((cap, 3), np.int32)
+        ve = np.empty((cap, 3), np.float32)
+        vs = np.empty(cap, np.float32)
+        n = lib.ref_tri_setup(nv, xyz.ctypes.data_as(_FP), nf, faces.ctypes.data_as(_IP),
+                              sp.ctypes.data_as(_FP) if sp is not None else None, 0 if sp is None else sp.size,
+                              fo.ctypes.data_as(_IP), eo.ctypes.data_as(_FP), so.ctypes.data_as(_FP),
+                              vc.ctypes.data_as(_IP), cap, vv.ctypes.data_as(_IP), ve.ctypes.data_as(_FP),
+                              vs.ctypes.data_as(_FP))
+        if n <= cap:
+            return {"faces": fo, "edges": eo, "speed_inv": so, "vf_count": vc, "vf_verts": vv[:n],
+                    "vf_edges": ve[:n], "vf_speed_inv": vs[:n]}
+        cap = n
+
+
+def ref_tet_gram(xyz, tets, speeds=None):
+    """The reference's own TetMesh::init + gettetmem (compiled from its sources):
+    per tet its metric (6 entries) and six metric edge products."""
+    lib = ref_host_lib("ref_host3d")
+    xyz, tets = _f(xyz), _i(tets)
+    nt = tets.shape[0]
+    sp = None if speeds is None else _f(speeds)
+    M = np.empty((nt, 6), np.float32)
+    G = np.empty((nt, 6), np.float32)
+    lib.ref_tet_gram(xyz.shape[0], xyz.ctypes.data_as(_FP), nt, tets.ctypes.data_as(_IP),
+                     sp.ctypes.data_as(_FP) if sp is not None else None, 0 if sp is None else sp.size,
+                     M.ctypes.data_as(_FP), G.ctypes.data_as(_FP))
+    return M, G
 
 
 def _f(a):
@@ -133,6 +201,18 @@ def solve2d(xyz, faces, speed_inv, obtuse, vf_off, vf_verts, labels, nblocks, se
     return res
 
 
+def partition_rcb(xyz, verts_per_block, dim=3):
+    """Labels and block count of the product's default partition (recursive
+    coordinate bisection with the reference's block-count rule), restated."""
+    xyz = _f(xyz)
+    lab = np.empty(xyz.shape[0], dtype=np.int32)
+    nb = lib().oracle_partition_rcb(xyz.shape[0], xyz.ctypes.data_as(_FP), int(verts_per_block), int(dim),
+                                    lab.ctypes.data_as(_IP))
+    if nb < 0:
+        raise ValueError("oracle_partition_rcb rejected its input")
+    return lab, nb
+
+
 def num_threads():
     return lib().oracle_num_threads()
 
@@ -160,6 +240,7 @@ def ref_gpu():
             return None
         g = ctypes.CDLL(path)
         g.refgpu_last_error.restype = ctypes.c_char_p
+        g.refgpu_last_loop_ms.restype = ctypes.c_double
         g.refgpu_tet_local_solver.restype = ctypes.c_int
         g.refgpu_tet_local_solver.argtypes = [ctypes.c_char_p, _FP, _FP, ctypes.c_int]
         g.refgpu_solve3d.restype = ctypes.c_int
@@ -216,7 +297,8 @@ def ref_gpu_solve3d(xyz, tets, metric6, labels, nblocks, seeds, max_iters=100, h
         M.ctypes.data_as(_FP), lab.ctypes.data_as(_IP), int(nblocks), sd.ctypes.data_as(_IP), sd.size,
         int(max_iters), out.ctypes.data_as(_FP), hist.ctypes.data_as(_FP) if history else None,
         int(max_iters) if history else 0, ctypes.byref(upd), ctypes.byref(mt)))
-    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_tets": mt.value}
+    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_tets": mt.value,
+           "loop_ms": ref_gpu().refgpu_last_loop_ms()}
     if history:
         res["history"] = hist[:it]
     return res

@@ -13,6 +13,7 @@
 // reference's own limit), host round trips every iteration.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <string>
 
 #include "oracle_scheme.hpp"
@@ -22,6 +23,7 @@ using namespace oracle;
 namespace {
 
 std::string g_err;
+double g_loop_ms = 0;  // wall time of the last 3D solve's outer loop
 
 #define RCK(x)                                                         \
   do {                                                                 \
@@ -84,6 +86,10 @@ int launch(cudaKernel_t k, unsigned grid, unsigned block, size_t smem, void** ar
 extern "C" {
 
 const char* refgpu_last_error(void) { return g_err.c_str(); }
+
+// Wall time (ms) of the outer loop of the last refgpu_solve3d: kernels and the
+// reference's per-iteration host round trips, without the layout set-up.
+double refgpu_last_loop_ms(void) { return g_loop_ms; }
 
 // Element-wise reference local solver: out[i] = localSolverTet1(in[9i..9i+8]).
 int refgpu_tet_local_solver(const char* cubin3d, const float* in, float* out, int n) {
@@ -175,6 +181,7 @@ int refgpu_solve3d(const char* cubin3d, int nv, const float* xyz, int nt, const 
   bool* pcon = (bool*)d_con.p; bool* pbc = (bool*)d_bc.p; int* pal = d_al.p;
   int nIter = 2;
   const size_t smem = 16 * (size_t)maxT + 4 * (size_t)maxIn * mapIn;
+  const auto t_loop = std::chrono::steady_clock::now();
   while (!act.empty()) {
     if (++total > (size_t)max_iters) break;
     int na = (int)act.size();
@@ -222,6 +229,7 @@ int refgpu_solve3d(const char* cubin3d, int nv, const float* xyz, int nt, const 
           history[(size_t)(iters - 1) * nv + O.inVerts[b][j]] = hvT[(size_t)b * maxIn + j];
   }
   TRY(d_vT.get(hvT.data(), hvT.size()));
+  g_loop_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_loop).count();
   for (int b = 0; b < nb; ++b)
     for (size_t j = 0; j < O.inVerts[b].size(); ++j) out_final[O.inVerts[b][j]] = hvT[(size_t)b * maxIn + j];
   if (updates) *updates = nupd;

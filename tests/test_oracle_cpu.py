@@ -141,3 +141,28 @@ def test_improve2d_rms_decreases(O, eik, golden):
         sol = 100.0 * np.arccos(np.clip(c, -1, 1))
         rms.append(np.sqrt(np.mean((sol - r) ** 2)))
     assert rms[0] > rms[1] > rms[2] > rms[3], rms
+
+
+@pytest.mark.parametrize("case", ["cube9_64", "cube33_64", "cube65_64", "icosphere4_16", "grid33_16"])
+def test_oracle_bisection_equals_the_products_partition(O, eik, mg, case):
+    """The benchmark's reference arm and CPU baseline take their partition from the
+    oracle's restatement of the default bisection, so that leg loads no product
+    code; it must give the product's labels exactly."""
+    if case.startswith("cube"):
+        n, k = (int(x) for x in case[4:].split("_"))
+        xyz, elems = mg.kuhn_cube(n, 0.2, seed=1)
+        dim = 3
+    elif case.startswith("icosphere"):
+        xyz, elems = mg.icosphere(4)
+        k, dim = 16, 2
+    else:
+        xyz, elems = mg.grid2d(33)
+        k, dim = 16, 2
+    e = eik.Eikonal(dim == 2)
+    e.set_mesh(xyz, elems)
+    e.maxVertsPerBlock_ = k
+    e.prepare()
+    lab, nb = e.getPartition()
+    olab, onb = O.partition_rcb(xyz, k, dim)
+    assert onb == nb
+    assert np.array_equal(olab, lab)
