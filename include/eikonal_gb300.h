@@ -155,6 +155,9 @@ int eik_solve(eik_solver* h);
 int eik_prepare(eik_solver* h);
 
 int eik_num_vertices(const eik_solver* h);
+/* Triangles (2D) or tets (3D) of the mesh: triMesh_->faces.size() /
+ * tetMesh_->tets.size() of the reference's public mesh members (src/Eikonal.h:54-55). */
+int eik_num_elements(const eik_solver* h);
 /* numIterations — src/Eikonal.cu:46-48. */
 int eik_num_iterations(const eik_solver* h);
 /* getFinalResult — src/Eikonal.cu:38-40 (nv floats, original vertex order). */
@@ -166,6 +169,14 @@ int eik_get_iteration(const eik_solver* h, int i, float* out, int nv);
 /* Block labels used by the last solve. */
 int eik_get_partition(const eik_solver* h, int* labels, int nv, int* nblocks);
 int eik_get_stats(const eik_solver* h, eik_stats* s);
+/* Per-outer-iteration figures of the last solve (no counterpart in the reference,
+ * whose GenerateData only prints totals under verbose, meshFIM3dEikonal.cu:544-548).
+ * For iteration i, out[10*i .. 10*i+9] = sweep-kernel launch span (ns, device
+ * timer), check-kernel launch span (ns), then the sweep kernel's block visits,
+ * element slots, halo vertices and owned vertices, then the same four for the
+ * check kernel.  Writes min(iterations, cap) rows and returns that count (>= 0), or
+ * a negative status (-EIK_ERR_ARG, -EIK_ERR_STATE before the first solve). */
+int eik_get_iteration_stats(const eik_solver* h, long long* out, int cap);
 /* writeVTK — src/Eikonal.cu:50-60: <prefix><i>.vtk for the last (all=0) or every
  * (all=1) iteration; the reference's prefix is "result". */
 int eik_write_vtk(const eik_solver* h, const char* prefix, int all);
@@ -175,6 +186,21 @@ int eik_write_vtk(const eik_solver* h, const char* prefix, int all);
  * Call with null arrays to get the sizes first. */
 int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned char* obtuse,
                  int* vf_off, int* vf_verts);
+/* The six metric edge products of every tet (AC.BC, BC.CD, AC.CD, AD.BD, AC.AD,
+ * BC.BD under the tet's metric) as the 3D block layout holds them, in tet order:
+ * the values gettetmem computes for the reference's GetTetMem (meshFIM3dEikonal.cu:
+ * 650-678).  from_device = 0: the host layout of the last eik_prepare / host-built
+ * solve; 1: the layout on the device after a solve (built on the device or
+ * uploaded).  Every slot copy of a tet must hold the same bits (EIK_ERR_STATE
+ * otherwise).  out holds 6 * ne floats (n). */
+int eik_tet_gram(const eik_solver* h, int from_device, float* out, long long n);
+/* The values the 2D block layout takes from that preparation, in the same order:
+ * per face the edge lengths |v1-v0|, |v2-v1|, |v0-v2| (TriMesh::need_faceedges,
+ * TriMesh_connectivity.cu:54-75) and the inverse speed (InitializeAttributes,
+ * TriMesh_stats.cu:64-68), per virtual face its edge lengths and inverse speed
+ * (SplitFace, TriMesh.h:215-313).  Arrays of 3*nf, nf, 3*nvirt and nvirt floats
+ * (sizes from eik_tri_prep); any may be null. */
+int eik_tri_prep_values(const eik_solver* h, float* edges, float* speed_inv, float* vf_edges, float* vf_speed_inv);
 
 /* Self-test of the device local updates on host arrays, element-wise:
  *   which = 0: tet update (localSolverTet1, core3d/cuda/CUDA_kernels.cu:69-225),
@@ -218,8 +244,20 @@ int eik_selftest_wait_timeout(double* waited_ms);
  * All calls share the array and it keeps the previous call's contents (the call
  * clears what must start at zero), so calls that overlap on the GPU, on any
  * stream or thread, race: serialise them.  Work runs on `stream` (a cudaStream_t,
- * null = the default stream) with one host round trip per outer iteration; the
- * call returns when the result is in out_times.
+ * null = the default stream) with one host round trip per outer iteration (the
+ * call synchronises `stream`); the call returns when the result is in out_times.
+ * While another stream is being captured, pass a stream created with
+ * cudaStreamNonBlocking (the legacy default stream would join the capture's
+ * stream and break it) and call from a thread that is not itself capturing (with
+ * cudaStreamCaptureModeGlobal or ThreadLocal the capturing thread may not
+ * synchronise); `stream` itself must not be capturing.
+ *
+ * Speeds and metrics are checked as eik_solve checks them (EIK_ERR_ARG for a
+ * non-positive or non-finite speed or scalar metric, or a non-finite metric
+ * entry).  A device-side wait that gave up returns EIK_ERR_DEVICE, as eik_solve
+ * does.  The visit kernels run 512-thread CTAs: eik_solve picks 512 or one
+ * thread per slot from a handle's first solves, and this call, which keeps no
+ * state between calls, takes 512, the size eik_solve keeps on isotropic meshes.
  *
  * Meshes whose layout and state exceed the array return EIK_ERR_LIMIT (about
  * 200k tets at 64 vertices per block); errbuf (may be null) receives the reason. */

@@ -104,8 +104,12 @@ SIGNATURES = {
     "eik_get_iteration": (ctypes.c_int, [_P, ctypes.c_int, _FP, ctypes.c_int]),
     "eik_get_partition": (ctypes.c_int, [_P, _IP, ctypes.c_int, _IP]),
     "eik_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(EikStats)]),
+    "eik_get_iteration_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "eik_write_vtk": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
     "eik_tri_prep": (ctypes.c_int, [_P, _IP, _IP, _IP, _UP, _IP, _IP]),
+    "eik_tri_prep_values": (ctypes.c_int, [_P, _FP, _FP, _FP, _FP]),
+    "eik_tet_gram": (ctypes.c_int, [_P, ctypes.c_int, _FP, ctypes.c_longlong]),
+    "eik_num_elements": (ctypes.c_int, [_P]),
     "eik_selftest_local_update": (ctypes.c_int, [ctypes.c_int, _FP, _FP, ctypes.c_int]),
     "eik_stream": (_P, [_P]),
     "eik_selftest_wait_timeout": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
@@ -328,6 +332,20 @@ class Eikonal:
         self._check(self._lib.eik_get_stats(self._h, ctypes.byref(s)))
         return s.as_dict()
 
+    ITERATION_STAT_COLUMNS = ("fim_ns", "check_ns", "fim_visits", "fim_slots", "fim_halo", "fim_owned",
+                              "check_visits", "check_slots", "check_halo", "check_owned")
+
+    def iterationStats(self):
+        """Per outer iteration of the last solve: launch spans of the sweep and check
+        kernels (ns) and the block visits, slots, halo and owned vertices each kernel
+        processed, as an (iterations, 10) int64 array (ITERATION_STAT_COLUMNS)."""
+        n = max(self.numIterations(), 0)
+        out = np.zeros((n, 10), dtype=np.int64)
+        rc = self._lib.eik_get_iteration_stats(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), n)
+        if rc < 0:
+            self._check(-rc)
+        return out[:rc]
+
     def writeVTK(self, all_iterations=False, prefix="result"):
         self._check(self._lib.eik_write_vtk(self._h, prefix.encode(), 1 if all_iterations else 0))
 
@@ -342,6 +360,26 @@ class Eikonal:
         self._check(self._lib.eik_tri_prep(self._h, None, None, _iptr(faces), obt.ctypes.data_as(_UP),
                                            _iptr(off), _iptr(vfv)))
         return faces, obt, off, vfv[:nvf.value]
+
+    def tetGram(self, from_device=False):
+        """The six metric edge products per tet (ne, 6) as the block layout holds
+        them: the host layout (after prepare) or the device's (after a solve)."""
+        out = np.empty((self._lib.eik_num_elements(self._h), 6), dtype=np.float32)
+        self._check(self._lib.eik_tet_gram(self._h, 1 if from_device else 0, _fptr(out), out.size))
+        return out
+
+    def triPrepValues(self):
+        """Edge lengths and inverse speeds of the faces and virtual faces as the 2D
+        block layout takes them: (edges (nf, 3), speed_inv (nf,), vf_edges
+        (nvirt, 3), vf_speed_inv (nvirt,))."""
+        faces, _, _, vfv = self.triPrep()
+        nf, nvf = faces.shape[0], vfv.shape[0]
+        ed = np.empty((nf, 3), dtype=np.float32)
+        si = np.empty(nf, dtype=np.float32)
+        ved = np.empty((max(nvf, 1), 3), dtype=np.float32)
+        vsi = np.empty(max(nvf, 1), dtype=np.float32)
+        self._check(self._lib.eik_tri_prep_values(self._h, _fptr(ed), _fptr(si), _fptr(ved), _fptr(vsi)))
+        return ed, si, ved[:nvf], vsi[:nvf]
 
     def printErrorGraph(self, solution):
         """src/Eikonal.cu:233-279: ASCII plot of the RMS error per iteration."""

@@ -112,23 +112,32 @@ std::vector<float> speed_inverse(const eik_solver* h) {
 // positive, 3D 6-entry metrics finite.  6-entry metrics are not required to be
 // positive definite: the reference's own anisotropic fixture (torus_matrices.txt)
 // holds indefinite matrices for half of its tets and the reference solves it.
+// The checks on one speed / metric vector of n values for ne elements: an empty
+// message when the values are usable (vectors of other lengths mean the
+// reference's defaults and are not checked).
+std::string speed_values_problem(const float* v, size_t n, int ne, int dim) {
+  if (!v || n == 0) return "";
+  if (n == (size_t)ne) {
+    for (size_t i = 0; i < n; ++i)
+      if (!(std::isfinite(v[i]) && v[i] > 0.0f))
+        return (dim == 2 ? "speed of face " : "metric of tet ") + std::to_string(i) +
+               " is not a positive finite number";
+  } else if (dim == 3 && n == 6 * (size_t)ne) {
+    for (int t = 0; t < ne; ++t) {
+      const float* m = v + 6 * (size_t)t;
+      bool finite = true;
+      for (int k = 0; k < 6; ++k) finite = finite && std::isfinite(m[k]);
+      if (!finite) return "metric of tet " + std::to_string(t) + " is not finite";
+    }
+  }
+  return "";
+}
+
 int check_speeds(eik_solver* h) {
   if (h->checked_speed == h->speed_ver && h->checked_mesh == h->mesh_ver) return EIK_OK;
   if (h->speeds_set) {
-    const size_t n = h->speeds.size();
-    if (n == (size_t)h->ne) {
-      for (size_t i = 0; i < n; ++i)
-        if (!(std::isfinite(h->speeds[i]) && h->speeds[i] > 0.0f))
-          return fail(h, EIK_ERR_ARG, (h->dim == 2 ? "speed of face " : "metric of tet ") + std::to_string(i) +
-                                          " is not a positive finite number");
-    } else if (h->dim == 3 && n == 6 * (size_t)h->ne) {
-      for (int t = 0; t < h->ne; ++t) {
-        const float* m = &h->speeds[6 * (size_t)t];
-        bool finite = true;
-        for (int k = 0; k < 6; ++k) finite = finite && std::isfinite(m[k]);
-        if (!finite) return fail(h, EIK_ERR_ARG, "metric of tet " + std::to_string(t) + " is not finite");
-      }
-    }
+    const std::string msg = speed_values_problem(h->speeds.data(), h->speeds.size(), h->ne, h->dim);
+    if (!msg.empty()) return fail(h, EIK_ERR_ARG, msg);
   }
   h->checked_speed = h->speed_ver;
   h->checked_mesh = h->mesh_ver;
@@ -521,6 +530,8 @@ int eik_prepare(eik_solver* h) {
 
 int eik_num_vertices(const eik_solver* h) { return h ? h->nv : 0; }
 
+int eik_num_elements(const eik_solver* h) { return h ? h->ne : 0; }
+
 int eik_num_iterations(const eik_solver* h) { return (h && h->solved) ? h->stats.iterations : 0; }
 
 int eik_get_result(const eik_solver* h, float* out, int nv) {
@@ -570,6 +581,15 @@ int eik_get_stats(const eik_solver* h, eik_stats* s) {
   return EIK_OK;
 }
 
+int eik_get_iteration_stats(const eik_solver* h, long long* out, int cap) {
+  if (!h || cap < 0 || (cap > 0 && !out)) return -EIK_ERR_ARG;
+  if (!h->solved || !h->dev) return -EIK_ERR_STATE;
+  const std::vector<long long>& v = h->dev->stats().iter_stats;
+  const int n = std::min(cap, (int)(v.size() / kIterStatWords));
+  if (n > 0) std::memcpy(out, v.data(), sizeof(long long) * kIterStatWords * (size_t)n);
+  return n;
+}
+
 int eik_write_vtk(const eik_solver* h, const char* prefix, int all) {
   eik_solver* m = const_cast<eik_solver*>(h);
   if (!h || !prefix) return fail(m, EIK_ERR_ARG, "null argument");
@@ -603,6 +623,68 @@ int eik_tri_prep(const eik_solver* h, int* nf, int* nvirt, int* faces, unsigned 
   if (obtuse) std::memcpy(obtuse, P.obtuse.data(), P.obtuse.size());
   if (vf_off) std::memcpy(vf_off, P.vf_off.data(), sizeof(int) * P.vf_off.size());
   if (vf_verts && !P.vf_verts.empty()) std::memcpy(vf_verts, P.vf_verts.data(), sizeof(int) * P.vf_verts.size());
+  return EIK_OK;
+}
+
+int eik_tet_gram(const eik_solver* h, int from_device, float* out, long long n) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h || !out) return EIK_ERR_ARG;
+  if (h->dim != 3) return fail(m, EIK_ERR_STATE, "not a tet mesh");
+  if (n != 6 * (long long)h->ne) return fail(m, EIK_ERR_ARG, "out must hold 6 floats per tet");
+  const Layout* L = nullptr;
+  std::vector<float> dcoef;
+  std::vector<int> dse;
+  const std::vector<float>* coef = nullptr;
+  const std::vector<int>* se = nullptr;
+  if (from_device) {
+    if (!h->dev || !h->solved) return fail(m, EIK_ERR_STATE, "no solve has run");
+    const bool built = h->dev->layout_built_on_device();
+    L = built ? &h->dlayout : &h->layout;
+    std::string e = h->dev->layout_arrays(&dcoef, built ? &dse : nullptr);
+    if (!e.empty()) return fail(m, EIK_ERR_CUDA, e);
+    coef = &dcoef;
+    se = built ? &dse : &L->slot_elem;
+  } else {
+    if (h->lay_mesh != h->mesh_ver || h->layout.nb == 0) return fail(m, EIK_ERR_STATE, "no host layout: call eik_prepare");
+    L = &h->layout;
+    coef = &L->coef;
+    se = &L->slot_elem;
+  }
+  std::vector<char> seen((size_t)h->ne, 0);
+  for (const BlockDesc& d : L->blocks)
+    for (int j = 0; j < d.nslots; ++j) {
+      const int t = (*se)[(size_t)d.slot_begin + j];
+      if (t < 0 || t >= h->ne) continue;
+      for (int k = 0; k < 6; ++k) {
+        const float v = (*coef)[6 * (size_t)d.slot_begin + (size_t)k * d.nslots_pad + j];
+        float& o = out[6 * (size_t)t + k];
+        if (!seen[t]) o = v;
+        else if (std::memcmp(&o, &v, sizeof(float)) != 0)
+          return fail(m, EIK_ERR_STATE, "copies of tet " + std::to_string(t) + " differ");
+      }
+      seen[t] = 1;
+    }
+  for (int t = 0; t < h->ne; ++t)
+    if (!seen[t]) return fail(m, EIK_ERR_STATE, "tet " + std::to_string(t) + " has no slot");
+  return EIK_OK;
+}
+
+int eik_tri_prep_values(const eik_solver* h, float* edges, float* speed_inv, float* vf_edges, float* vf_speed_inv) {
+  eik_solver* m = const_cast<eik_solver*>(h);
+  if (!h) return EIK_ERR_ARG;
+  if (h->dim != 2 || h->prep_mesh != h->mesh_ver) return fail(m, EIK_ERR_STATE, "no triangle mesh set");
+  const TriPrep& P = h->prep;
+  const size_t nvf = P.vf_verts.size() / 3;
+  if (edges) std::memcpy(edges, P.edges.data(), sizeof(float) * P.edges.size());
+  if (speed_inv) {
+    const std::vector<float> inv = speed_inverse(h);
+    std::memcpy(speed_inv, inv.data(), sizeof(float) * inv.size());
+  }
+  if (vf_edges && nvf) std::memcpy(vf_edges, P.vf_edges.data(), sizeof(float) * P.vf_edges.size());
+  // virtual faces take the inverse speed of the reference's default speed type
+  // (ONE, TriMesh.h:240-257), whatever the faces' speeds
+  if (vf_speed_inv)
+    for (size_t i = 0; i < nvf; ++i) vf_speed_inv[i] = 1.0f;
   return EIK_OK;
 }
 
@@ -640,6 +722,9 @@ int eik_solve3d_noalloc(const float* xyz, int nv, const int* tets, int nt, const
   std::vector<int> sd = (nseeds > 0) ? std::vector<int>(seeds, seeds + nseeds) : std::vector<int>(1, 0);
   for (int v : sd)
     if (v < 0 || v >= nv) return report(EIK_ERR_ARG, "seed out of range");
+  // the same speed / metric checks as eik_solve
+  msg = speed_values_problem(nspeeds > 0 ? speeds : nullptr, (size_t)std::max(0ll, nspeeds), nt, 3);
+  if (!msg.empty()) return report(EIK_ERR_ARG, msg);
   std::vector<float> M;
   tet_metrics(nt, nspeeds > 0 ? speeds : nullptr, (size_t)std::max(0ll, nspeeds), M);
   std::vector<int> labels;
@@ -650,8 +735,13 @@ int eik_solve3d_noalloc(const float* xyz, int nv, const int* tets, int nt, const
   if (!msg.empty()) return report(EIK_ERR_MESH, msg);
   int it = 0;
   size_t need = 0;
-  msg = solve3d_noalloc(L, sd, max_iterations, out_times, (cudaStream_t)stream, &it, &need);
-  if (!msg.empty()) return report(msg.find("too large") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, msg);
+  NoAllocFailure kind = NoAllocFailure::kNone;
+  msg = solve3d_noalloc(L, sd, max_iterations, out_times, (cudaStream_t)stream, &it, &need, &kind);
+  if (!msg.empty())
+    return report(kind == NoAllocFailure::kLimit    ? EIK_ERR_LIMIT
+                  : kind == NoAllocFailure::kDevice ? EIK_ERR_DEVICE
+                                                    : EIK_ERR_CUDA,
+                  msg);
   if (iterations) *iterations = it;
   return EIK_OK;
 }

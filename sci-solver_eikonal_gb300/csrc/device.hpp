@@ -20,6 +20,8 @@ typedef struct CUstream_st* cudaStream_t;
 
 namespace eikgb {
 
+constexpr int kIterStatWords = 10;
+
 struct SolveStats {
   int iterations = 0;
   long long vertex_updates = 0;  // owned vertices x sweeps over all block visits
@@ -35,6 +37,10 @@ struct SolveStats {
   float fim_kernel_ms = 0.0f;    // summed launch spans of the sweep kernel (device timer)
   float check_kernel_ms = 0.0f;  // same for the neighbour-check kernel
   int fim_launches = 0, check_launches = 0;
+  // per outer iteration, kIterStatWords values: sweep-kernel and check-kernel
+  // launch spans (ns, device timer), then the sweep kernel's block visits, element
+  // slots, halo vertices and owned vertices, then the same four for the check kernel
+  std::vector<long long> iter_stats;
   long long h2d_bytes = 0;       // host-to-device bytes the last solve copied (initial state)
   std::vector<int> inst_iters;   // outer iterations run by every instance
   // precision mode: FP64 residual check after the solve
@@ -123,6 +129,9 @@ class DeviceSolve {
   // a new per-tet metric (6 entries per tet, host array).
   std::string refresh_coef_built(const float* M, int mcomp);
   bool layout_built_on_device() const;
+  // Copies of the uploaded layout's per-slot coefficients and (device-built 3D
+  // layouts only) the element id of every slot, for checks against the reference.
+  std::string layout_arrays(std::vector<float>* coef, std::vector<int>* slot_elem) const;
   // Seeds are original vertex ids.  init_vals (2D only, may be null) are the
   // vertex values the reference's all-vertex convergence test starts from.
   std::string set_seeds(const std::vector<int>& seeds_orig, const float* init_vals);
@@ -185,8 +194,10 @@ std::string selftest_wait_timeout(int* status, double* waited_ms);
 // 32 MiB array of the library's device image (no cudaMalloc / cudaFree).  Runs on
 // `stream` (a cudaStream_t, may be null), one host round trip per outer
 // iteration.  Fails with a message when the mesh needs more scratch than the array
-// holds (bytes_needed reports the requirement).
+// holds (bytes_needed reports the requirement); *failure says which kind of
+// failure a non-empty message is.
+enum class NoAllocFailure { kNone, kLimit, kDevice, kCuda };
 std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int max_iters, float* out_host,
-                            cudaStream_t stream, int* iterations, size_t* bytes_needed);
+                            cudaStream_t stream, int* iterations, size_t* bytes_needed, NoAllocFailure* failure);
 
 }  // namespace eikgb

@@ -91,7 +91,11 @@ struct DevArgs {
   Ctl* ctl;
   float* hist;
   int hist_cap;
-  unsigned long long* ktime;  // per iteration: [fim start, fim end, check start, check end] (globaltimer ns)
+  // per iteration, kKStride words: [~sweep start, sweep end, ~check start, check
+  // end] (globaltimer ns; starts stored complemented so the zeroed buffer and
+  // atomicMax give the earliest start), then the sweep kernel's visits, slots, halo and owned
+  // vertices, then the same four for the check kernel
+  unsigned long long* ktime;
   int ktime_cap;
   int fim_sweeps;
   int max_slots_pad, max_local, max_owned;
@@ -125,6 +129,7 @@ struct DevArgs {
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
 constexpr float kEps2D = 1e-5f;
 constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
+constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::ktime)
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + 1D bulk copy (TMA engine)
@@ -184,10 +189,22 @@ __device__ __forceinline__ void fence_proxy_async() {
 
 // launch span of a visit kernel: earliest CTA start, latest CTA end
 __device__ __forceinline__ void stamp_start(const DevArgs& a, int iter, int which) {
-  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap) atomicMin(&a.ktime[4 * iter + 2 * which], global_ns());
+  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap)
+    atomicMax(&a.ktime[kKStride * iter + 2 * which], ~global_ns());
 }
 __device__ __forceinline__ void stamp_end(const DevArgs& a, int iter, int which) {
-  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap) atomicMax(&a.ktime[4 * iter + 2 * which + 1], global_ns());
+  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap)
+    atomicMax(&a.ktime[kKStride * iter + 2 * which + 1], global_ns());
+}
+// one visit's inputs into this iteration's telemetry (caller: one thread)
+__device__ __forceinline__ void count_visit(const DevArgs& a, int iter, int which, int slots, int halo, int owned) {
+  if (a.ktime && iter < a.ktime_cap) {
+    unsigned long long* w = a.ktime + kKStride * iter + 4 + 4 * which;
+    atomicAdd(w, 1ull);
+    atomicAdd(w + 1, (unsigned long long)slots);
+    atomicAdd(w + 2, (unsigned long long)halo);
+    atomicAdd(w + 3, (unsigned long long)owned);
+  }
 }
 
 // order-preserving float <-> int keys for shared-memory atomicMin
@@ -520,6 +537,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
         atomicAdd(&a.ctl->chk_visits, 1ull);
       }
       atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
+      count_visit(a, iter, kCheck ? 1 : 0, ns, bd.nhalo, nown);
       atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
       atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
       atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
@@ -677,6 +695,7 @@ __global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
         atomicAdd(&a.ctl->chk_visits, 1ull);
       }
       atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
+      count_visit(a, iter, kCheck ? 1 : 0, ns, bd.nhalo, nown);
       atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
       atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
       atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
@@ -851,6 +870,7 @@ __global__ void __launch_bounds__(1024) k_visit2d_slot(DevArgs a) {
         atomicAdd(&a.ctl->chk_visits, 1ull);
       }
       atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
+      count_visit(a, iter, kCheck ? 1 : 0, ns, bd.nhalo, nown);
       atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
       atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
       atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
@@ -1315,6 +1335,21 @@ __global__ void k_selftest_quot(const float* in, float* out, int n) {
     if (e_ != cudaSuccess) return std::string(#x ": ") + cudaGetErrorString(e_);       \
   } while (0)
 
+// Raises a kernel's dynamic shared-memory limit on the current device to at least
+// `bytes`, never lowering it: handles, batches, servers and the allocation-free
+// path share the kernels, and one that set a smaller limit after another had set a
+// larger one would make the other's launches fail.  The read and the write are one
+// step under a lock.
+std::mutex g_smem_attr_mutex;
+cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+  std::lock_guard<std::mutex> lock(g_smem_attr_mutex);
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaFuncGetAttributes(&fa, func);
+  if (e != cudaSuccess) return e;
+  if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // CTA sizes of the 3D visit kernels when the caller gives none.  One thread per
 // element slot of the largest block (up to 1024) runs every slot's updates side by
 // side; 512 threads lets two CTAs (64 registers per thread) share an SM and overlap
@@ -1403,7 +1438,6 @@ struct DeviceSolve::Impl {
   double* coef64 = nullptr;
   unsigned long long* res_cand = nullptr;  // nv + 3 words: per-vertex FP64 minimum, then the reduction
   bool prec = false;
-  std::vector<unsigned long long> h_ktime;
   // graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1561,8 +1595,8 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
       kv_chk = (void*)k_visit2d<true>;
       vthreads = std::min(vthreads, 256);  // the slot-loop kernel's launch bound
     }
-    CK(cudaFuncSetAttribute(kv_fim, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
-    CK(cudaFuncSetAttribute(kv_chk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem_chk));
+    CK(raise_smem_limit(kv_fim, vsmem));
+    CK(raise_smem_limit(kv_chk, vsmem_chk));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kv_fim, vthreads, vsmem));
     if (occ < 1) return "visit kernel cannot be resident (shared memory / registers)";
@@ -1726,6 +1760,21 @@ std::string DeviceSolve::upload_built(const Layout& L, Built3D& b) {
 }
 
 bool DeviceSolve::layout_built_on_device() const { return p_->built; }
+
+std::string DeviceSolve::layout_arrays(std::vector<float>* coef, std::vector<int>* slot_elem) const {
+  const Impl& P = *p_;
+  if (!P.coef) return "no layout on the device";
+  if (coef) {
+    coef->resize(P.coef_n);
+    CK(cudaMemcpy(coef->data(), P.coef, sizeof(float) * P.coef_n, cudaMemcpyDeviceToHost));
+  }
+  if (slot_elem) {
+    if (!P.built || !P.slot_elem) return "element ids of the slots are kept on the host for this layout";
+    slot_elem->resize(P.coef_n / 6);
+    CK(cudaMemcpy(slot_elem->data(), P.slot_elem, sizeof(int) * slot_elem->size(), cudaMemcpyDeviceToHost));
+  }
+  return "";
+}
 
 std::string DeviceSolve::refresh_coef_built(const float* M, int mcomp) {
   Impl& P = *p_;
@@ -1904,17 +1953,10 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     if (P.ktime) cudaFree(P.ktime);
     P.ktime = nullptr;
     P.ktime_cap = max_iters + 1;
-    CK(cudaMalloc((void**)&P.ktime, sizeof(unsigned long long) * 4 * (size_t)P.ktime_cap));
+    CK(cudaMalloc((void**)&P.ktime, sizeof(unsigned long long) * kKStride * (size_t)P.ktime_cap));
     P.drop_graph();
   }
-  {
-    // starts at +inf, ends at 0
-    std::vector<unsigned long long> kt(4 * (size_t)P.ktime_cap);
-    for (size_t i = 0; i < kt.size(); ++i) kt[i] = (i % 2 == 0) ? ~0ull : 0ull;
-    P.h_ktime.swap(kt);
-    CK(cudaMemcpyAsync(P.ktime, P.h_ktime.data(), sizeof(unsigned long long) * P.h_ktime.size(),
-                       cudaMemcpyHostToDevice, st));
-  }
+  CK(cudaMemsetAsync(P.ktime, 0, sizeof(unsigned long long) * kKStride * (size_t)P.ktime_cap, st));
   // initial state
   // initial state built on the device: only the seed ids, the starting blocks and
   // (when given) the caller's initial values cross from the host
@@ -1967,8 +2009,7 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     CK(cudaMemsetAsync(P.inst_nnext, 0, sizeof(int) * P.ninst, st));
     CK(cudaMemsetAsync(P.inst_fail, 0, sizeof(int) * P.ninst, st));
   }
-  stats_.h2d_bytes = (long long)sizeof(unsigned long long) * P.h_ktime.size() +
-                     (long long)sizeof(float) * P.h_prev.size() + (long long)sizeof(int) * nseed +
+  stats_.h2d_bytes = (long long)sizeof(float) * P.h_prev.size() + (long long)sizeof(int) * nseed +
                      (long long)sizeof(int) * P.h_act.size() + 2ll * sizeof(int) * P.ninst + (long long)sizeof(Ctl);
   Ctl c{};
   c.max_iters = max_iters;
@@ -2024,13 +2065,19 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   stats_.fim_owned = (long long)out.fim_owned;
   const bool measured = tune_slot >= 0 && stats_.error == 0 && stats_.fim_slots > 0;
   {
-    std::vector<unsigned long long> kt(4 * (size_t)P.ktime_cap);
+    std::vector<unsigned long long> kt(kKStride * (size_t)P.ktime_cap);
     CK(cudaMemcpy(kt.data(), P.ktime, sizeof(unsigned long long) * kt.size(), cudaMemcpyDeviceToHost));
     double fim = 0, chk = 0;
     int nf = 0, nc = 0;
-    for (int i = 0; i < std::min(out.iter, P.ktime_cap); ++i) {
-      if (kt[4 * i + 1] > kt[4 * i] && kt[4 * i] != ~0ull) { fim += (double)(kt[4 * i + 1] - kt[4 * i]); ++nf; }
-      if (kt[4 * i + 3] > kt[4 * i + 2] && kt[4 * i + 2] != ~0ull) { chk += (double)(kt[4 * i + 3] - kt[4 * i + 2]); ++nc; }
+    const int nit = std::min(out.iter, P.ktime_cap);
+    stats_.iter_stats.assign(kIterStatWords * (size_t)nit, 0);
+    for (int i = 0; i < nit; ++i) {
+      const unsigned long long* k = &kt[kKStride * (size_t)i];
+      long long* o = &stats_.iter_stats[kIterStatWords * (size_t)i];
+      const unsigned long long f0 = ~k[0], c0 = ~k[2];
+      if (k[0] && k[1] > f0) { fim += (double)(k[1] - f0); ++nf; o[0] = (long long)(k[1] - f0); }
+      if (k[2] && k[3] > c0) { chk += (double)(k[3] - c0); ++nc; o[1] = (long long)(k[3] - c0); }
+      for (int w = 0; w < 8; ++w) o[2 + w] = (long long)k[4 + w];
     }
     stats_.fim_kernel_ms = (float)(fim * 1e-6);
     if (measured && fim > 0) {  // sweep-kernel time per slot visit of this CTA size
@@ -2129,10 +2176,10 @@ std::string DeviceSolve::visit_once(bool check, const float* T_host, float* out_
   const int vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
   const size_t vsmem = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
   if (!check) {
-    CK(cudaFuncSetAttribute((const void*)k_visit2d_slot<false, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    CK(raise_smem_limit((const void*)k_visit2d_slot<false, 7>, vsmem));
     k_visit2d_slot<false, 7><<<std::min(L.nb, nsm * 8), vthreads, vsmem, st>>>(a);
   } else {
-    CK(cudaFuncSetAttribute((const void*)k_visit2d_slot<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    CK(raise_smem_limit((const void*)k_visit2d_slot<true, 1>, vsmem));
     k_visit2d_slot<true, 1><<<std::min(L.nb, nsm * 8), vthreads, vsmem, st>>>(a);
   }
   CK(cudaGetLastError());
@@ -2492,8 +2539,17 @@ T* carve_scratch(unsigned char* base, size_t& off, size_t n) {
 
 }  // namespace
 
+// CTA size of the allocation-free path's visit kernels.  The regular path picks
+// 512 or one thread per slot per handle from its first solves; this path keeps no
+// state between calls, so it runs 512 (two CTAs per SM), the size the regular path
+// keeps on isotropic meshes such as the jittered cubes.
+constexpr int kNoAllocThreads = 512;
+
 std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int max_iters, float* out_host,
-                            cudaStream_t st, int* iterations, size_t* bytes_needed) {
+                            cudaStream_t st, int* iterations, size_t* bytes_needed, NoAllocFailure* failure) {
+  NoAllocFailure dummy;
+  NoAllocFailure& fk = failure ? *failure : dummy;
+  fk = NoAllocFailure::kCuda;  // what a CK() return below means
   const int ncoef = 6;
   // byte budget of the layout and the state
   size_t need = 0;
@@ -2514,9 +2570,11 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
     carve_scratch<int>(z, need, 4);                                         // instance control
   }
   if (bytes_needed) *bytes_needed = need;
-  if (need > kNoAllocScratchBytes)
+  if (need > kNoAllocScratchBytes) {
+    fk = NoAllocFailure::kLimit;
     return "mesh too large for the allocation-free path: needs " + std::to_string(need >> 20) +
            " MiB of scratch, the fixed array holds " + std::to_string(kNoAllocScratchBytes >> 20) + " MiB";
+  }
   const int max_slots_pad = (L.max_slots + 3) & ~3;
   const int max_local = std::max(L.max_local, 1), max_owned = std::max(L.max_owned, 1);
   const size_t smem = smem_bytes(ncoef, max_slots_pad, max_local, max_owned);
@@ -2524,7 +2582,10 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  if (smem + 64 > (size_t)maxsm) return "block too large for shared memory; use fewer vertices per block";
+  if (smem + 64 > (size_t)maxsm) {
+    fk = NoAllocFailure::kLimit;
+    return "block too large for shared memory; use fewer vertices per block";
+  }
   void* basev = nullptr;
   std::string e = noalloc_base(&basev);
   if (!e.empty()) return e;
@@ -2597,10 +2658,10 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
   a.fim_sweeps = 2; a.max_slots_pad = max_slots_pad; a.max_local = max_local; a.max_owned = max_owned;
   a.blk_inst = blk_inst; a.inst_done = inst_ctl; a.inst_iters = inst_ctl + 1; a.inst_nnext = inst_ctl + 2;
   a.inst_fail = inst_ctl + 3; a.ninst = 1;
-  CK(cudaFuncSetAttribute((const void*)k_visit3d<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  CK(cudaFuncSetAttribute((const void*)k_visit3d<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CK(raise_smem_limit((const void*)k_visit3d<false>, smem));
+  CK(raise_smem_limit((const void*)k_visit3d<true>, smem));
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_visit3d<false>, 256, smem));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_visit3d<false>, kNoAllocThreads, smem));
   if (occ < 1) return "visit kernel cannot be resident";
   const int grid = std::min(occ * nsm, std::max(L.nb, 1));
   int iters = 0;
@@ -2609,11 +2670,14 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
     CK(cudaMemcpyAsync(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     iters = h.iter;
-    if (h.error) return "device reported error flags " + std::to_string(h.error);
+    if (h.error) {
+      fk = NoAllocFailure::kDevice;
+      return "device reported error flags " + std::to_string(h.error);
+    }
     if (h.nact == 0 || h.iter >= max_iters) break;
-    k_visit3d<false><<<grid, 256, smem, st>>>(a);
+    k_visit3d<false><<<grid, kNoAllocThreads, smem, st>>>(a);
     k_commit3d<<<nsm * 4, 256, 0, st>>>(a);
-    k_visit3d<true><<<grid, 256, smem, st>>>(a);
+    k_visit3d<true><<<grid, kNoAllocThreads, smem, st>>>(a);
     k_close3d_noalloc<<<1, 32, 0, st>>>(a);
     CK(cudaGetLastError());
   }
@@ -2623,6 +2687,7 @@ std::string solve3d_noalloc(const Layout& L, const std::vector<int>& seeds, int 
   CK(cudaMemcpyAsync(out_host, out, sizeof(float) * L.nv, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (iterations) *iterations = iters;
+  fk = NoAllocFailure::kNone;
   return "";
 }
 
