@@ -3,14 +3,21 @@
   meshes.npz          the reference's own test meshes (src/test/test_data of
                       SCI-Solver_Eikonal): TetGen balls sphere8/13/334, the 16^3
                       CubeMesh, the torus with its per-tet metric file, and the PLY
-                      spheres / square used by the 2D tests.  Read from REFERENCE_ROOT
-                      (default /root/reference) in this container.
+                      spheres / square used by the 2D tests.  Read from the reference
+                      source tree named by REFERENCE_ROOT.
+  ref_host_setup.npz  inputs and outputs of the reference's own host set-up compiled
+                      here from its sources (oracle/_ref/libref_tri.so: the 2D mesh
+                      preparation; oracle/_ref/libref_host3d.so: TetMesh::init +
+                      gettetmem) on meshes with obtuse corners, heterogeneous speeds,
+                      near-right angles, slivers and anisotropic metrics; written with
+                      `python tests/golden/make_golden.py --ref-host`.
   ref_gpu_outputs.npz travel times produced by the reference's own CUDA kernels
                       (oracle/_ref/*.cubin run by oracle/ref_gpu_driver.cpp) on fixed
                       inputs and partitions; written on a GPU machine with
                       `python tests/golden/make_golden.py --ref-gpu`.
 
     python tests/golden/make_golden.py            # meshes.npz (needs the reference tree)
+    python tests/golden/make_golden.py --ref-host # ref_host_setup.npz (needs the reference tree)
     python tests/golden/make_golden.py --ref-gpu  # ref_gpu_outputs.npz (needs a GPU)
 """
 import os
@@ -133,8 +140,64 @@ def make_ref_gpu():
     np.savez_compressed(os.path.join(HERE, "ref_gpu_outputs.npz"), **out)
 
 
+def ref_host_cases():
+    """Inputs of the host set-up fixtures: (name, dim, xyz, elems, speeds)."""
+    import importlib
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    g = np.load(os.path.join(HERE, "meshes.npz"))
+    cases = []
+    # 2D: obtuse corners (PLY spheres), the same with heterogeneous face speeds,
+    # right angles (grid, square), corners within rounding of 90 degrees
+    cases.append(("sphere74", 2, g["sphere_74verts_xyz"], g["sphere_74verts_faces"], None))
+    xyz, f = g["sphere_1154verts_xyz"], g["sphere_1154verts_faces"]
+    cases.append(("sphere1154_speed", 2, xyz, f, mg.batch_speed(xyz, f)))
+    xyz, f = mg.grid2d(33)
+    cases.append(("grid33", 2, xyz, f, None))
+    cases.append(("square16", 2, g["SquareMesh_size16_xyz"], g["SquareMesh_size16_faces"] - 1, None))
+    rng = np.random.default_rng(12)
+    xyz, f = mg.grid2d(21)
+    xyz = xyz.copy()
+    xyz[:, :2] += rng.uniform(-1e-7 / 20, 1e-7 / 20, (xyz.shape[0], 2)).astype(np.float32)
+    cases.append(("grid21_near_right", 2, xyz, f, np.exp(rng.uniform(np.log(0.5), np.log(2), f.shape[0])).astype(
+        np.float32)))
+    # 3D: the reference's ball and anisotropic torus, a jittered cube with scalar
+    # metrics, slivers with anisotropic 6-entry metrics
+    cases.append(("sphere334", 3, g["sphere334_xyz"], g["sphere334_tets"], None))
+    cases.append(("torus", 3, g["torus_xyz"], g["torus_tets"], g["torus_metric"]))
+    xyz, t = mg.kuhn_cube(9, 0.2, seed=1)
+    cases.append(("cube9", 3, xyz, t, (1.0 / mg.log_uniform_speeds(t.shape[0], seed=2).astype(np.float64) ** 2)
+                  .astype(np.float32)))
+    xyz, t, _ = mg.sliver_cube(9, 0.10, seed=5)
+    cases.append(("sliver9_aniso", 3, xyz, t, mg.anisotropic_metrics(t.shape[0], seed=6).ravel()))
+    return cases
+
+
+def make_ref_host():
+    from oracle import oracle as O
+    if O.ref_host_lib("ref_tri") is None or O.ref_host_lib("ref_host3d") is None:
+        raise SystemExit("the reference host builds are missing: run oracle/build_oracle.py with the reference tree")
+    out = {}
+    for name, dim, xyz, el, sp in ref_host_cases():
+        out[name + "_xyz"] = np.asarray(xyz, np.float32)
+        out[name + "_elems"] = np.asarray(el, np.int32)
+        if sp is not None:
+            out[name + "_speeds"] = np.asarray(sp, np.float32)
+        if dim == 2:
+            r = O.ref_tri_setup(xyz, el, sp)
+            for k, v in r.items():
+                out[name + "_" + k] = v
+            print(name, el.shape[0], "faces", r["vf_verts"].shape[0], "virtual")
+        else:
+            _, G = O.ref_tet_gram(xyz, el, sp)
+            out[name + "_gram"] = G
+            print(name, el.shape[0], "tets")
+    np.savez_compressed(os.path.join(HERE, "ref_host_setup.npz"), **out)
+
+
 if __name__ == "__main__":
     if "--ref-gpu" in sys.argv:
         make_ref_gpu()
+    elif "--ref-host" in sys.argv:
+        make_ref_host()
     else:
         make_meshes()

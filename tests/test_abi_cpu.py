@@ -283,3 +283,27 @@ def test_metis_partition(eik, mg, dim):
     with pytest.raises(eik.EikonalError) as ex:
         e.prepare()
     assert ex.value.code == 1
+
+
+@pytest.mark.parametrize("bad", ["nan", "zero", "negative", "inf_metric6"])
+def test_invalid_speeds_rejected_by_both_3d_entry_points(eik, mg, bad):
+    """eik_solve and the allocation-free eik_solve3d_noalloc apply the same speed and
+    metric checks before any device work (EIK_ERR_ARG = 1)."""
+    xyz, tets = mg.kuhn_cube(5, 0.0)
+    nt = tets.shape[0]
+    if bad == "inf_metric6":
+        sp = np.tile(np.array([1, 0, 0, 1, 0, 1], np.float32), nt)
+        sp[6 * 3 + 1] = np.inf
+    else:
+        sp = np.ones(nt, np.float32)
+        sp[7] = {"nan": np.nan, "zero": 0.0, "negative": -1.0}[bad]
+    e = eik.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.initSpeedMtxMultipliers(sp)
+    with pytest.raises(eik.EikonalError) as ex:
+        e.prepare()
+    assert ex.value.code == 1
+    with pytest.raises(eik.EikonalError) as ex:
+        eik.solve3d_noalloc(xyz, tets, sp, [0])
+    assert ex.value.code == 1
+    assert "tet" in str(ex.value)
