@@ -8,6 +8,21 @@
                                host from the reference tree (ref_tethost.cpp + refshim/)
   oracle/_ref/ref3d.cubin      the reference's 3D kernels for sm_103a (ref_wrap3d.cu)
   oracle/_ref/ref2d.cubin      the reference's 2D kernels for sm_103a (ref_wrap2d.cu)
+  oracle/_ref/libref_tri.so    the reference's 2D mesh preparation (its trimesh sources
+                               src/core2d/cuda/TriMesh_*.cu, filter.cc, ... compiled as host
+                               C++ with g++, driven by ref_trihost.cpp)
+  oracle/_ref/libref_host3d.so the reference's TetMesh::init and gettetmem (tetmesh.cu,
+                               meshFIM3dEikonal.cu and CUDA_kernels.cu compiled by nvcc, as
+                               its own build compiles them, driven by ref_tethost3d.cu; shims
+                               for cusp and metis.h in refshim_nvcc/, cudaThreadSynchronize
+                               mapped to cudaDeviceSynchronize)
+
+Host floating point of the reference builds: x86-64's baseline instruction set has
+no fused multiply-add, so g++ and nvcc's host pass round every product and sum
+separately there, whatever -ffp-contract says; the product's host set-up is built
+with -ffp-contract=off to give those bits on every host, including aarch64, where
+gcc would otherwise fuse (its default is -ffp-contract=fast).  The pin tests hold
+the product's host set-up to these builds bit for bit.
 
 The _ref artefacts need the reference sources (REFERENCE_ROOT, default
 /root/reference); where they are absent only liboracle.so is built and whatever
@@ -23,6 +38,12 @@ REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
 OUT_REF = os.path.join(HERE, "_ref")
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
+
+
+# host sources of the reference's trimesh directory (src/core2d/cuda)
+TRI_SOURCES = ["TriMesh_connectivity.cu", "TriMesh_stats.cu", "TriMesh_normals.cu", "TriMesh_tstrips.cu",
+               "TriMesh_bounding.cu", "TriMesh_grid.cu", "TriMesh_io.cu", "filter.cc", "TriMesh_curvature.cc",
+               "TriMesh_pointareas.cc", "KDtree.cc", "remove.cc", "reorder_verts.cc"]
 
 
 def _run(cmd):
@@ -71,12 +92,36 @@ def build(force=False):
             jobs.append([NVCC, "-std=c++17", "-O3", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a",
                          "-maxrregcount=64", "-w", "-I", os.path.join(sdir, "include"), "-I", sdir, wrap,
                          "-o", cub])
+    # the reference's 2D mesh preparation: every host source of its trimesh
+    # directory (they reference each other), plus the driver
+    tri = os.path.join(OUT_REF, "libref_tri.so")
+    tri_srcs = [os.path.join(src2, "cuda", f) for f in TRI_SOURCES] + [os.path.join(HERE, "ref_trihost.cpp")]
+    tri_objs = []
+    if force or _stale(tri, tri_srcs):
+        objdir = os.path.join(OUT_REF, "tri_obj")
+        os.makedirs(objdir, exist_ok=True)
+        for src in tri_srcs:
+            obj = os.path.join(objdir, os.path.basename(src) + ".o")
+            tri_objs.append(obj)
+            jobs.append([CXX, "-O2", "-std=c++17", "-w", "-fPIC", "-x", "c++", "-include",
+                         os.path.join(HERE, "refshim", "host_minmax.h"), "-I", os.path.join(src2, "include"),
+                         "-c", src, "-o", obj])
+    h3 = os.path.join(OUT_REF, "libref_host3d.so")
+    drv3 = os.path.join(HERE, "ref_tethost3d.cu")
+    if force or _stale(h3, [drv3]):
+        jobs.append([NVCC, "-std=c++17", "-O2", "-w", "-rdc=true", "-shared", "-Xcompiler", "-fPIC", "--cudart", "static",
+                     "-gencode", "arch=compute_103a,code=sm_103a", "-DcudaThreadSynchronize=cudaDeviceSynchronize",
+                     "-I", os.path.join(HERE, "refshim_nvcc"), "-I", os.path.join(src3, "include"), "-I", src3, drv3,
+                     os.path.join(src3, "cuda", "meshFIM3dEikonal.cu"), os.path.join(src3, "cuda", "tetmesh.cu"),
+                     os.path.join(src3, "cuda", "CUDA_kernels.cu"), "-o", h3])
     procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True) for j in jobs]
     for j, p in zip(jobs, procs):
         out, err = p.communicate()
         if p.returncode != 0:
             raise RuntimeError("oracle build failed: " + " ".join(j) + "\n" + out + err)
-    built += [tet, os.path.join(OUT_REF, "ref3d.cubin"), os.path.join(OUT_REF, "ref2d.cubin")]
+    if tri_objs:
+        _run([CXX, "-shared", "-Wl,--no-undefined", "-o", tri, *tri_objs])
+    built += [tet, os.path.join(OUT_REF, "ref3d.cubin"), os.path.join(OUT_REF, "ref2d.cubin"), tri, h3]
     return built
 
 

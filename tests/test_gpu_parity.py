@@ -114,10 +114,15 @@ def _ref3d_cases(mg, golden):
     xyz, tets, sp, seed = cube(mg, 17)
     out.append(("cube17_three_seeds_16vpb", xyz, tets, sp, [0, seed, xyz.shape[0] - 1], {"maxVertsPerBlock_": 16}))
     out.append(("cube17_stop_after_3", xyz, tets, sp, [seed], {"maxIterations_": 3}))
+    # the precision workload's shape in FP32: 10% sliver tets, anisotropic 6-entry metrics
+    xyz, tets, _ = mg.sliver_cube(17, 0.10, seed=5)
+    M6 = mg.anisotropic_metrics(tets.shape[0], seed=6).ravel()
+    seeds = np.random.default_rng(9).choice(xyz.shape[0], 4, replace=False).tolist()
+    out.append(("sliver17_anisotropic", xyz, tets, M6, seeds, {"maxIterations_": 1000}))
     return out
 
 
-@pytest.mark.parametrize("idx", range(8))
+@pytest.mark.parametrize("idx", range(9))
 def test_3d_bitwise_vs_reference_kernels(need_gpu, eik, O, mg, golden, idx):
     need_ref(O)
     name, xyz, tets, sp, seeds, opts = _ref3d_cases(mg, golden)[idx]
@@ -379,12 +384,17 @@ def _cases2d(mg, golden):
     out.append(("sphere74", golden["sphere_74verts_xyz"], golden["sphere_74verts_faces"], None, [0], {}))
     out.append(("sphere1154", golden["sphere_1154verts_xyz"], golden["sphere_1154verts_faces"], None, [0],
                 {"maxVertsPerBlock_": 32}))
+    # obtuse corners (3,072 virtual faces) under heterogeneous face speeds: the
+    # virtual faces keep inverse speed 1 (the reference's speed type ONE), the real
+    # faces carry 1/speed
+    xyz, f = golden["sphere_1154verts_xyz"], golden["sphere_1154verts_faces"]
+    out.append(("sphere1154_speed", xyz, f, mg.batch_speed(xyz, f), [0, 500], {"maxVertsPerBlock_": 32}))
     out.append(("square16_structured", golden["SquareMesh_size16_xyz"], golden["SquareMesh_size16_faces"], None,
                 [0], {"isStructured_": 1, "squareBlockLength_": 4, "squareBlockWidth_": 4}))
     return out
 
 
-@pytest.mark.parametrize("idx", range(7))
+@pytest.mark.parametrize("idx", range(8))
 def test_2d_vs_reference_kernels(need_gpu, eik, O, mg, golden, idx):
     need_ref(O)
     name, xyz, f, sp, seeds, opts = _cases2d(mg, golden)[idx]
