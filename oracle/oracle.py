@@ -246,6 +246,8 @@ def ref_gpu():
         g.refgpu_solve3d.restype = ctypes.c_int
         g.refgpu_solve3d.argtypes = [ctypes.c_char_p, ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _IP, ctypes.c_int,
                                      _IP, ctypes.c_int, ctypes.c_int, _FP, _FP, ctypes.c_int, _LP, _IP]
+        g.refgpu_tet_blocks.restype = ctypes.c_int
+        g.refgpu_tet_blocks.argtypes = [ctypes.c_char_p, _FP, ctypes.c_int, _FP]
         g.refgpu_tri_blocks.restype = ctypes.c_int
         g.refgpu_tri_blocks.argtypes = [ctypes.c_char_p, _FP, ctypes.c_int, ctypes.c_int, _FP]
         g.refgpu_solve2d.restype = ctypes.c_int
@@ -273,6 +275,17 @@ def ref_gpu_tet_local_solver(inputs9):
     out = np.empty(a.shape[0], dtype=np.float32)
     _gpu_check(ref_gpu().refgpu_tet_local_solver(CUBIN3D.encode(), a.ctypes.data_as(_FP), out.ctypes.data_as(_FP),
                                                  a.shape[0]))
+    return out
+
+
+def ref_gpu_tet_blocks(inputs10):
+    """Single-tet blocks through the reference's 3D FIMCuda, one sweep; inputs
+    TA TB TC TD and the six metric edge products; returns the four vertex values
+    (each min(T_k, the update of apex k) as FIMCuda computes it)."""
+    a = _f(inputs10).reshape(-1, 10)
+    out = np.empty((a.shape[0], 4), dtype=np.float32)
+    _gpu_check(ref_gpu().refgpu_tet_blocks(CUBIN3D.encode(), a.ctypes.data_as(_FP), a.shape[0],
+                                           out.ctypes.data_as(_FP)))
     return out
 
 

@@ -345,6 +345,52 @@ int refgpu_solve2d(const char* cubin2d, int nv, const float* xyz, int nf, const 
 // slot + 2 empty slots); one launch of the reference's 2D FIMCuda (7 sweeps, check
 // = 0) or run_check_neighbor (1 sweep, check = 1).  in: T0 T1 T2 e01 e12 e20
 // speedInv per case; out: the three vertex values the kernel writes back.
+// Single-tet blocks through the reference's 3D FIMCuda with one sweep
+// (CUDA_kernels.cu:383-489): block b holds one tet in slot 0 (three padding slots
+// at LARGENUM) whose four corners are the block's vertices, so vertex k of block b
+// ends at min(T_k, localSolverTet1 of apex k) as FIMCuda's four inlined updates
+// compute it.  in: 10 floats per block (TA TB TC TD, then the six metric edge
+// products ACBC BCCD ACCD ADBD ACAD BCBD); out: 4 floats per block.
+int refgpu_tet_blocks(const char* cubin3d, const float* in, int n, float* out) {
+  TRY(load(g_lib3, cubin3d));
+  cudaKernel_t kfim;
+  TRY(kernel(g_lib3, "ref3d_fim", &kfim));
+  const int maxT = 4, maxIn = 4, mapIn = 1, mapOut = 1;
+  const size_t nslot = (size_t)n * maxT;
+  std::vector<float> m0(3 * nslot, 0.f), m1(3 * nslot, 0.f), tT(4 * nslot, (float)kLarge3D);
+  std::vector<int> vm((size_t)n * maxIn), vmo((size_t)n * maxIn, -1), bs(n, 4), al(n);
+  for (int b = 0; b < n; ++b) {
+    const float* c = in + 10 * (size_t)b;
+    const size_t s0 = (size_t)b * maxT;
+    for (int k = 0; k < 4; ++k) tT[4 * s0 + k] = c[k];
+    for (int k = 0; k < 3; ++k) {
+      m0[3 * s0 + k] = c[4 + k];
+      m1[3 * s0 + k] = c[7 + k];
+    }
+    for (int k = 0; k < 4; ++k) vm[(size_t)b * maxIn + k] = (int)(4 * s0) + k;
+    al[b] = b;
+  }
+  DBuf<float> d_m0, d_m1, d_tT, d_vT, d_sp;
+  DBuf<int> d_vm, d_vmo, d_bs, d_al;
+  DBuf<char> d_con;
+  TRY(d_m0.alloc(3 * nslot)); TRY(d_m1.alloc(3 * nslot)); TRY(d_tT.alloc(4 * nslot));
+  TRY(d_vT.alloc((size_t)n * maxIn)); TRY(d_sp.alloc(nslot)); TRY(d_vm.alloc(vm.size()));
+  TRY(d_vmo.alloc(vmo.size())); TRY(d_bs.alloc(n)); TRY(d_al.alloc(n)); TRY(d_con.alloc((size_t)n * maxIn));
+  TRY(d_m0.put(m0.data(), m0.size())); TRY(d_m1.put(m1.data(), m1.size())); TRY(d_tT.put(tT.data(), tT.size()));
+  TRY(d_vm.put(vm.data(), vm.size())); TRY(d_vmo.put(vmo.data(), vmo.size())); TRY(d_bs.put(bs.data(), n));
+  TRY(d_al.put(al.data(), n));
+  float3* pm0 = (float3*)d_m0.p; float3* pm1 = (float3*)d_m1.p; float4* ptT = (float4*)d_tT.p;
+  float* pvT = d_vT.p; float* psp = d_sp.p; int* pvm = d_vm.p; int* pvmo = d_vmo.p; int* pbs = d_bs.p;
+  bool* pcon = (bool*)d_con.p; int* pal = d_al.p;
+  int mI = maxIn, mpI = mapIn, mpO = mapOut, nIter = 1;
+  void* a_fim[] = {&pm0, &pm1, &ptT, &pvT, &psp, &pvm, &pvmo, &pbs, &pcon, &pal, &mI, &mpI, &mpO, &nIter};
+  const size_t smem = 16 * (size_t)maxT + 4 * (size_t)maxIn * mapIn;
+  TRY(launch(kfim, n, maxT, smem, a_fim));
+  RCK(cudaDeviceSynchronize());
+  TRY(d_vT.get(out, (size_t)n * maxIn));
+  return 0;
+}
+
 int refgpu_tri_blocks(const char* cubin2d, const float* in, int n, int check, float* out) {
   TRY(load(g_lib2, cubin2d));
   cudaKernel_t kfim, kchk;
