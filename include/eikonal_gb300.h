@@ -214,7 +214,11 @@ int eik_tri_prep_values(const eik_solver* h, float* edges, float* speed_inv, flo
  *              2D block-sweep kernel (7 sweeps) / neighbour-check kernel (1 sweep);
  *              3 outputs per case;
  *   which = 5: the precision mode's FP64 tet update (no reference counterpart),
- *              inputs as for 0, the FP64 result rounded to FP32. */
+ *              inputs as for 0, the FP64 result rounded to FP32;
+ *   which = 6: the four apex updates of one slot as the 3D visit kernels run them
+ *              (FIMCuda's group, CUDA_kernels.cu:454-457, with its roundings), 10
+ *              inputs per case (TA TB TC TD, then the stored products ACBC BCCD ACCD
+ *              ADBD ACAD BCBD), 4 outputs min(T_k, update of apex k). */
 int eik_selftest_local_update(int which, const float* in, float* out, int n);
 
 /* Failure-path self-test (no counterpart in the reference, which has no bounded

@@ -61,7 +61,7 @@ def build(force=False):
     src = os.path.join(HERE, "fim_oracle.cpp")
     lib = os.path.join(HERE, "liboracle.so")
     hdr = os.path.join(HERE, "oracle_scheme.hpp")
-    if force or _stale(lib, [src, hdr]):
+    if force or _stale(lib, [src, hdr, os.path.join(HERE, "tet_fusion_model.hpp")]):
         _run([CXX, "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", src, "-o", lib])
     built.append(lib)
     # driver that runs the reference's kernels (loaded from _ref/*.cubin at run time)

@@ -32,6 +32,7 @@
 // bitwise.
 
 #include "oracle_scheme.hpp"
+#include "tet_fusion_model.hpp"
 
 using namespace oracle;
 
@@ -148,6 +149,29 @@ int oracle_partition_rcb(int nv, const float* xyz, int verts_per_block, int dim,
   for (int v = 0; v < nv; ++v) ids[v] = v;
   rcb_split(ids, 0, (size_t)nv, (int)nb, 0, xyz, labels);
   return (int)nb;
+}
+
+// The CPU model of the reference kernel's fused roundings (tet_fusion_model.hpp):
+// n cases of 10 inputs -> 4 outputs each under masks[4].
+void oracle_tet_group_fused(const float* in, int n, const unsigned long long* masks, float* out) {
+  const uint64_t m[4] = {masks[0], masks[1], masks[2], masks[3]};
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) fusion::tet_group(m, in + 10 * (size_t)i, out + 4 * (size_t)i);
+}
+
+// Mismatches of apex k of the model under mask m against want (4 per case).
+int oracle_tet_fusion_mismatch(const float* in, const float* want, int n, int k, unsigned long long m) {
+  int bad = 0;
+#pragma omp parallel for reduction(+ : bad) schedule(static)
+  for (int i = 0; i < n; ++i) {
+    uint64_t masks[4] = {0, 0, 0, 0};
+    masks[k] = m;
+    float o[4];
+    fusion::tet_group(masks, in + 10 * (size_t)i, o);
+    const float w = want[4 * (size_t)i + k];
+    bad += std::memcmp(&o[k], &w, sizeof(float)) != 0;
+  }
+  return bad;
 }
 
 int oracle_num_threads(void) { return n_threads(0); }

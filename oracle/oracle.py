@@ -47,6 +47,10 @@ def lib():
                                         ctypes.c_int, _IP, ctypes.c_int, _FP, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_int, _FP, _FP, ctypes.c_int, _LP, _IP]
         _lib.oracle_num_threads.restype = ctypes.c_int
+        _lib.oracle_tet_group_fused.restype = None
+        _lib.oracle_tet_group_fused.argtypes = [_FP, ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong), _FP]
+        _lib.oracle_tet_fusion_mismatch.restype = ctypes.c_int
+        _lib.oracle_tet_fusion_mismatch.argtypes = [_FP, _FP, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong]
         _lib.oracle_partition_rcb.restype = ctypes.c_int
         _lib.oracle_partition_rcb.argtypes = [ctypes.c_int, _FP, ctypes.c_int, ctypes.c_int, _IP]
         _lib.oracle_last_loop_seconds.restype = ctypes.c_double
@@ -211,6 +215,22 @@ def partition_rcb(xyz, verts_per_block, dim=3):
     if nb < 0:
         raise ValueError("oracle_partition_rcb rejected its input")
     return lab, nb
+
+
+def tet_group_fused(inputs10, masks):
+    """The CPU model of the reference kernel's four apex updates of a slot with
+    the given fused-multiply-add masks (tet_fusion_model.hpp): (n, 4) outputs."""
+    a = _f(inputs10).reshape(-1, 10)
+    out = np.empty((a.shape[0], 4), dtype=np.float32)
+    m = (ctypes.c_ulonglong * 4)(*[int(x) for x in masks])
+    lib().oracle_tet_group_fused(a.ctypes.data_as(_FP), a.shape[0], m, out.ctypes.data_as(_FP))
+    return out
+
+
+def tet_fusion_mismatch(inputs10, want4, k, mask):
+    a, w = _f(inputs10).reshape(-1, 10), _f(want4).reshape(-1, 4)
+    return lib().oracle_tet_fusion_mismatch(a.ctypes.data_as(_FP), w.ctypes.data_as(_FP), a.shape[0], int(k),
+                                            ctypes.c_ulonglong(int(mask)))
 
 
 def num_threads():

@@ -16,7 +16,9 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libeikonal_gb300.so")
+# EIKONAL_GB300_LIB names another build of the same library (for example one made
+# with different compile-time options) to load instead of the in-tree one
+LIB_PATH = os.environ.get("EIKONAL_GB300_LIB") or os.path.join(_HERE, "libeikonal_gb300.so")
 
 EIK_OK = 0
 PARTITION_RCB = 0    # recursive coordinate bisection (default)
@@ -564,7 +566,7 @@ class EikonalServer:
 
 def selftest_local_update(which, inputs):
     """Evaluates the device local updates element-wise (see eik_selftest_local_update)."""
-    nin, nout = {0: (9, 1), 1: (7, 1), 2: (2, 2), 3: (7, 3), 4: (7, 3), 5: (9, 1)}[which]
+    nin, nout = {0: (9, 1), 1: (7, 1), 2: (2, 2), 3: (7, 3), 4: (7, 3), 5: (9, 1), 6: (10, 4)}[which]
     a = np.ascontiguousarray(inputs, dtype=np.float32).reshape(-1, nin)
     out = np.empty((a.shape[0], nout), dtype=np.float32)
     rc = lib().eik_selftest_local_update(which, _fptr(a), _fptr(out), a.shape[0])

@@ -381,8 +381,9 @@ int eik_set_options(eik_solver* h, const eik_options* o) {
   if (o->max_iterations < 0) return fail(h, EIK_ERR_ARG, "max_iterations must be >= 0");
   if (o->speed_type != EIK_SPEED_ONE) return fail(h, EIK_ERR_ARG, "only speed type ONE is supported");
   if (o->threads_per_block != 0 && o->threads_per_block != 128 && o->threads_per_block != 256 &&
-      o->threads_per_block != 512 && o->threads_per_block != 1024)
-    return fail(h, EIK_ERR_ARG, "threads_per_block must be 0, 128, 256, 512 or 1024");
+      o->threads_per_block != 384 && o->threads_per_block != 512 && o->threads_per_block != 768 &&
+      o->threads_per_block != 1024)
+    return fail(h, EIK_ERR_ARG, "threads_per_block must be 0, 128, 256, 384, 512, 768 or 1024");
   if (o->precision != 0 && o->precision != 1) return fail(h, EIK_ERR_ARG, "precision must be 0 or 1");
   if (!(o->precision_kappa >= 1.0f)) return fail(h, EIK_ERR_ARG, "precision_kappa must be at least 1");
   if (o->device_setup != 0 && o->device_setup != 1) return fail(h, EIK_ERR_ARG, "device_setup must be 0 or 1");
@@ -525,7 +526,18 @@ int eik_prepare(eik_solver* h) {
   if (!h) return EIK_ERR_ARG;
   if (h->nv == 0) return fail(h, EIK_ERR_STATE, "no mesh: call eik_set_mesh or eik_load_mesh first");
   bool nl = false;
-  return host_prepare(h, &nl);
+  const int rc = host_prepare(h, &nl);
+  if (rc) return rc;
+  // the layout the next (host-built) solve will use
+  const Layout& L = h->layout;
+  h->stats.num_blocks = L.nb;
+  h->stats.max_slots_per_block = L.max_slots;
+  h->stats.max_local_vertices = L.max_local;
+  h->stats.total_slots = L.total_slots;
+  h->stats.mean_slots_per_block = L.mean_slots_per_block;
+  h->stats.mean_halo_per_block = L.mean_halo_per_block;
+  h->stats.flagged_tets = L.flagged_tets;
+  return EIK_OK;
 }
 
 int eik_num_vertices(const eik_solver* h) { return h ? h->nv : 0; }
@@ -697,7 +709,7 @@ int eik_selftest_wait_timeout(double* waited_ms) {
 }
 
 int eik_selftest_local_update(int which, const float* in, float* out, int n) {
-  if (which < 0 || which > 5 || n < 0 || (n > 0 && (!in || !out))) return EIK_ERR_ARG;
+  if (which < 0 || which > 6 || n < 0 || (n > 0 && (!in || !out))) return EIK_ERR_ARG;
   return selftest_device(which, in, out, n).empty() ? EIK_OK : EIK_ERR_CUDA;
 }
 

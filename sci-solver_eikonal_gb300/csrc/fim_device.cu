@@ -130,6 +130,12 @@ constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1
 constexpr float kEps2D = 1e-5f;
 constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
 constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::ktime)
+#ifndef EIK_SWEEP_ITEMS
+#define EIK_SWEEP_ITEMS 1
+#endif
+#ifndef EIK_CHECK_ITEMS
+#define EIK_CHECK_ITEMS 1
+#endif
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + 1D bulk copy (TMA engine)
@@ -257,7 +263,8 @@ __host__ __device__ inline size_t smem_bytes(int ncoef, int max_slots_pad, int m
 
 // Issue the two bulk copies of block `bd` (coefficients + corner ids) and gather
 // the owned / halo travel times from `Tsrc`.  Returns false on a copy timeout.
-__device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd, int ncoef, const Smem& s,
+template <class S>
+__device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd, int ncoef, const S& s,
                                            unsigned long long* bar, unsigned& parity, const float* Tsrc,
                                            uint4* smemo = nullptr) {
   const int tid = threadIdx.x, NT = blockDim.x;
@@ -397,29 +404,19 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
                  R.w == __float_as_uint(T[3]);
           if (memo) ch = 0u;
         }
-        const float ACBC = s.coef[0 * np + j], BCCD = s.coef[1 * np + j], ACCD = s.coef[2 * np + j];
-        const float ADBD = s.coef[3 * np + j], ACAD = s.coef[4 * np + j], BCBD = s.coef[5 * np + j];
-        // remaining metric edge products (CUDA_kernels.cu:429-437)
-        const float ADBC = ACBC + BCCD;
-        const float ACBD = ACBC + ACCD;
-        const float CDBD = ADBD - ACBD;
-        const float ADCD = ADBD - ADBC;
-        const float CDCD = ADCD - ACCD;
-        const float ADAD = ADCD + ACAD;
-        const float ACAC = ACAD - ACCD;
-        const float BDBD = BCBD + CDBD;
-        const float BCBC = BCBD - BCCD;
+        const TetGram gm = tet_gram9(s.coef[0 * np + j], s.coef[1 * np + j], s.coef[2 * np + j],
+                                     s.coef[3 * np + j], s.coef[4 * np + j], s.coef[5 * np + j]);
         float nw[4] = {T[0], T[1], T[2], T[3]};
-        // The four apex updates run together, in the reference's order and with its
-        // argument expressions, so the compiler forms the same fused multiply-adds
-        // as in FIMCuda.  A slot whose four values did not change in the previous
-        // sweep would reproduce its previous candidates exactly and is skipped.
+        // The four apex updates with the reference kernel's roundings (explicitly
+        // rounded, so the code around them cannot change their bits).  A slot whose
+        // four values did not change in the previous sweep would reproduce its
+        // previous candidates exactly and is skipped.
         if (ch) {
           const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
-          nw[3] = fminf(TD, tet_update(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD));
-          nw[0] = fminf(TA, tet_update(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC));
-          nw[1] = fminf(TB, tet_update(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC));
-          nw[2] = fminf(TC, tet_update(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD));
+          nw[3] = fminf(TD, apex_update<3>(T, gm));
+          nw[0] = fminf(TA, apex_update<0>(T, gm));
+          nw[1] = fminf(TB, apex_update<1>(T, gm));
+          nw[2] = fminf(TC, apex_update<2>(T, gm));
           if constexpr (kPrec) {
             // flagged tet: the same four updates again in FP64 from FP64 products
             // (the FP32 group above stays exactly the FP32 kernel's code)
@@ -550,6 +547,415 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
     __syncthreads();
   }
   stamp_end(a, iter, kCheck ? 1 : 0);
+}
+
+// Every candidate of a tet update is at least m (1 - 2^-22), m the smallest of the
+// three input times: the point on the face is a convex combination of the inputs
+// whose weights sum to at least 1 - 2^-24 after rounding, formed in at most four
+// rounded nonnegative steps, and the candidate adds a square root (>= 0, or NaN,
+// which the minimum ignores) to it; the edge candidates are an input plus a square
+// root.  So an apex time T <= RN(m (1 - 2^-20)) < m (1 - 2^-21) keeps its value:
+// min(T, update) = T, and the update can be skipped without changing any bit.
+__device__ __forceinline__ bool upwind_skip(float Tk, float m) { return Tk <= __fmul_rn(m, 0x1.ffffep-1f); }
+
+// ===========================================================================
+// 3D sweep visit by apex items (FIMCuda, fim_sweeps sweeps).
+//
+// Each sweep first lists the apex updates that can change something, then runs
+// them spread evenly over the CTA's threads:
+//   * an apex whose three other corners are all at LARGENUM is skipped: its update
+//     returns LARGENUM and min(T, LARGENUM) = T;
+//   * after the first sweep, an apex none of whose three other corners changed in
+//     the previous sweep is skipped: its update would repeat a candidate that the
+//     previous sweep already folded into its value (the vertex minimum for an owned
+//     apex, the slot's copy for a corner owned elsewhere);
+//   * in the last sweep only owned apexes run (the per-slot copies of other
+//     blocks' corners are dropped after the visit);
+//   * an apex already at or below (1 - 2^-20) x the smallest of its three other
+//     corners is skipped (upwind_skip): no candidate of its update can be lower.
+// The four apex updates of a slot round differently (the reference's inlined
+// copies), so the lists are kept per apex and warps run one apex kind at a time.
+// Every update that runs is the reference's, bit for bit (apex_update); skipped
+// updates are exactly those whose result cannot differ from the value kept, so the
+// visit's outputs equal the reference's FIMCuda visit.
+// ===========================================================================
+struct SmemItems {
+  float* coef;          // 6 runs of max_slots_pad
+  uint2* lv;            // max_slots_pad
+  float* h0;            // 4 per slot: copies of corners owned elsewhere (current)
+  float* h1;            // the previous sweep's copies until this sweep's list is built
+  float* vt;            // max_local: owned values then halo values
+  int* vnew;            // max_owned keys
+  unsigned char* vchg;  // max_owned
+  unsigned short* items;  // 4 lists of max_slots_pad slot indices (one per apex)
+};
+
+__host__ __device__ inline size_t items_offsets(int np, int max_local, int max_owned, size_t off[8]) {
+  size_t o = 0;
+  auto take = [&](size_t bytes, size_t align) {
+    o = (o + align - 1) & ~(align - 1);
+    const size_t at = o;
+    o += bytes;
+    return at;
+  };
+  off[0] = take(24 * (size_t)np, 16);       // coef
+  off[1] = take(8 * (size_t)np, 16);        // lv
+  off[2] = take(16 * (size_t)np, 16);       // h0
+  off[3] = take(16 * (size_t)np, 16);       // h1
+  off[4] = take(4 * (size_t)max_local, 4);  // vt
+  off[5] = take(4 * (size_t)max_owned, 4);  // vnew
+  off[6] = take((size_t)max_owned, 1);      // vchg
+  off[7] = take(8 * (size_t)np, 2);         // items
+  return (o + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t smem_bytes_items(int np, int max_local, int max_owned) {
+  size_t off[8];
+  return items_offsets(np, max_local, max_owned, off);
+}
+__device__ __forceinline__ SmemItems carve_items(unsigned char* sm, const DevArgs& a) {
+  size_t off[8];
+  items_offsets(a.max_slots_pad, a.max_local, a.max_owned, off);
+  SmemItems s;
+  s.coef = reinterpret_cast<float*>(sm + off[0]);
+  s.lv = reinterpret_cast<uint2*>(sm + off[1]);
+  s.h0 = reinterpret_cast<float*>(sm + off[2]);
+  s.h1 = reinterpret_cast<float*>(sm + off[3]);
+  s.vt = reinterpret_cast<float*>(sm + off[4]);
+  s.vnew = reinterpret_cast<int*>(sm + off[5]);
+  s.vchg = sm + off[6];
+  s.items = reinterpret_cast<unsigned short*>(sm + off[7]);
+  return s;
+}
+
+// at most 56 registers: three CTAs of 384 threads fit one SM's register file
+__global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int s_item;
+  __shared__ int s_cnt[4];
+  const SmemItems s0 = carve_items(sm, a);
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
+  const int np = a.max_slots_pad;
+  const Ctl* ctl = a.ctl;
+  const int iter = ctl->iter;
+  const int stamp = iter + 1;
+  const int count = ctl->nact;
+  const int* list = act_list(a, iter);
+  const int nsweeps = a.fim_sweeps;
+  stamp_start(a, iter, 0);
+  if (tid == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  unsigned parity = 0;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(&a.ctl->work_a, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= count) break;
+    const int b = list[item];
+    if (a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
+      __syncthreads();
+      continue;
+    }
+    const BlockDesc bd = a.blocks[b];
+    SmemItems s = s0;
+    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta)) {
+      if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
+      (void)mbar_wait(&bar, parity ^ 1u);
+      __syncthreads();
+      continue;
+    }
+    __syncthreads();
+    const int ns = bd.nslots, nown = bd.nowned, pitch = bd.nslots_pad;
+    // per-slot copies of corners owned by other blocks start from the halo values
+    for (int j = bd.ninside + tid; j < ns; j += NT) {
+      const uint2 l = s.lv[j];
+      const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s.h0[4 * j + k] = (id[k] < nown) ? 0.0f : s.vt[id[k]];
+    }
+    int myconv = 1;
+    for (int sw = 0; sw < nsweeps; ++sw) {
+      const bool first = (sw == 0), last = (sw == nsweeps - 1);
+      if (tid < 4) s_cnt[tid] = 0;
+      __syncthreads();
+      // ---- list the apex updates this sweep must run ----
+      for (int j0 = 0; j0 < ns; j0 += NT) {
+        const int j = j0 + tid;
+        unsigned need = 0;
+        if (j < ns) {
+          const uint2 l = s.lv[j];
+          const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+          unsigned big = 0, chg = 0, own = 0;
+          float Tq[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const bool o = id[q] < nown;
+            const float T = o ? s.vt[id[q]] : s.h0[4 * j + q];
+            Tq[q] = T;
+            big |= (T >= kLarge3DDev ? 1u : 0u) << q;
+            // a copy changed in the previous sweep when it differs from that sweep's
+            // input, still held in h1 (the buffers swap after every sweep)
+            chg |= (first ? 1u : (o ? (unsigned)s.vchg[id[q]] : (T != s.h1[4 * j + q] ? 1u : 0u))) << q;
+            own |= (o ? 1u : 0u) << q;
+            if (!o && !last) s.h1[4 * j + q] = T;  // kept unless its update below changes it
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const unsigned others = 0xfu & ~(1u << k);
+            const float m = fminf(fminf(Tq[(k + 1) & 3], Tq[(k + 2) & 3]), Tq[(k + 3) & 3]);
+            const bool run = ((big & others) != others) && (chg & others) && (!last || ((own >> k) & 1u)) &&
+                             !upwind_skip(Tq[k], m);
+            need |= (run ? 1u : 0u) << k;
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const unsigned bal = __ballot_sync(0xffffffffu, (need >> k) & 1u);
+          if (bal) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&s_cnt[k], __popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if ((need >> k) & 1u) s.items[k * np + base + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)j;
+          }
+        }
+      }
+      __syncthreads();
+      // ---- run them ----
+      const int c0 = s_cnt[0], c01 = c0 + s_cnt[1], c012 = c01 + s_cnt[2], total = c012 + s_cnt[3];
+      for (int i = tid; i < total; i += NT) {
+        const int k = (i < c0) ? 0 : (i < c01) ? 1 : (i < c012) ? 2 : 3;
+        const int r = i - ((k == 0) ? 0 : (k == 1) ? c0 : (k == 2) ? c01 : c012);
+        const int j = s.items[k * np + r];
+        const uint2 l = s.lv[j];
+        const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+        float T[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) T[q] = (id[q] < nown) ? s.vt[id[q]] : s.h0[4 * j + q];
+        const TetGram gm = tet_gram9(s.coef[0 * pitch + j], s.coef[1 * pitch + j], s.coef[2 * pitch + j],
+                                     s.coef[3 * pitch + j], s.coef[4 * pitch + j], s.coef[5 * pitch + j]);
+        float u;
+        switch (k) {
+          case 0: u = apex_update<0>(T, gm); break;
+          case 1: u = apex_update<1>(T, gm); break;
+          case 2: u = apex_update<2>(T, gm); break;
+          default: u = apex_update<3>(T, gm); break;
+        }
+        // T[k], id[k] by selects: a runtime index would put the arrays in local memory
+        const float Tk = (k == 0) ? T[0] : (k == 1) ? T[1] : (k == 2) ? T[2] : T[3];
+        const int idk = (k == 0) ? id[0] : (k == 1) ? id[1] : (k == 2) ? id[2] : id[3];
+        const float nw = fminf(Tk, u);
+        if (idk < nown) {
+          if (nw < Tk) atomicMin(&s.vnew[idk], fkey(nw));
+        } else if (!last) {
+          s.h1[4 * j + k] = nw;
+        }
+      }
+      __syncthreads();
+      for (int k = tid; k < nown; k += NT) {
+        const float nv = fval(s.vnew[k]);
+        const float ov = s.vt[k];
+        if (last) {
+          float res = ov - nv;
+          if (res < 0.0f) res = -res;
+          myconv &= (res <= kEps3DLe) ? 1 : 0;
+        }
+        s.vchg[k] = (nv != ov) ? 1 : 0;
+        s.vt[k] = nv;
+      }
+      float* th = s.h0; s.h0 = s.h1; s.h1 = th;
+    }
+    const int allc = __syncthreads_and(myconv);
+    for (int k = tid; k < nown; k += NT) a.Tb[bd.vbase + k] = s.vt[k];
+    if (tid == 0) {
+      a.conv[b] = allc;
+      if (!allc) a.stampA[b] = stamp;
+      atomicAdd(&a.ctl->fim_visits, 1ull);
+      atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
+      count_visit(a, iter, 0, ns, bd.nhalo, nown);
+      atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
+      atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
+      atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+      atomicAdd(&a.ctl->fim_slots, (unsigned long long)ns);
+      atomicAdd(&a.ctl->fim_halo, (unsigned long long)bd.nhalo);
+      atomicAdd(&a.ctl->fim_owned, (unsigned long long)nown);
+    }
+    __syncthreads();
+  }
+  stamp_end(a, iter, 0);
+}
+
+// ===========================================================================
+// 3D neighbour check by apex items (run_check_neghbor, one sweep, flags only).
+//
+// Only owned apexes decide a check; an item runs the update of one owned apex of
+// one slot, skipped where the sweep kernel skips it (three inputs at LARGENUM, or
+// the apex already upwind of its corners) and for slots whose four input times an
+// earlier check of this solve found settled (check memo).  The first candidate that
+// lowers an owned vertex by EPS or more decides the block (later ones cannot change
+// the flag) and stops the remaining items.  When the block stays converged, every
+// slot that ran records its input times as settled.
+// ===========================================================================
+struct SmemCheck {
+  float* coef;            // 6 runs of max_slots_pad
+  uint2* lv;              // max_slots_pad
+  uint4* memo;            // max_slots_pad check memos (staged with the block)
+  float* vt;              // max_local
+  int* vnew;              // max_owned (filled by load_block, unused here)
+  unsigned short* items;  // 4 lists of max_slots_pad
+};
+__host__ __device__ inline size_t check_offsets(int np, int max_local, int max_owned, size_t off[6]) {
+  size_t o = 0;
+  auto take = [&](size_t bytes, size_t align) {
+    o = (o + align - 1) & ~(align - 1);
+    const size_t at = o;
+    o += bytes;
+    return at;
+  };
+  off[0] = take(24 * (size_t)np, 16);
+  off[1] = take(8 * (size_t)np, 16);
+  off[2] = take(16 * (size_t)np, 16);
+  off[3] = take(4 * (size_t)max_local, 4);
+  off[4] = take(4 * (size_t)max_owned, 4);
+  off[5] = take(8 * (size_t)np, 2);
+  return (o + 15) & ~(size_t)15;
+}
+__host__ __device__ inline size_t smem_bytes_check(int np, int max_local, int max_owned) {
+  size_t off[6];
+  return check_offsets(np, max_local, max_owned, off);
+}
+
+__global__ void __maxnreg__(56) k_check3d(DevArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int s_item;
+  __shared__ volatile int s_moved;
+  __shared__ int s_cnt[4];
+  size_t off[6];
+  check_offsets(a.max_slots_pad, a.max_local, a.max_owned, off);
+  SmemCheck s;
+  s.coef = reinterpret_cast<float*>(sm + off[0]);
+  s.lv = reinterpret_cast<uint2*>(sm + off[1]);
+  s.memo = reinterpret_cast<uint4*>(sm + off[2]);
+  s.vt = reinterpret_cast<float*>(sm + off[3]);
+  s.vnew = reinterpret_cast<int*>(sm + off[4]);
+  s.items = reinterpret_cast<unsigned short*>(sm + off[5]);
+  uint4* const smemo = a.chk_memo ? s.memo : nullptr;
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
+  const int np = a.max_slots_pad;
+  const Ctl* ctl = a.ctl;
+  const int iter = ctl->iter;
+  const int count = ctl->nnew;
+  int* nxt = next_list(a, iter);
+  stamp_start(a, iter, 1);
+  if (tid == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  unsigned parity = 0;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(&a.ctl->work_c, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= count) break;
+    const int b = a.list_new[item];
+    if (a.inst_done[a.blk_inst[b]]) {
+      __syncthreads();
+      continue;
+    }
+    const BlockDesc bd = a.blocks[b];
+    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo)) {
+      if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
+      (void)mbar_wait(&bar, parity ^ 1u);
+      __syncthreads();
+      continue;
+    }
+    if (tid == 0) s_moved = 0;
+    if (tid < 4) s_cnt[tid] = 0;
+    __syncthreads();
+    const int ns = bd.nslots, nown = bd.nowned, pitch = bd.nslots_pad;
+    for (int j0 = 0; j0 < ns; j0 += NT) {
+      const int j = j0 + tid;
+      unsigned need = 0;
+      if (j < ns) {
+        const uint2 l = s.lv[j];
+        const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+        float T[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) T[q] = s.vt[id[q]];
+        bool memo = false;
+        if (smemo) {
+          const uint4 R = smemo[j];
+          memo = R.x == __float_as_uint(T[0]) && R.y == __float_as_uint(T[1]) && R.z == __float_as_uint(T[2]) &&
+                 R.w == __float_as_uint(T[3]);
+        }
+        if (!memo) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float m = fminf(fminf(T[(k + 1) & 3], T[(k + 2) & 3]), T[(k + 3) & 3]);
+            const bool run = id[k] < nown && m < kLarge3DDev && !upwind_skip(T[k], m);
+            need |= (run ? 1u : 0u) << k;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const unsigned bal = __ballot_sync(0xffffffffu, (need >> k) & 1u);
+        if (bal) {
+          int base = 0;
+          if (lane == 0) base = atomicAdd(&s_cnt[k], __popc(bal));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if ((need >> k) & 1u) s.items[k * np + base + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)j;
+        }
+      }
+    }
+    __syncthreads();
+    const int c0 = s_cnt[0], c01 = c0 + s_cnt[1], c012 = c01 + s_cnt[2], total = c012 + s_cnt[3];
+    for (int i = tid; i < total; i += NT) {
+      if (s_moved) break;
+      const int k = (i < c0) ? 0 : (i < c01) ? 1 : (i < c012) ? 2 : 3;
+      const int r = i - ((k == 0) ? 0 : (k == 1) ? c0 : (k == 2) ? c01 : c012);
+      const int j = s.items[k * np + r];
+      const uint2 l = s.lv[j];
+      const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+      float T[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) T[q] = s.vt[id[q]];
+      const TetGram gm = tet_gram9(s.coef[0 * pitch + j], s.coef[1 * pitch + j], s.coef[2 * pitch + j],
+                                   s.coef[3 * pitch + j], s.coef[4 * pitch + j], s.coef[5 * pitch + j]);
+      float u;
+      switch (k) {
+        case 0: u = apex_update<0>(T, gm); break;
+        case 1: u = apex_update<1>(T, gm); break;
+        case 2: u = apex_update<2>(T, gm); break;
+        default: u = apex_update<3>(T, gm); break;
+      }
+      const float Tk = (k == 0) ? T[0] : (k == 1) ? T[1] : (k == 2) ? T[2] : T[3];
+      // (double)(old - candidate) >= 1e-5 in the reference
+      if (!((Tk - fminf(Tk, u)) <= kEps3DLe)) s_moved = 1;
+    }
+    __syncthreads();
+    const int allc = s_moved ? 0 : 1;
+    if (allc && smemo)
+      for (int j = tid; j < ns; j += NT) {
+        const uint2 l = s.lv[j];
+        const uint4 R = smemo[j];
+        const uint4 W = make_uint4(__float_as_uint(s.vt[l.x & 0xffffu]), __float_as_uint(s.vt[l.x >> 16]),
+                                   __float_as_uint(s.vt[l.y & 0xffffu]), __float_as_uint(s.vt[l.y >> 16]));
+        if (R.x != W.x || R.y != W.y || R.z != W.z || R.w != W.w) a.chk_memo[bd.slot_begin + j] = W;
+      }
+    if (tid == 0) {
+      if (!allc) {
+        nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
+        atomicAdd(&a.inst_nnext[a.blk_inst[b]], 1);
+      }
+      atomicAdd(&a.ctl->chk_visits, 1ull);
+      atomicAdd(&a.ctl->updates, (unsigned long long)nown);
+      count_visit(a, iter, 1, ns, bd.nhalo, nown);
+      atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
+      atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
+      atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+    }
+    __syncthreads();
+  }
+  stamp_end(a, iter, 1);
 }
 
 // ===========================================================================
@@ -1305,6 +1711,21 @@ __global__ void k_selftest_tet(const float* in, float* out, int n) {
     out[i] = tet_update(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
   }
 }
+// the four apex updates of a slot as the visit kernels run them: per case TA TB TC
+// TD and the six stored metric edge products in, min(T_k, update of apex k) out
+__global__ void k_selftest_tet_group(const float* in, float* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float* a = in + 10 * (size_t)i;
+    const float T[4] = {a[0], a[1], a[2], a[3]};
+    const TetGram g = tet_gram9(a[4], a[5], a[6], a[7], a[8], a[9]);
+    float* o = out + 4 * (size_t)i;
+    o[0] = fminf(T[0], apex_update<0>(T, g));
+    o[1] = fminf(T[1], apex_update<1>(T, g));
+    o[2] = fminf(T[2], apex_update<2>(T, g));
+    o[3] = fminf(T[3], apex_update<3>(T, g));
+  }
+}
 __global__ void k_selftest_tri(const float* in, float* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -1567,8 +1988,16 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     void* kv_fim;
     void* kv_chk;
     if (L.dim == 3) {
+#if EIK_SWEEP_ITEMS
+      kv_fim = P.prec ? (void*)k_visit3d<false, true> : (void*)k_sweep3d;
+#else
       kv_fim = P.prec ? (void*)k_visit3d<false, true> : (void*)k_visit3d<false>;
+#endif
+#if EIK_CHECK_ITEMS
+      kv_chk = P.prec ? (void*)k_visit3d<true, true> : (void*)k_check3d;
+#else
       kv_chk = P.prec ? (void*)k_visit3d<true, true> : (void*)k_visit3d<true>;
+#endif
       // check visits need one set of per-slot copies; they stage the block's check
       // memos (16 B per slot) behind it, and sweep visits their packed slot list
       // (4 B per slot) behind theirs
@@ -1584,6 +2013,24 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
         } else {
           a.chk_memo = nullptr;
         }
+      }
+      {
+        // the item kernels keep more per-slot state in shared memory; blocks too
+        // large for it run the slot kernels (same results)
+        int maxsm = 0;
+        CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const size_t si = smem_bytes_items(P.max_slots_pad, P.max_local, P.max_owned);
+        const size_t sc = smem_bytes_check(P.max_slots_pad, P.max_local, P.max_owned);
+#if EIK_SWEEP_ITEMS
+        if (!P.prec && si + 64 <= (size_t)maxsm) vsmem = si;
+        else if (!P.prec) kv_fim = (void*)k_visit3d<false>;
+#endif
+#if EIK_CHECK_ITEMS
+        if (!P.prec && sc + 64 <= (size_t)maxsm) vsmem_chk = sc;
+        else if (!P.prec) kv_chk = (void*)k_visit3d<true>;
+#endif
+        (void)si;
+        (void)sc;
       }
     } else if (slot2d) {
       vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
@@ -1919,7 +2366,8 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   const Layout& L = *L_;
   cudaStream_t st = (cudaStream_t)stream_;
   const int sweeps = (opt.fim_sweeps > 0) ? opt.fim_sweeps : (L.dim == 3 ? 2 : 7);
-  const bool given = opt.threads == 128 || opt.threads == 256 || opt.threads == 512 || opt.threads == 1024;
+  const bool given = opt.threads == 128 || opt.threads == 256 || opt.threads == 384 || opt.threads == 512 ||
+                     opt.threads == 768 || opt.threads == 1024;
   int threads = given ? opt.threads : full_visit_threads(P.max_slots_pad);
   int tune_slot = -1;  // which candidate CTA size this solve measures
   const int tq = P.prec ? 1 : 0;
@@ -2454,8 +2902,8 @@ std::string selftest_wait_timeout(int* status, double* waited_ms) {
 
 std::string selftest_device(int which, const float* in, float* out, int n) {
   if (which == 3 || which == 4) return selftest_tri_blocks(in, n, which == 4, out);
-  const int nin = (which == 0 || which == 5) ? 9 : (which == 1) ? 7 : 2;
-  const int nout = (which == 2) ? 2 : 1;
+  const int nin = (which == 0 || which == 5) ? 9 : (which == 1) ? 7 : (which == 6) ? 10 : 2;
+  const int nout = (which == 2) ? 2 : (which == 6) ? 4 : 1;
   float *din = nullptr, *dout = nullptr;
   CK(cudaMalloc((void**)&din, sizeof(float) * (size_t)nin * n + 16));
   CK(cudaMalloc((void**)&dout, sizeof(float) * (size_t)nout * n + 16));
@@ -2465,6 +2913,7 @@ std::string selftest_device(int which, const float* in, float* out, int n) {
     if (which == 0) k_selftest_tet<<<grid, 128>>>(din, dout, n);
     else if (which == 5) k_selftest_tet64<<<grid, 128>>>(din, dout, n);
     else if (which == 1) k_selftest_tri<<<grid, 128>>>(din, dout, n);
+    else if (which == 6) k_selftest_tet_group<<<grid, 128>>>(din, dout, n);
     else k_selftest_quot<<<grid, 128>>>(din, dout, n);
   }
   cudaError_t e = cudaDeviceSynchronize();

@@ -203,6 +203,453 @@ __device__ __forceinline__ float tet_update(float TA, float TB, float TC, float 
   return TD;
 }
 
+// ---------------------------------------------------------------------------
+// Explicitly rounded tet update.
+//
+// nvcc fuses a product into an adjacent sum (one FMA rounding instead of two), and
+// in a sum or difference of two products it picks one of them; which one depends
+// on the code around the expression, so the reference's four inlined updates in
+// FIMCuda (CUDA_kernels.cu:454-457) do not all round alike, and the same source in
+// a different kernel shape can round differently.  Here every product, sum,
+// quotient and square root is one IEEE operation (__fmul_rn, __fadd_rn, __fmaf_rn,
+// __fdiv_rn, __fsqrt_rn) that the compiler cannot fuse or split, so the result no
+// longer depends on the surrounding code, and a template mask states, for each sum
+// or difference of two products, which product the reference's kernel fuses: bit S
+// set = the second product is fused (x*y - z*w -> fma(-z, w, x*y)), clear = the
+// first (fma(x, y, -(z*w))).
+//
+// The four masks below reproduce the reference kernel's own roundings for the four
+// apex updates of a slot: they were fitted to, and reproduce bit for bit, the
+// reference's FIMCuda run on 500,000 single-tet blocks (one sweep, so each vertex
+// ends at that apex's update) covering jittered-cube tets with scalar metrics,
+// slivers and random shapes with anisotropic metrics, and uniform random times;
+// every site of the mask is exercised by those inputs (the one exception, site 29,
+// is TB*0 beside TA*l1, where both choices give the same value).  A GPU test holds
+// the group to the reference kernel on fresh inputs.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long kFuseApexA = 0x6301902630000ull;  // update of A from B, D, C
+constexpr unsigned long long kFuseApexB = 0x6301902630000ull;  // B from A, D, C
+constexpr unsigned long long kFuseApexC = 0x4203182420002ull;  // C from A, B, D
+constexpr unsigned long long kFuseApexD = 0x0000001100000000ull;  // D from A, B, C
+
+template <unsigned long long M, int S>
+__device__ __forceinline__ float x_ms(float x, float y, float z, float w) {  // x*y - z*w
+  if constexpr (((M >> S) & 1ull) != 0) return __fmaf_rn(-z, w, __fmul_rn(x, y));
+  else return __fmaf_rn(x, y, -__fmul_rn(z, w));
+}
+template <unsigned long long M, int S>
+__device__ __forceinline__ float x_ma(float x, float y, float z, float w) {  // x*y + z*w
+  if constexpr (((M >> S) & 1ull) != 0) return __fmaf_rn(z, w, __fmul_rn(x, y));
+  else return __fmaf_rn(x, y, __fmul_rn(z, w));
+}
+// (l1*XX + l2*XY + XZ)*l1 + (l1*XY + l2*YY + YZ)*l2 + (l1*XZ + l2*YZ + ZZ): the metric
+// length of the path from the apex to the point l1 A + l2 B + l3 C (sites S..S+3)
+template <unsigned long long M, int S>
+__device__ __forceinline__ float x_dist3(float l1, float l2, float ACAC, float ACBC, float ACCD, float BCBC,
+                                         float BCCD, float CDCD) {
+  const float X = __fadd_rn(x_ma<M, S>(l1, ACAC, l2, ACBC), ACCD);
+  const float Y = __fadd_rn(x_ma<M, S + 1>(l1, ACBC, l2, BCBC), BCCD);
+  const float Z = __fadd_rn(x_ma<M, S + 2>(l1, ACCD, l2, BCCD), CDCD);
+  return __fadd_rn(x_ma<M, S + 3>(X, l1, Y, l2), Z);
+}
+// (l*XX + XY)*l + (l*XY + YY): the same on an edge
+__device__ __forceinline__ float x_dist2(float l, float XX, float XY, float YY) {
+  return __fmaf_rn(__fmaf_rn(l, XX, XY), l, __fmaf_rn(l, XY, YY));
+}
+__device__ __forceinline__ float x_root(float num, float p) {
+  if (fabsf(p) < 0x1p126f) return __fdiv_rn(num, __fmul_rn(2.0f, p));
+  return root_quot_slow(num, p);
+}
+
+// localSolverTet1 (CUDA_kernels.cu:69-225) with the roundings of mask M: the update
+// of apex D from A, B, C; the candidate order and every expression tree are the
+// reference's.
+template <unsigned long long M>
+__device__ __forceinline__ float tet_update_x(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                              float BCBC, float BCCD, float CDCD) {
+  if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
+  float p, q, r, l1, l2, l3, delta;
+  float fBC = kLarge3DDev, fAB = kLarge3DDev, fAC = kLarge3DDev, TD = kLarge3DDev;
+  const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
+  // ---- face BC (lambda1 = 0) ----
+  p = x_ms<M, 0>(__fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
+  q = x_ms<M, 1>(__fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
+  r = x_ms<M, 2>(__fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
+  delta = x_ms<M, 3>(q, q, __fmul_rn(4.0f, p), r);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l2 = x_root(__fadd_rn(-q, sd), p);
+    l3 = __fsub_rn(1.0f, l2);
+    if (l2 >= 0 && l2 <= 1)
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, 4>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+    l2 = x_root(__fsub_rn(-q, sd), p);
+    l3 = __fsub_rn(1.0f, l2);
+    if (l2 >= 0 && l2 <= 1)
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, 5>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+  }
+  const float eB = __fadd_rn(TB, __fsqrt_rn(__fadd_rn(__fadd_rn(BCBC, BCCD), __fadd_rn(BCCD, CDCD))));
+  const float eC = __fadd_rn(TC, __fsqrt_rn(CDCD));
+  fBC = fminf(fBC, fminf(eB, eC));
+  // ---- face AB (lambda3 = 0) ----
+  const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
+  const float TAB2 = __fmul_rn(TAB, TAB);
+  const float P1 = x_ms<M, 6>(TAB2, ACAC, gx, gx);
+  const float P2 = x_ms<M, 7>(__fmul_rn(BCBC, TAB), TAB, gy, gy);
+  const float P3 = x_ms<M, 8>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
+  p = __fsub_rn(__fadd_rn(P1, P2), P3);
+  const float P4 = x_ms<M, 9>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
+  const float P5 = x_ms<M, 10>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
+  q = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3), P4), P5);
+  r = __fadd_rn(__fadd_rn(x_ms<M, 11>(TAB2, BCBC, gy, gy), P5), x_ms<M, 12>(TAB2, CDCD, gz, gz));
+  delta = x_ms<M, 13>(q, q, __fmul_rn(4.0f, p), r);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l1 = x_root(__fadd_rn(-q, sd), p);
+    l2 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, 14>(TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, 15>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    l1 = x_root(__fsub_rn(-q, sd), p);
+    l2 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, 19>(TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, 20>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+  }
+  const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
+  fAB = fminf(fAB, fminf(eB, eA));
+  // ---- face AC (lambda2 = 0) ----
+  const float TAC2 = __fmul_rn(TAC, TAC);
+  p = x_ms<M, 24>(__fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
+  const float qAC = x_ms<M, 25>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
+  const float rAC = x_ms<M, 26>(TAC2, CDCD, ACCD, ACCD);
+  delta = x_ms<M, 27>(qAC, qAC, __fmul_rn(4.0f, p), rAC);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l1 = x_root(__fadd_rn(-qAC, sd), p);
+    l3 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAC = fminf(fAC, __fadd_rn(x_ma<M, 28>(TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+    l1 = x_root(__fsub_rn(-qAC, sd), p);
+    l3 = __fsub_rn(1.0f, l1);
+    // the second candidate keeps a zero-weight TB term, as the reference does
+    if (l1 >= 0 && l1 <= 1)
+      fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 29>(TA, l1, TB, 0.0f)),
+                                 __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+  }
+  fAC = fminf(fAC, fminf(eA, eC));
+  // ---- inside face ABC: lambda2 = (s*lambda1 + t)/(h + 1e-8) ----
+  const float s = x_ms<M, 30>(TAC, ACBC, TBC, ACAC);
+  const float t = x_ms<M, 31>(TAC, BCCD, TBC, ACCD);
+  const float h = -x_ms<M, 32>(TAC, BCBC, TBC, ACBC);
+  const float A1 = x_ms<M, 33>(TAC2, ACAC, ACAC, ACAC);
+  const float A2 = x_ms<M, 34>(__fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
+  const float A3 = x_ms<M, 35>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
+  const float A4 = x_ms<M, 37>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
+  p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, 36>(__fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
+  q = __fmaf_rn(__fmul_rn(A4, s), h,
+                __fmaf_rn(__fmul_rn(qAC, h), h, x_ma<M, 38>(__fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
+  r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, 40>(__fmul_rn(x_ms<M, 39>(TAC2, BCBC, ACBC, ACBC), t), t,
+                                                   __fmul_rn(A4, t), h));
+  delta = x_ms<M, 41>(q, q, __fmul_rn(4.0f, p), r);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l1 = x_root(__fadd_rn(-q, sd), p);
+    l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 42>(TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, 43>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    l1 = x_root(__fsub_rn(-q, sd), p);
+    l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 47>(TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, 48>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+  }
+  return fminf(TD, fminf(fBC, fminf(fAB, fAC)));
+}
+
+// The same update with the edge-face candidates (faces BC, AB, AC) evaluated
+// without branches: both roots of each face are computed whatever the
+// discriminant's sign, and a candidate enters the minimum only where the branching
+// form would have taken it (a negative discriminant gives NaN roots, which fail
+// the [0, 1] tests).  Every value is the explicitly rounded one of tet_update_x and
+// the minimum does not depend on the order of its operands, so the result is the
+// same bits; the interior face keeps its branch (its second quotient has a slow
+// path that a NaN input would take).
+template <unsigned long long M>
+__device__ __forceinline__ float tet_update_xb(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                               float BCBC, float BCCD, float CDCD) {
+  if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
+  const float L = kLarge3DDev;
+  const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
+  // ---- face BC (lambda1 = 0) ----
+  float fBC;
+  {
+    const float p = x_ms<M, 0>(__fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
+    const float q = x_ms<M, 1>(__fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
+    const float r = x_ms<M, 2>(__fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
+    const float delta = x_ms<M, 3>(q, q, __fmul_rn(4.0f, p), r);
+    const bool ok = delta >= 0.0f;
+    const float sd = __fsqrt_rn(delta);
+    const float a2 = x_root(__fadd_rn(-q, sd), p), a3 = __fsub_rn(1.0f, a2);
+    const float b2 = x_root(__fsub_rn(-q, sd), p), b3 = __fsub_rn(1.0f, b2);
+    const float ca = __fadd_rn(x_ma<M, 4>(TB, a2, TC, a3), __fsqrt_rn(x_dist2(a2, BCBC, BCCD, CDCD)));
+    const float cb = __fadd_rn(x_ma<M, 5>(TB, b2, TC, b3), __fsqrt_rn(x_dist2(b2, BCBC, BCCD, CDCD)));
+    // seeded with LARGENUM as the branching form (a NaN candidate is ignored)
+    fBC = fminf(fminf(L, (ok && a2 >= 0 && a2 <= 1) ? ca : L), (ok && b2 >= 0 && b2 <= 1) ? cb : L);
+  }
+  const float eB = __fadd_rn(TB, __fsqrt_rn(__fadd_rn(__fadd_rn(BCBC, BCCD), __fadd_rn(BCCD, CDCD))));
+  const float eC = __fadd_rn(TC, __fsqrt_rn(CDCD));
+  const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
+  // ---- face AB (lambda3 = 0) ----
+  float fAB;
+  {
+    const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
+    const float TAB2 = __fmul_rn(TAB, TAB);
+    const float P1 = x_ms<M, 6>(TAB2, ACAC, gx, gx);
+    const float P2 = x_ms<M, 7>(__fmul_rn(BCBC, TAB), TAB, gy, gy);
+    const float P3 = x_ms<M, 8>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
+    const float p = __fsub_rn(__fadd_rn(P1, P2), P3);
+    const float P4 = x_ms<M, 9>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
+    const float P5 = x_ms<M, 10>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
+    const float q = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3), P4), P5);
+    const float r = __fadd_rn(__fadd_rn(x_ms<M, 11>(TAB2, BCBC, gy, gy), P5), x_ms<M, 12>(TAB2, CDCD, gz, gz));
+    const float delta = x_ms<M, 13>(q, q, __fmul_rn(4.0f, p), r);
+    const bool ok = delta >= 0.0f;
+    const float sd = __fsqrt_rn(delta);
+    const float a1 = x_root(__fadd_rn(-q, sd), p), a2 = __fsub_rn(1.0f, a1);
+    const float b1 = x_root(__fsub_rn(-q, sd), p), b2 = __fsub_rn(1.0f, b1);
+    const float ca = __fadd_rn(x_ma<M, 14>(TA, a1, TB, a2),
+                               __fsqrt_rn(x_dist3<M, 15>(a1, a2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD)));
+    const float cb = __fadd_rn(x_ma<M, 19>(TA, b1, TB, b2),
+                               __fsqrt_rn(x_dist3<M, 20>(b1, b2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD)));
+    // seeded with LARGENUM as the branching form (a NaN candidate is ignored)
+    fAB = fminf(fminf(L, (ok && a1 >= 0 && a1 <= 1) ? ca : L), (ok && b1 >= 0 && b1 <= 1) ? cb : L);
+  }
+  // ---- face AC (lambda2 = 0) ----
+  const float TAC2 = __fmul_rn(TAC, TAC);
+  const float qAC = x_ms<M, 25>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
+  const float rAC = x_ms<M, 26>(TAC2, CDCD, ACCD, ACCD);
+  float fAC;
+  {
+    const float p = x_ms<M, 24>(__fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
+    const float delta = x_ms<M, 27>(qAC, qAC, __fmul_rn(4.0f, p), rAC);
+    const bool ok = delta >= 0.0f;
+    const float sd = __fsqrt_rn(delta);
+    const float a1 = x_root(__fadd_rn(-qAC, sd), p), a3 = __fsub_rn(1.0f, a1);
+    const float b1 = x_root(__fsub_rn(-qAC, sd), p), b3 = __fsub_rn(1.0f, b1);
+    const float ca = __fadd_rn(x_ma<M, 28>(TA, a1, TC, a3), __fsqrt_rn(x_dist2(a1, ACAC, ACCD, CDCD)));
+    // the second candidate keeps a zero-weight TB term, as the reference does
+    const float cb = __fadd_rn(__fmaf_rn(TC, b3, x_ma<M, 29>(TA, b1, TB, 0.0f)),
+                               __fsqrt_rn(x_dist2(b1, ACAC, ACCD, CDCD)));
+    // seeded with LARGENUM as the branching form (a NaN candidate is ignored)
+    fAC = fminf(fminf(L, (ok && a1 >= 0 && a1 <= 1) ? ca : L), (ok && b1 >= 0 && b1 <= 1) ? cb : L);
+  }
+  const float edges = fminf(fminf(fBC, fminf(eB, eC)), fminf(fminf(fAB, fminf(eB, eA)), fminf(fAC, fminf(eA, eC))));
+  // ---- inside face ABC: lambda2 = (s*lambda1 + t)/(h + 1e-8) ----
+  const float s = x_ms<M, 30>(TAC, ACBC, TBC, ACAC);
+  const float t = x_ms<M, 31>(TAC, BCCD, TBC, ACCD);
+  const float h = -x_ms<M, 32>(TAC, BCBC, TBC, ACBC);
+  const float A1 = x_ms<M, 33>(TAC2, ACAC, ACAC, ACAC);
+  const float A2 = x_ms<M, 34>(__fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
+  const float A3 = x_ms<M, 35>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
+  const float A4 = x_ms<M, 37>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
+  const float p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, 36>(__fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
+  const float q = __fmaf_rn(__fmul_rn(A4, s), h,
+                            __fmaf_rn(__fmul_rn(qAC, h), h,
+                                      x_ma<M, 38>(__fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
+  const float r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, 40>(__fmul_rn(x_ms<M, 39>(TAC2, BCBC, ACBC, ACBC), t), t,
+                                                               __fmul_rn(A4, t), h));
+  const float delta = x_ms<M, 41>(q, q, __fmul_rn(4.0f, p), r);
+  float TD = L;
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    float l1 = x_root(__fadd_rn(-q, sd), p);
+    float l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    float l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 42>(TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, 43>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    l1 = x_root(__fsub_rn(-q, sd), p);
+    l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 47>(TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, 48>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+  }
+  return fminf(TD, edges);
+}
+
+// tet_update_x with the four faces' quadratic coefficients and discriminants
+// formed before any root is taken: the four chains are independent and can
+// interleave; the roots keep their branches.  Same operations, same bits.
+template <unsigned long long M>
+__device__ __forceinline__ float tet_update_xd(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                               float BCBC, float BCCD, float CDCD) {
+  if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
+  const float L = kLarge3DDev;
+  const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
+  // face BC
+  const float pBC = x_ms<M, 0>(__fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
+  const float qBC = x_ms<M, 1>(__fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
+  const float rBC = x_ms<M, 2>(__fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
+  const float dBC = x_ms<M, 3>(qBC, qBC, __fmul_rn(4.0f, pBC), rBC);
+  // face AB
+  const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
+  const float TAB2 = __fmul_rn(TAB, TAB);
+  const float P2 = x_ms<M, 7>(__fmul_rn(BCBC, TAB), TAB, gy, gy);
+  const float P3 = x_ms<M, 8>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
+  const float pAB = __fsub_rn(__fadd_rn(x_ms<M, 6>(TAB2, ACAC, gx, gx), P2), P3);
+  const float P5 = x_ms<M, 10>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
+  const float qAB = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3),
+                                        x_ms<M, 9>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz)),
+                              P5);
+  const float rAB = __fadd_rn(__fadd_rn(x_ms<M, 11>(TAB2, BCBC, gy, gy), P5), x_ms<M, 12>(TAB2, CDCD, gz, gz));
+  const float dAB = x_ms<M, 13>(qAB, qAB, __fmul_rn(4.0f, pAB), rAB);
+  // face AC
+  const float TAC2 = __fmul_rn(TAC, TAC);
+  const float pAC = x_ms<M, 24>(__fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
+  const float qAC = x_ms<M, 25>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
+  const float rAC = x_ms<M, 26>(TAC2, CDCD, ACCD, ACCD);
+  const float dAC = x_ms<M, 27>(qAC, qAC, __fmul_rn(4.0f, pAC), rAC);
+  // face ABC
+  const float s = x_ms<M, 30>(TAC, ACBC, TBC, ACAC);
+  const float t = x_ms<M, 31>(TAC, BCCD, TBC, ACCD);
+  const float h = -x_ms<M, 32>(TAC, BCBC, TBC, ACBC);
+  const float A1 = x_ms<M, 33>(TAC2, ACAC, ACAC, ACAC);
+  const float A2 = x_ms<M, 34>(__fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
+  const float A3 = x_ms<M, 35>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
+  const float A4 = x_ms<M, 37>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
+  const float p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, 36>(__fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
+  const float q = __fmaf_rn(__fmul_rn(A4, s), h,
+                            __fmaf_rn(__fmul_rn(qAC, h), h,
+                                      x_ma<M, 38>(__fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
+  const float r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, 40>(__fmul_rn(x_ms<M, 39>(TAC2, BCBC, ACBC, ACBC), t), t,
+                                                               __fmul_rn(A4, t), h));
+  const float delta = x_ms<M, 41>(q, q, __fmul_rn(4.0f, p), r);
+  const float eB = __fadd_rn(TB, __fsqrt_rn(__fadd_rn(__fadd_rn(BCBC, BCCD), __fadd_rn(BCCD, CDCD))));
+  const float eC = __fadd_rn(TC, __fsqrt_rn(CDCD));
+  const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
+  float fBC = L, fAB = L, fAC = L, TD = L, l1, l2, l3;
+  if (dBC >= 0.0f) {
+    const float sd = __fsqrt_rn(dBC);
+    l2 = x_root(__fadd_rn(-qBC, sd), pBC);
+    l3 = __fsub_rn(1.0f, l2);
+    if (l2 >= 0 && l2 <= 1)
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, 4>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+    l2 = x_root(__fsub_rn(-qBC, sd), pBC);
+    l3 = __fsub_rn(1.0f, l2);
+    if (l2 >= 0 && l2 <= 1)
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, 5>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+  }
+  fBC = fminf(fBC, fminf(eB, eC));
+  if (dAB >= 0.0f) {
+    const float sd = __fsqrt_rn(dAB);
+    l1 = x_root(__fadd_rn(-qAB, sd), pAB);
+    l2 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, 14>(TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, 15>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    l1 = x_root(__fsub_rn(-qAB, sd), pAB);
+    l2 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, 19>(TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, 20>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+  }
+  fAB = fminf(fAB, fminf(eB, eA));
+  if (dAC >= 0.0f) {
+    const float sd = __fsqrt_rn(dAC);
+    l1 = x_root(__fadd_rn(-qAC, sd), pAC);
+    l3 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAC = fminf(fAC, __fadd_rn(x_ma<M, 28>(TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+    l1 = x_root(__fsub_rn(-qAC, sd), pAC);
+    l3 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 29>(TA, l1, TB, 0.0f)),
+                                 __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+  }
+  fAC = fminf(fAC, fminf(eA, eC));
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l1 = x_root(__fadd_rn(-q, sd), p);
+    l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 42>(TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, 43>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    l1 = x_root(__fsub_rn(-q, sd), p);
+    l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 47>(TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, 48>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+  }
+  return fminf(TD, fminf(fBC, fminf(fAB, fAC)));
+}
+
+#ifndef EIK_TET_BRANCHFREE
+#define EIK_TET_BRANCHFREE 0
+#endif
+#if EIK_TET_BRANCHFREE == 1
+#define EIK_TET_UPDATE tet_update_xb
+#elif EIK_TET_BRANCHFREE == 2
+#define EIK_TET_UPDATE tet_update_xd
+#else
+#define EIK_TET_UPDATE tet_update_x
+#endif
+
+// The remaining metric edge products of a slot from its six stored ones
+// (CUDA_kernels.cu:429-437), in the order the tet updates take them.
+struct TetGram {
+  float ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, ADAD, ADBD, ADCD, BDBD, CDBD;
+};
+__device__ __forceinline__ TetGram tet_gram9(float ACBC, float BCCD, float ACCD, float ADBD, float ACAD, float BCBD) {
+  TetGram g;
+  const float ADBC = __fadd_rn(ACBC, BCCD);
+  const float ACBD = __fadd_rn(ACBC, ACCD);
+  g.CDBD = __fsub_rn(ADBD, ACBD);
+  g.ADCD = __fsub_rn(ADBD, ADBC);
+  g.CDCD = __fsub_rn(g.ADCD, ACCD);
+  g.ADAD = __fadd_rn(g.ADCD, ACAD);
+  g.ACAC = __fsub_rn(ACAD, ACCD);
+  g.BDBD = __fadd_rn(BCBD, g.CDBD);
+  g.BCBC = __fsub_rn(BCBD, BCCD);
+  g.ACBC = ACBC;
+  g.BCCD = BCCD;
+  g.ACCD = ACCD;
+  g.ADBD = ADBD;
+  return g;
+}
+
+#ifndef EIK_TET_NOINLINE
+#define EIK_TET_NOINLINE 0
+#endif
+#if EIK_TET_NOINLINE
+// one out-of-line body per mask (apexes A and B share theirs): less code for the
+// instruction cache than four inlined copies
+template <unsigned long long M>
+__device__ __noinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                              float BCBC, float BCCD, float CDCD) {
+  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+}
+#define EIK_TET_APEX tet_update_call
+#else
+#define EIK_TET_APEX EIK_TET_UPDATE
+#endif
+
+// The update of apex k (0..3 = A, B, C, D) of a slot with corner times T, as the
+// reference's FIMCuda computes it for that apex (its arguments and its roundings).
+template <int K>
+__device__ __forceinline__ float apex_update(const float T[4], const TetGram& g) {
+  if constexpr (K == 3) return EIK_TET_APEX<kFuseApexD>(T[0], T[1], T[2], g.ACAC, g.ACBC, g.ACCD, g.BCBC, g.BCCD, g.CDCD);
+  if constexpr (K == 0) return EIK_TET_APEX<kFuseApexA>(T[1], T[3], T[2], g.BCBC, -g.BCCD, -g.ACBC, g.CDCD, g.ACCD, g.ACAC);
+  if constexpr (K == 1) return EIK_TET_APEX<kFuseApexB>(T[0], T[3], T[2], g.ACAC, -g.ACCD, -g.ACBC, g.CDCD, g.BCCD, g.BCBC);
+  if constexpr (K == 2) return EIK_TET_APEX<kFuseApexC>(T[0], T[1], T[3], g.ADAD, g.ADBD, -g.ADCD, g.BDBD, -g.CDBD, g.CDCD);
+  return kLarge3DDev;
+}
+
 // Square root of a non-negative candidate distance for the FP64 update: the
 // argument is formed in FP64 (where the cancellation is), the root taken in FP32
 // (relative error below 1e-7, far inside the scheme's 1e-5 tolerance), which

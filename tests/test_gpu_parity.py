@@ -61,6 +61,71 @@ def test_tet_update_bitwise_vs_reference_kernel(need_gpu, eik, O):
     assert bits_equal(eik.selftest_local_update(0, inp), O.ref_gpu_tet_local_solver(inp))
 
 
+def _tet_block_cases(rng, mg, n):
+    """Single-tet cases (TA TB TC TD and the six stored metric edge products):
+    jittered-cube tets under scalar metrics with arrival times from a point source,
+    random shapes and slivers under anisotropic metrics, and uniform random times;
+    about a fifth of the times at LARGENUM (the wavefront's far side)."""
+    def gram(P, M):
+        def vmv(u, v):
+            Mu = np.stack([u[:, 0] * M[:, 0] + u[:, 1] * M[:, 1] + u[:, 2] * M[:, 2],
+                           u[:, 0] * M[:, 1] + u[:, 1] * M[:, 3] + u[:, 2] * M[:, 4],
+                           u[:, 0] * M[:, 2] + u[:, 1] * M[:, 4] + u[:, 2] * M[:, 5]], 1)
+            return (Mu * v).sum(1)
+        A, B, C, D = P[:, 0], P[:, 1], P[:, 2], P[:, 3]
+        return np.stack([vmv(C - A, C - B), vmv(C - B, D - C), vmv(C - A, D - C), vmv(D - A, D - B),
+                         vmv(C - A, D - A), vmv(C - B, D - B)], 1).astype(np.float32)
+    out = []
+    xyz, tets = mg.kuhn_cube(13, 0.2, seed=31)
+    P = xyz[tets[rng.integers(0, tets.shape[0], n)]].astype(np.float64)
+    M = np.zeros((n, 6))
+    M[:, 0] = M[:, 3] = M[:, 5] = np.exp(rng.uniform(np.log(0.25), np.log(4), n))
+    src = rng.uniform(-0.5, 1.5, (n, 3))
+    T = np.linalg.norm(P - src[:, None, :], axis=2) * np.sqrt(M[:, :1]) * (1 + rng.normal(0, 1e-3, (n, 4)))
+    out.append(np.concatenate([T, gram(P, M)], 1))
+    P = rng.normal(size=(n, 4, 3)) * np.exp(rng.uniform(-3, 3, (n, 1, 1)))
+    fl = rng.random(n) < 0.3
+    P[fl, 3] = P[fl, :3].mean(1) + rng.normal(0, 1e-3, (fl.sum(), 3)) * np.abs(P[fl, :1, 0])
+    Q, _ = np.linalg.qr(rng.normal(size=(n, 3, 3)))
+    ev = np.exp(rng.uniform(0, np.log(100), (n, 3)))
+    Mf = np.einsum("nij,nj,nkj->nik", Q, ev, Q)
+    M = np.stack([Mf[:, 0, 0], Mf[:, 0, 1], Mf[:, 0, 2], Mf[:, 1, 1], Mf[:, 1, 2], Mf[:, 2, 2]], 1)
+    src = P[:, 0] + rng.normal(size=(n, 3)) * 4 * np.abs(P - P[:, :1]).max(axis=(1, 2))[:, None]
+    d = P - src[:, None, :]
+    T = np.sqrt(np.maximum(np.einsum("nvi,nij,nvj->nv", d, Mf, d), 0)) * (1 + rng.normal(0, 1e-2, (n, 4)))
+    out.append(np.concatenate([T, gram(P, M)], 1))
+    P = rng.normal(size=(n, 4, 3)) * np.exp(rng.uniform(-4, 4, (n, 1, 1)))
+    T = rng.uniform(0, 2, (n, 4)) * np.abs(P[:, :1, 0])
+    M = np.tile([1.0, 0, 0, 1, 0, 1], (n, 1))
+    out.append(np.concatenate([T, gram(P, M)], 1))
+    inp = np.concatenate(out, 0).astype(np.float32)
+    inp[:, :4][rng.random((inp.shape[0], 4)) < 0.2] = np.float32(1e9)
+    return inp
+
+
+def test_tet_group_bitwise_vs_reference_fimcuda(need_gpu, eik, O, mg):
+    """The four apex updates of a slot as the product's visit kernels run them
+    (explicitly rounded, with the reference kernel's fused multiply-adds) against
+    the reference's own FIMCuda on single-tet blocks, one sweep: every vertex ends
+    at min(T_k, its apex update), bit for bit."""
+    need_ref(O)
+    inp = _tet_block_cases(np.random.default_rng(77), mg, 100000)
+    want = O.ref_gpu_tet_blocks(inp)
+    got = eik.selftest_local_update(6, inp)
+    assert np.mean(want < inp[:, :4]) > 0.2  # a fair share of updates lower their vertex
+    assert bits_equal(got, want)
+    # the oracle's CPU model of the fused roundings, with the masks the product's
+    # header states, reproduces the reference kernel too
+    import os
+    import re
+    from conftest import ROOT
+    text = open(os.path.join(ROOT, "sci-solver_eikonal_gb300", "csrc", "local_update.cuh")).read()
+    masks = dict(re.findall(r"kFuseApex([ABCD]) = (0x[0-9a-fA-F]+)ull", text))
+    assert sorted(masks) == ["A", "B", "C", "D"]
+    model = O.tet_group_fused(inp, [int(masks[k], 16) for k in "ABCD"])
+    assert bits_equal(model, want)
+
+
 def test_fp32_quotients_equal_the_references_fp64_ones(need_gpu, eik):
     rng = np.random.default_rng(5)
     n = 500000
