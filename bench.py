@@ -67,7 +67,8 @@ def parse():
                         "serve: Poisson request stream over a resident mesh pool; "
                         "prec: sliver + anisotropic 49^3 mesh, FP32 vs mixed FP32/FP64 vs an FP64 run")
     p.add_argument("--serve-rates", default="50,200,500,1000,2000")
-    p.add_argument("--serve-budget-gb", type=float, default=16.0)
+    p.add_argument("--serve-budget-gb", type=float, default=64.0,
+                   help="HBM the serving pool may hold (slots per mesh follow from it)")
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--batch-vpb", type=int, default=0, help="batch: vertices per block (0 = autotune)")
     p.add_argument("--no-plain", action="store_true", help="batch: skip the one-at-a-time comparison")
@@ -500,6 +501,33 @@ def bench_serve(args, E, torch):
     res = {"metric": METRIC, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "steps": args.steps, "warmup": args.warmup,
            "config": {"workload": SERVE_WORKLOAD, "rates_per_s": rates, "hbm_budget_gb": args.serve_budget_gb}}
+    # server start (pool layouts, arena, graph) and each pool mesh's first request,
+    # with the pool meshes' layouts built on the device and on the host (fresh
+    # handles each); the first requests' results must be the same bits
+    startup, firsts = {}, {}
+    for build, dev in (("host_setup", 0), ("device_setup", 1)):
+        fresh = serve_pool(E, mg)
+        for e, _ in fresh:
+            e.deviceSetup_ = dev
+        srv = E.EikonalServer(hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)), keep_results=True)
+        t0 = time.perf_counter()
+        ids = [srv.add_mesh(e) for e, _ in fresh]
+        srv.start()
+        start_s = time.perf_counter() - t0
+        lat, outs = [], []
+        for i in ids:
+            t = time.perf_counter()
+            rid = srv.submit(i, [0], 1.0)
+            srv.drain()
+            lat.append(round(1e3 * (time.perf_counter() - t), 3))
+            srv.poll(max_items=16)
+            outs.append(srv.result(rid, i))
+        srv.close()
+        firsts[build] = outs
+        startup[build] = {"start_s": round(start_s, 3), "first_request_ms_by_mesh": lat}
+    startup["bitwise_equal"] = all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
+                                   for a, b in zip(firsts["host_setup"], firsts["device_setup"]))
+    res["startup"] = startup
     modes = {}
     for mode, inflight in (("served", 0), ("plain", 1)):
         srv = E.EikonalServer(hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)), max_inflight=inflight)
@@ -542,6 +570,9 @@ def bench_serve(args, E, torch):
     res["served"] = modes["served"]
     res["plain"] = modes["plain"]
     res["served_over_plain"] = top["solves_per_s"] / modes["plain"]["per_rate"][-1]["solves_per_s"]
+    res["served_over_plain_per_rate"] = [
+        {"rate_per_s": a["rate_per_s"], "ratio": a["solves_per_s"] / b["solves_per_s"]}
+        for a, b in zip(modes["served"]["per_rate"], modes["plain"]["per_rate"])]
     res["e2e"] = {"value": top["solves_per_s"], "unit": "solves/s", "note": "requests submitted from the host, "
                   "travel times copied back to pinned host memory before completion"}
     return res
@@ -599,10 +630,15 @@ def bench_prec(args, E, torch):
         out[name] = {"solve_ms": r["ms"], "iterations": st["iterations"],
                      "vertex_updates_per_s": st["vertex_updates"] / (r["ms"] * 1e-3),
                      "error_vs_fp64": err(r["result"]), "flagged_tets": st["flagged_tets"],
-                     "residual_max_rel": st["residual_max_rel"], "residual_vertices": st["residual_vertices"]}
+                     "residual_max_rel": st["residual_max_rel"], "residual_vertices": st["residual_vertices"],
+                     "residual_below_rel": st["residual_below_rel"], "polish_rounds": st["polish_rounds"],
+                     "polish_blocks": st["polish_blocks"]}
     out["value"] = out[modes[-1]]["vertex_updates_per_s"]
     out["ms_per_step"] = runs[modes[-1]]["ms"]
-    out["fp64_oracle"] = {"seconds": c64["seconds"], "iterations": c64["iterations"], "threads": c64["cores"]}
+    from oracle import oracle as O  # the FP64 run's own residual, beside the device's
+    res64 = O.fp64_residual(xyz, tets, O.metrics_from_speeds(tets.shape[0], M6.ravel()), ref)
+    out["fp64_oracle"] = {"seconds": c64["seconds"], "iterations": c64["iterations"], "threads": c64["cores"],
+                          "residual_max_rel": res64["lowerable"], "residual_below_rel": res64["below"]}
     out["cpu_baseline"] = {k: c64[k] for k in ("value", "unit", "cores", "kind", "sample")}
     out["e2e"] = None
     return out
@@ -758,7 +794,7 @@ def main():
                                   "process whose kernels are loaded"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": tva["sweep"]["traffic"], "peak_source": peak_src,
-                     "kernel": "k_visit3d<false> (block sweeps)",
+                     "kernel": "k_sweep3d (block sweeps)",
                      "kernel_ms_per_step": fim_ms / args.steps,
                      "algorithmic_bytes_per_launch": tva["sweep"]["algorithmic"],
                      "traffic_over_algorithmic": tva["sweep"]["traffic_over_algorithmic"],
@@ -855,6 +891,68 @@ def c2d_summary(E):
             "error_vs_exact_distance": error_stats(got, dist)}
 
 
+def first_solve_2d(E, batch_count=256, vpb=128):
+    """First-solve latency of 2D meshes with the layout built on the device and on
+    the host: one icosphere of level 7 (163,842 vertices) and the icosphere batch
+    (one batch solve over all instances), each on fresh handles in a process whose
+    kernels are loaded.  The triangle preparation of set_mesh (orientation, obtuse
+    corners, virtual faces; host work in both builds) is timed apart.  The two
+    builds must give the same bits."""
+    mg = importlib.import_module("sci-solver_eikonal_gb300.meshgen")
+    xyz, faces = mg.icosphere(7)
+    sp = mg.batch_speed(xyz, faces)
+    work = mg.batch_workload(batch_count)
+    warm = E.Eikonal(True)
+    wx, wf = mg.icosphere(2)
+    warm.set_mesh(wx, wf)
+    for dev in (1, 0):
+        warm.deviceSetup_ = dev
+        warm.solveEikonal()
+        E.EikonalBatch([warm]).solveEikonal()
+    out = {"workload": "icosphere level 7 (163,842 vertices, per-triangle speed 1 + 0.5 sin(3x) cos(2y) sin(z), "
+                       f"seed vertex 0) and the batch of {batch_count} icospheres, {vpb} verts/block"}
+    res = {}
+    for name, dev in (("device_setup", 1), ("host_setup", 0)):
+        t0 = time.perf_counter()
+        e = E.Eikonal(True)
+        e.set_mesh(xyz, faces)
+        prep_s = time.perf_counter() - t0
+        e.initSpeedMtxMultipliers(sp)
+        e.setSeeds([0])
+        e.maxVertsPerBlock_ = vpb
+        e.deviceSetup_ = dev
+        t0 = time.perf_counter()
+        e.solveEikonal()
+        r = e.getFinalResult()
+        one_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        solvers = []
+        for wxyz, wfaces, wsp, wseeds in work:
+            h = E.Eikonal(True)
+            h.set_mesh(wxyz, wfaces)
+            h.initSpeedMtxMultipliers(wsp)
+            h.setSeeds(wseeds)
+            h.maxVertsPerBlock_ = vpb
+            h.deviceSetup_ = dev
+            solvers.append(h)
+        bprep_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        b = E.EikonalBatch(solvers)
+        b.solveEikonal()
+        rb = b.getFinalResults()
+        batch_s = time.perf_counter() - t0
+        res[name] = (r, rb)
+        out[name] = {"single_first_solve_s": round(one_s, 4), "single_triangle_prep_s": round(prep_s, 4),
+                     "single_solve_ms": e.stats()["solve_ms"], "batch_first_solve_s": round(batch_s, 4),
+                     "batch_triangle_prep_s": round(bprep_s, 3), "batch_solve_ms": b.stats()["solve_ms"]}
+    a, h = res["device_setup"], res["host_setup"]
+    out["bitwise_equal"] = bool(np.array_equal(a[0].view(np.uint32), h[0].view(np.uint32)) and all(
+        np.array_equal(x.view(np.uint32), y.view(np.uint32)) for x, y in zip(a[1], h[1])))
+    out["note"] = ("first solve = partition, block layout, upload, graph and solve (results copied back); "
+                   "the triangle preparation is host work in both builds")
+    return out
+
+
 def metis_summary(E, torch):
     """The headline workload on a METIS k-way partition (the reference's partitioner
     kind; the headline uses coordinate bisection): partition time, device solve
@@ -899,8 +997,12 @@ def pattern_summaries(args, E, torch, local):
         out["metis_partition"] = {"error": repr(ex)}
     try:
         out["plain_2d"] = c2d_summary(E)
-    except Exception as ex:  # keep the headline line even if a pattern fails
+    except Exception as ex:
         out["plain_2d"] = {"error": repr(ex)}
+    try:
+        out["first_solve_2d"] = first_solve_2d(E)
+    except Exception as ex:  # keep the headline line even if a pattern fails
+        out["first_solve_2d"] = {"error": repr(ex)}
     try:
         b = bench_batch(args, E, torch, 1, local)
         out["batched"] = {"workload": BATCH_WORKLOAD, "solves_per_s": b["value"],
@@ -919,8 +1021,10 @@ def pattern_summaries(args, E, torch, local):
                                       for r in sv["served"]["per_rate"]],
                          "plain_per_rate": [{k: r[k] for k in ("rate_per_s", "solves_per_s", "p50_ms", "p99_ms")}
                                             for r in sv["plain"]["per_rate"]],
-                         "ratio_at_top_rate": sv["served_over_plain"], "slots": sv["served"]["slots"],
-                         "device_bytes": sv["served"]["device_bytes"]}
+                         "ratio_at_top_rate": sv["served_over_plain"],
+                         "ratio_per_rate": sv["served_over_plain_per_rate"], "slots": sv["served"]["slots"],
+                         "device_bytes": sv["served"]["device_bytes"], "hbm_budget_gb": args.serve_budget_gb,
+                         "setup_s": sv["served"]["setup_s"], "startup": sv["startup"]}
     except Exception as ex:
         out["served"] = {"error": repr(ex)}
     try:
@@ -928,8 +1032,9 @@ def pattern_summaries(args, E, torch, local):
         out["precision"] = {"workload": PREC_WORKLOAD, "sliver_fraction": pr["config"]["sliver_fraction"],
                             "fp32": {k: pr["fp32"][k] for k in ("solve_ms", "error_vs_fp64")},
                             "mixed": {k: pr["mixed"][k] for k in ("solve_ms", "error_vs_fp64", "flagged_tets",
-                                                                  "residual_max_rel")},
-                            "fp64_oracle_s": pr["fp64_oracle"]["seconds"]}
+                                                                  "residual_max_rel", "residual_below_rel",
+                                                                  "polish_rounds", "polish_blocks")},
+                            "fp64_oracle": pr["fp64_oracle"]}
     except Exception as ex:
         out["precision"] = {"error": repr(ex)}
     return out

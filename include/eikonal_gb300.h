@@ -68,10 +68,13 @@ typedef struct eik_options {
                               updates in FP64 from FP64 metric edge products; every other tet
                               stays FP32.  An FP64 residual check runs after the solve. */
   float precision_kappa;   /* flagging threshold on ||G||_F ||G^-1||_F (1e4) */
-  int device_setup;        /* 1 (default): a 3D solve builds its block layout (renumbering, element slots,
-                              halo lists, metric edge products, neighbour graph) on the GPU;
-                              0: on the host.  Same layout, same results; precision mode,
-                              batches and the server use the host build. */
+  int device_setup;        /* 1 (default): a solve builds its block layout (renumbering, element slots,
+                              halo lists, metric edge products or inverse face speeds,
+                              neighbour graph) on the GPU; 2D meshes keep their triangle
+                              preparation (orientation, obtuse corners, virtual faces) on the
+                              host.  0: on the host.  Same layout, same results.  A batch builds
+                              on the device when all its handles do (one pass over all
+                              instances); 3D precision mode and the server build on the host. */
   int partitioner;         /* EIK_PARTITION_RCB (default) or EIK_PARTITION_METIS: the reference's
                               partitioner kind, here METIS 5 from the CUDA toolkit where the
                               reference calls METIS 4 (so labels differ from the reference's);
@@ -104,9 +107,19 @@ typedef struct eik_stats {
   long long h2d_bytes;       /* host-to-device bytes copied by the last solve (initial state) */
   /* precision mode (precision = 1) */
   long long flagged_tets;    /* tets whose updates run in FP64 */
-  double residual_max_abs;   /* FP64 check: max |T_v - min over incident tets of the FP64 update| */
+  /* FP64 check of the final times, c_v = min over incident tets of the FP64 update: */
+  double residual_max_abs;   /* max (T_v - c_v) over vertices with c_v < T_v (more updates would lower T_v) */
   double residual_max_rel;   /* the same relative to T_v */
-  long long residual_vertices; /* vertices with |residual| > 1e-5 * T_v */
+  long long residual_vertices; /* vertices with (T_v - c_v) > 1e-5 * T_v */
+  /* precision mode's polish: after the solve, blocks owning a vertex that the FP64
+   * update of its tets would lower by more than 1e-6 relative run the loop again
+   * with every slot's update in FP64, round after round (at most 8) */
+  int polish_rounds;          /* rounds run */
+  long long polish_blocks;    /* blocks queued over those rounds */
+  double residual_below_rel; /* max (c_v - T_v) / T_v over vertices below every FP64 update of their
+                                tets: the local update is not monotone in its inputs, so a time can
+                                end below the update of its final neighbour times (the FP64 run of
+                                the scheme does too); no further update changes these */
 } eik_stats;
 
 /* Fills `o` with the reference's defaults (src/Eikonal.cu:4-24). */

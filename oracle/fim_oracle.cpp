@@ -174,6 +174,36 @@ int oracle_tet_fusion_mismatch(const float* in, const float* want, int n, int k,
   return bad;
 }
 
+// FP64 fixed-point residual of travel times T: per vertex the smallest FP64 tet
+// update over its incident tets (the four apex updates of the sweep above, from the
+// FP64 edge products), LARGENUM where no update is finite.  Used to state how far a
+// result is from a fixed point of the scheme, for the GPU result and for the FP64
+// run of the scheme itself.
+int oracle3d_fp64_candidates(int nv, const float* xyz, int nt, const int* tets, const float* M, const float* T,
+                             double* cand) {
+  if (nv <= 0 || nt <= 0) return -1;
+  Oracle3D<double> o;
+  o.nv = nv; o.nt = nt; o.xyz = xyz; o.tets = tets; o.M = M;
+  for (int v = 0; v < nv; ++v) cand[v] = (double)kLarge3D;
+  for (int t = 0; t < nt; ++t) {
+    double g[6];
+    o.tet_gram(t, g);
+    const double ACBC = g[0], BCCD = g[1], ACCD = g[2], ADBD = g[3], ACAD = g[4], BCBD = g[5];
+    const double ADBC = ACBC + BCCD, ACBD = ACBC + ACCD, CDBD = ADBD - ACBD, ADCD = ADBD - ADBC;
+    const double CDCD = ADCD - ACCD, ADAD = ADCD + ACAD, ACAC = ACAD - ACCD, BDBD = BCBD + CDBD;
+    const double BCBC = BCBD - BCCD;
+    const int* v = tets + 4 * (size_t)t;
+    const double TA = T[v[0]], TB = T[v[1]], TC = T[v[2]], TD = T[v[3]];
+    const double u[4] = {tet_update<double>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC),
+                         tet_update<double>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC),
+                         tet_update<double>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD),
+                         tet_update<double>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD)};
+    for (int k = 0; k < 4; ++k)
+      if (u[k] >= 0.0 && u[k] < cand[v[k]]) cand[v[k]] = u[k];
+  }
+  return 0;
+}
+
 int oracle_num_threads(void) { return n_threads(0); }
 
 // Wall time of the outer iterations of the last oracle3d_solve (its layout set-up

@@ -54,6 +54,9 @@ def lib():
         _lib.oracle_partition_rcb.restype = ctypes.c_int
         _lib.oracle_partition_rcb.argtypes = [ctypes.c_int, _FP, ctypes.c_int, ctypes.c_int, _IP]
         _lib.oracle_last_loop_seconds.restype = ctypes.c_double
+        _lib.oracle3d_fp64_candidates.restype = ctypes.c_int
+        _lib.oracle3d_fp64_candidates.argtypes = [ctypes.c_int, _FP, ctypes.c_int, _IP, _FP, _FP,
+                                                  ctypes.POINTER(ctypes.c_double)]
     return _lib
 
 
@@ -231,6 +234,33 @@ def tet_fusion_mismatch(inputs10, want4, k, mask):
     a, w = _f(inputs10).reshape(-1, 10), _f(want4).reshape(-1, 4)
     return lib().oracle_tet_fusion_mismatch(a.ctypes.data_as(_FP), w.ctypes.data_as(_FP), a.shape[0], int(k),
                                             ctypes.c_ulonglong(int(mask)))
+
+
+def fp64_candidates(xyz, tets, metric6, T):
+    """Per vertex the smallest FP64 tet update over its incident tets from the
+    times T (FP64 edge products of the 6-entry metrics); 1e9 where none is finite."""
+    xyz, tets, M, T = _f(xyz), _i(tets), _f(metric6), _f(T)
+    out = np.empty(xyz.shape[0], dtype=np.float64)
+    rc = lib().oracle3d_fp64_candidates(xyz.shape[0], xyz.ctypes.data_as(_FP), tets.shape[0], tets.ctypes.data_as(_IP),
+                                        M.ctypes.data_as(_FP), T.ctypes.data_as(_FP),
+                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    if rc < 0:
+        raise ValueError("oracle3d_fp64_candidates rejected its input")
+    return out
+
+
+def fp64_residual(xyz, tets, metric6, T):
+    """FP64 fixed-point residual of T, split by sign, relative to T (seeds and
+    unreached vertices left out): "lowerable" = max (T - c) / T where an FP64
+    update c lies below T (more FIM updates would lower T there), "below" =
+    max (c - T) / T where T lies below every FP64 update of its tets."""
+    T = np.asarray(T, dtype=np.float32)
+    c = fp64_candidates(xyz, tets, metric6, T)
+    t = T.astype(np.float64)
+    ok = (t > 0) & (t < 1e9) & (c < 1e9)
+    d = (t - c)[ok] / t[ok]
+    return {"lowerable": float(max(d.max(initial=0.0), 0.0)), "below": float(max((-d).max(initial=0.0), 0.0)),
+            "lowerable_1e-5": int((d > 1e-5).sum()), "below_1e-5": int((d < -1e-5).sum())}
 
 
 def num_threads():

@@ -60,6 +60,8 @@ class EikStats(ctypes.Structure):
         ("h2d_bytes", ctypes.c_longlong),
         ("flagged_tets", ctypes.c_longlong), ("residual_max_abs", ctypes.c_double),
         ("residual_max_rel", ctypes.c_double), ("residual_vertices", ctypes.c_longlong),
+        ("polish_rounds", ctypes.c_int), ("polish_blocks", ctypes.c_longlong),
+        ("residual_below_rel", ctypes.c_double),
     ]
 
     def as_dict(self):

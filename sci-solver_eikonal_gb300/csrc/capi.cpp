@@ -18,7 +18,8 @@
 
 using namespace eikgb;
 
-// 3D solves build their block layout on the GPU unless eik_options.device_setup = 0
+// Solves build their block layout on the GPU unless eik_options.device_setup = 0
+// (3D precision mode builds on the host)
 #define DEVICE_SETUP_DEFAULT 1
 
 struct eik_solver {
@@ -46,6 +47,7 @@ struct eik_solver {
   unsigned prep_mesh = ~0u;
   std::vector<int> labels;
   int nb = 0;
+  std::string labels_key;  // mesh version and partition inputs `labels` were made for
   unsigned lay_mesh = ~0u, lay_part = ~0u, lay_speed = ~0u;
   std::string lay_key;
   std::string prec_key;  // precision settings the layout's FP64 data was built for
@@ -96,7 +98,15 @@ int make_partition(eik_solver* h) {
     partition_rcb(h->nv, h->xyz.data(), h->nb, h->labels);
   }
   h->opt.max_blocks = h->nb;  // the reference overwrites maxBlocks_ the same way
+  h->labels_key = std::to_string(h->mesh_ver) + "/" + partition_key(h);
   return EIK_OK;
+}
+
+// make_partition unless `labels` already hold this mesh's partition for the
+// current partition inputs.
+int ensure_partition(eik_solver* h) {
+  if (!h->labels.empty() && h->labels_key == std::to_string(h->mesh_ver) + "/" + partition_key(h)) return EIK_OK;
+  return make_partition(h);
 }
 
 std::vector<float> speed_inverse(const eik_solver* h) {
@@ -266,6 +276,9 @@ void fill_stats(eik_stats& s, const SolveStats& st, const Layout& L, float setup
   s.residual_max_abs = st.residual_max_abs;
   s.residual_max_rel = st.residual_max_rel;
   s.residual_vertices = st.residual_vertices;
+  s.residual_below_rel = st.residual_below_rel;
+  s.polish_rounds = st.polish_rounds;
+  s.polish_blocks = st.polish_blocks;
 }
 
 // The 3D layout built on the device (build_layout3d_device), cached while the mesh
@@ -285,6 +298,12 @@ const float* compact_metrics(const eik_solver* h, std::vector<float>& ones, int*
   return ones.data();
 }
 
+// 2D face speeds as the layout takes them: the caller's per-face speeds, else none
+// (inverse speed 1, TriMesh_stats.cu:64-68)
+const float* face_speeds(const eik_solver* h) {
+  return (h->speeds_set && (int)h->speeds.size() == h->ne) ? h->speeds.data() : nullptr;
+}
+
 int device_prepare(eik_solver* h) {
   if (int rc = check_speeds(h)) return rc;
   const std::string key = partition_key(h);
@@ -297,11 +316,15 @@ int device_prepare(eik_solver* h) {
     const auto t1 = clk::now();
     std::vector<float> ones;
     int mcomp = 6;
-    const float* M = compact_metrics(h, ones, &mcomp);
+    const float* M = (h->dim == 3) ? compact_metrics(h, ones, &mcomp) : nullptr;
     const auto t2 = clk::now();
     Built3D b;
-    std::string e = build_layout3d_device(h->nv, h->xyz.data(), h->ne, h->elems.data(), M, mcomp, h->labels.data(),
-                                          h->nb, (cudaStream_t)h->dev->stream(), b, h->dlayout);
+    std::string e = (h->dim == 3)
+                        ? build_layout3d_device(h->nv, h->xyz.data(), h->ne, h->elems.data(), M, mcomp,
+                                                h->labels.data(), h->nb, (cudaStream_t)h->dev->stream(), b,
+                                                h->dlayout)
+                        : build_layout2d_device(h->nv, h->prep, face_speeds(h), h->labels.data(), h->nb,
+                                                (cudaStream_t)h->dev->stream(), b, h->dlayout);
     if (h->opt.verbose) {
       const auto t3 = clk::now();
       auto ms = [](clk::time_point a, clk::time_point z) { return std::chrono::duration<double, std::milli>(z - a).count(); };
@@ -326,8 +349,13 @@ int device_prepare(eik_solver* h) {
   } else if (h->dlay_speed != h->speed_ver) {
     std::vector<float> ones;
     int mcomp = 6;
-    const float* M = compact_metrics(h, ones, &mcomp);
-    std::string e = h->dev->refresh_coef_built(M, mcomp);
+    std::string e;
+    if (h->dim == 3) {
+      const float* M = compact_metrics(h, ones, &mcomp);
+      e = h->dev->refresh_coef_built(M, mcomp);
+    } else {
+      e = h->dev->refresh_speed_built(face_speeds(h));
+    }
     if (!e.empty()) return fail(h, EIK_ERR_CUDA, e);
     h->dlay_speed = h->speed_ver;
   }
@@ -335,7 +363,7 @@ int device_prepare(eik_solver* h) {
 }
 
 bool use_device_setup(const eik_solver* h) {
-  return h->dim == 3 && h->opt.device_setup == 1 && h->opt.precision == 0;
+  return h->opt.device_setup == 1 && (h->dim == 2 || h->opt.precision == 0);
 }
 
 }  // namespace
@@ -768,16 +796,52 @@ int eikgb::snapshot_for_server(eik_solver* h, MeshSnapshot& out, std::string& er
     err = "no mesh: call eik_set_mesh or eik_load_mesh first";
     return EIK_ERR_STATE;
   }
-  bool nl = false;
-  int rc = host_prepare(h, &nl);
-  if (rc) {
-    err = h->err;
-    return rc;
+  out.built.reset();
+  if (use_device_setup(h)) {
+    // the layout built on the device, kept there until the server replicates it
+    int rc = check_speeds(h);
+    if (!rc) rc = ensure_partition(h);
+    if (rc) {
+      err = h->err;
+      return rc;
+    }
+    cudaStream_t st = new_stream();
+    if (!st) {
+      err = "CUDA stream creation failed (no usable GPU?)";
+      return EIK_ERR_CUDA;
+    }
+    std::shared_ptr<Built3D> b(new Built3D, [](Built3D* x) {
+      x->release();
+      delete x;
+    });
+    std::string e;
+    if (h->dim == 3) {
+      std::vector<float> ones;
+      int mcomp = 6;
+      const float* M = compact_metrics(h, ones, &mcomp);
+      e = build_layout3d_device(h->nv, h->xyz.data(), h->ne, h->elems.data(), M, mcomp, h->labels.data(), h->nb, st,
+                                *b, out.layout);
+    } else {
+      e = build_layout2d_device(h->nv, h->prep, face_speeds(h), h->labels.data(), h->nb, st, *b, out.layout);
+    }
+    free_stream(st);
+    if (!e.empty()) {
+      err = e;
+      return e.find("too many local") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA;
+    }
+    out.built = b;
+  } else {
+    bool nl = false;
+    int rc = host_prepare(h, &nl);
+    if (rc) {
+      err = h->err;
+      return rc;
+    }
+    out.layout = h->layout;
   }
   out.dim = h->dim;
   out.nv = h->nv;
   out.ne = h->ne;
-  out.layout = h->layout;
   out.xyz = h->xyz;
   out.max_iterations = h->opt.max_iterations;
   out.fim_sweeps = h->opt.fim_sweeps;
@@ -819,6 +883,104 @@ std::string layout_identity(const eik_solver* h) {
   return std::to_string(h->lay_mesh) + "/" + h->lay_key + "/" + std::to_string(h->lay_speed);
 }
 
+// A batch builds its layout on the device when every handle would build its own
+// there (device_setup = 1; 3D precision mode builds on the host).
+bool batch_on_device(const eik_batch* b) {
+  for (const eik_solver* h : b->solvers)
+    if (!use_device_setup(h)) return false;
+  return true;
+}
+
+// The batch's layout built on the device in one pass: the instances' meshes as one
+// disconnected mesh, vertex, element and block ids offset instance by instance.
+// Its layout is the concatenation of the instances' own layouts (concat_layouts):
+// the renumbering orders vertices by block, slots, halo lists and the 2D copy cap
+// are decided block by block or vertex by vertex, and no element or block spans
+// two instances.
+std::string batch_device_pack(eik_batch* b) {
+  const int n = (int)b->solvers.size();
+  const int dim = b->solvers[0]->dim;
+  Layout& L = b->layout;
+  std::vector<int> labels, bbeg{0}, vbeg{0};
+  int nb = 0, nv = 0, ne = 0;
+  for (const eik_solver* h : b->solvers) {
+    for (int l : h->labels) labels.push_back(l + nb);
+    nb += h->nb;
+    nv += h->nv;
+    ne += h->ne;
+    bbeg.push_back(nb);
+    vbeg.push_back(nv);
+  }
+  if (!b->dev) b->dev.reset(new DeviceSolve);
+  cudaStream_t st = (cudaStream_t)b->dev->stream();
+  Built3D built;
+  std::string e;
+  if (dim == 2) {
+    TriPrep U;
+    U.nv = nv;
+    U.vf_off.push_back(0);
+    std::vector<float> speeds;
+    speeds.reserve(ne);
+    int voff = 0, vfoff = 0;
+    for (const eik_solver* h : b->solvers) {
+      const TriPrep& P = h->prep;
+      for (int x : P.faces) U.faces.push_back(x + voff);
+      U.obtuse.insert(U.obtuse.end(), P.obtuse.begin(), P.obtuse.end());
+      U.edges.insert(U.edges.end(), P.edges.begin(), P.edges.end());
+      U.vf_edges.insert(U.vf_edges.end(), P.vf_edges.begin(), P.vf_edges.end());
+      for (int i = 1; i <= P.nf; ++i) U.vf_off.push_back(P.vf_off[i] + vfoff);
+      for (int x : P.vf_verts) U.vf_verts.push_back(x + voff);
+      const float* sp = face_speeds(h);
+      if (sp) speeds.insert(speeds.end(), sp, sp + P.nf);
+      else speeds.insert(speeds.end(), (size_t)P.nf, 1.0f);
+      U.nf += P.nf;
+      vfoff += P.vf_off[P.nf];
+      voff += h->nv;
+    }
+    e = build_layout2d_device(nv, U, speeds.data(), labels.data(), nb, st, built, L);
+  } else {
+    // scalar metrics stay one float per tet unless some instance gives 6 entries,
+    // then every instance's are expanded (s I: the same products)
+    bool full = false;
+    for (const eik_solver* h : b->solvers) full = full || (h->speeds_set && h->speeds.size() == 6 * (size_t)h->ne);
+    std::vector<float> xyz, M;
+    std::vector<int> tets;
+    xyz.reserve(3 * (size_t)nv);
+    tets.reserve(4 * (size_t)ne);
+    int voff = 0;
+    for (const eik_solver* h : b->solvers) {
+      xyz.insert(xyz.end(), h->xyz.begin(), h->xyz.end());
+      for (int x : h->elems) tets.push_back(x + voff);
+      if (full) {
+        std::vector<float> m6;
+        tet_metrics(h->ne, h->speeds_set ? h->speeds.data() : nullptr, h->speeds.size(), m6);
+        M.insert(M.end(), m6.begin(), m6.end());
+      } else {
+        std::vector<float> ones;
+        int mc = 1;
+        const float* m = compact_metrics(h, ones, &mc);
+        M.insert(M.end(), m, m + h->ne);
+      }
+      voff += h->nv;
+    }
+    e = build_layout3d_device(nv, xyz.data(), ne, tets.data(), M.data(), full ? 6 : 1, labels.data(), nb, st, built,
+                              L);
+  }
+  if (!e.empty()) {
+    built.release();
+    return e;
+  }
+  L.ninst = n;
+  L.inst_bbeg = bbeg;
+  L.inst_vbeg = vbeg;
+  L.blk_inst.assign(nb, 0);
+  for (int i = 0; i < n; ++i)
+    for (int k = bbeg[i]; k < bbeg[i + 1]; ++k) L.blk_inst[k] = i;
+  e = b->dev->upload_built(L, built);
+  if (!e.empty()) built.release();
+  return e;
+}
+
 }  // namespace
 
 int eik_batch_create(eik_solver* const* solvers, int n, eik_batch** out) {
@@ -844,27 +1006,45 @@ int eik_batch_solve(eik_batch* b) {
   std::vector<const float*> init(n, nullptr);
   bool repack = !b->packed || (int)b->keys.size() != n;
   b->keys.resize(n);
+  const bool on_device = batch_on_device(b);
   for (int i = 0; i < n; ++i) {
     eik_solver* h = b->solvers[i];
     if (h->nv == 0) return bfail(b, EIK_ERR_STATE, "instance " + std::to_string(i) + ": no mesh");
     int rc = resolve_seeds(h, seeds[i], &init[i]);
     if (rc) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
-    bool nl = false;
-    rc = host_prepare(h, &nl);
+    std::string key;
+    if (on_device) {
+      rc = check_speeds(h);
+      if (!rc) rc = ensure_partition(h);
+      key = "device/" + std::to_string(h->mesh_ver) + "/" + partition_key(h) + "/" + std::to_string(h->speed_ver);
+    } else {
+      bool nl = false;
+      rc = host_prepare(h, &nl);
+      key = layout_identity(h);
+    }
     if (rc) return bfail(b, rc, "instance " + std::to_string(i) + ": " + h->err);
-    const std::string key = layout_identity(h);
     if (key != b->keys[i]) repack = true;
     b->keys[i] = key;
   }
   if (repack) {
     b->packed = false;
-    std::vector<const Layout*> parts(n);
-    for (int i = 0; i < n; ++i) parts[i] = &b->solvers[i]->layout;
-    std::string e = concat_layouts(parts, b->layout);
-    if (!e.empty()) return bfail(b, EIK_ERR_ARG, e);
-    if (!b->dev) b->dev.reset(new DeviceSolve);
-    e = b->dev->upload(b->layout);
-    if (!e.empty()) return bfail(b, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+    std::string e;
+    if (on_device) {
+      e = batch_device_pack(b);
+      if (!e.empty())
+        return bfail(b, e.find("too many local") != std::string::npos || e.find("shared memory") != std::string::npos
+                            ? EIK_ERR_LIMIT
+                            : EIK_ERR_CUDA,
+                     e);
+    } else {
+      std::vector<const Layout*> parts(n);
+      for (int i = 0; i < n; ++i) parts[i] = &b->solvers[i]->layout;
+      e = concat_layouts(parts, b->layout);
+      if (!e.empty()) return bfail(b, EIK_ERR_ARG, e);
+      if (!b->dev) b->dev.reset(new DeviceSolve);
+      e = b->dev->upload(b->layout);
+      if (!e.empty()) return bfail(b, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
+    }
     b->packed = true;
   }
   std::string e = b->dev->set_seeds_multi(seeds, init);

@@ -44,8 +44,10 @@ struct SolveStats {
   long long h2d_bytes = 0;       // host-to-device bytes the last solve copied (initial state)
   std::vector<int> inst_iters;   // outer iterations run by every instance
   // precision mode: FP64 residual check after the solve
-  double residual_max_abs = 0, residual_max_rel = 0;
+  double residual_max_abs = 0, residual_max_rel = 0, residual_below_rel = 0;
   long long residual_vertices = 0;
+  int polish_rounds = 0;         // rounds of FP64 re-visits after the solve
+  long long polish_blocks = 0;   // blocks queued over those rounds
 };
 
 struct SolveOptions {
@@ -98,6 +100,7 @@ struct Built3D {
   float* M6 = nullptr;          // metric per tet: mcomp entries (6: full, 1: scalar times I)
   int mcomp = 6;
   int total_slots = 0, nhalo = 0, nnbr = 0;
+  int dim = 3;                  // 2: tets holds the oriented faces (3 each), M6 the face speeds
   void release();
 };
 
@@ -109,8 +112,25 @@ struct Built3D {
 std::string build_layout3d_device(int nv, const float* xyz, int nt, const int* tets, const float* M, int mcomp,
                                   const int* labels, int nb, cudaStream_t st, Built3D& out, Layout& L);
 
-// Device bytes one instance of this layout occupies (layout arrays + state).
-size_t device_footprint(const Layout& L);
+// The 2D layout of build_layout2d built on the device from a prepared triangle mesh
+// (oriented faces, obtuse corners, virtual faces and edge lengths stay host work)
+// and per-face speeds (null: all 1); same arrays, including the bit-15 marks of the
+// copies the reference never refreshes.  out.dim = 2.
+std::string build_layout2d_device(int nv, const TriPrep& P, const float* speeds, const int* labels, int nb,
+                                  cudaStream_t st, Built3D& out, Layout& L);
+
+// A non-blocking CUDA stream of the current device (null on failure), and its release.
+cudaStream_t new_stream();
+void free_stream(cudaStream_t st);
+
+// Device bytes one instance of this layout occupies (layout arrays + state);
+// b: the device-built arrays of a layout whose host part L holds none of them.
+size_t device_footprint(const Layout& L, const Built3D* b = nullptr);
+
+// Copies a device-built layout's arrays (coefficients, corner ids, element ids,
+// halo lists, neighbour graph) into the host layout L that holds its host part,
+// which then equals the host build's layout.
+std::string download_built(const Built3D& b, Layout& L);
 
 class DeviceSolve {
  public:
@@ -125,9 +145,16 @@ class DeviceSolve {
   std::string upload_coef(const Layout& L);
   // Take over a device-built 3D layout (L: its host part, kept by the caller).
   std::string upload_built(const Layout& L, Built3D& b);
+  // Several instances of device-built layouts concatenated on the device (the
+  // server's arena): parts[i] holds instance i's arrays (a part may repeat), L the
+  // host part of the concatenation (concat_layout_headers).  The parts stay the
+  // caller's.
+  std::string upload_replicas(const Layout& L, const std::vector<const Built3D*>& parts);
   // Device-built layouts: recompute the per-slot coefficients on the device from
   // a new per-tet metric (6 entries per tet, host array).
   std::string refresh_coef_built(const float* M, int mcomp);
+  // Device-built 2D layouts: new inverse speeds from per-face speeds (null: all 1).
+  std::string refresh_speed_built(const float* speed);
   bool layout_built_on_device() const;
   // Copies of the uploaded layout's per-slot coefficients and (device-built 3D
   // layouts only) the element id of every slot, for checks against the reference.

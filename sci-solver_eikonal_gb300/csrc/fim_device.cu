@@ -62,6 +62,7 @@ struct Ctl {
   int done_d;     // 2D: CTAs of the all-vertex test finished (the last one closes)
   int error;
   int stop;       // set when the outer loop must end (read by the direct-launch loop)
+  int f64_all;    // precision mode's polish: every slot's update in FP64
   unsigned long long updates, fim_visits, chk_visits, slot_visits, halo_visits, owned_visits;
   unsigned long long fim_slots, fim_halo, fim_owned;  // per-visit inputs of the sweep kernel only
 };
@@ -124,6 +125,9 @@ struct DevArgs {
   // 3D check visits: per slot the four input times of an earlier check of this
   // solve that lowered no owned vertex by EPS (all ones: none recorded)
   uint4* chk_memo;
+  // 3D sweep visits (k_sweep3d): per slot the four input times of the last sweep
+  // of the block's latest visit in this solve (all ones: none recorded)
+  uint4* fim_memo;
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -132,6 +136,22 @@ constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
 constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::ktime)
 #ifndef EIK_SWEEP_ITEMS
 #define EIK_SWEEP_ITEMS 1
+#endif
+#ifndef EIK_SWEEP_MEMO
+#define EIK_SWEEP_MEMO 1
+#endif
+// precision mode's polish: every slot's update in FP64 (1) or only the flagged
+// tets' (0), and the relative gap to the FP64 update that re-queues a block
+#ifndef EIK_POLISH_F64ALL
+#define EIK_POLISH_F64ALL 1
+#endif
+#ifndef EIK_POLISH_TOL
+#define EIK_POLISH_TOL 1e-6
+#endif
+// item kernels: warps take chunks of 32 items from a shared counter (1) or a
+// fixed stride of the CTA's threads (0)
+#ifndef EIK_ITEM_STEAL
+#define EIK_ITEM_STEAL 0
 #endif
 #ifndef EIK_CHECK_ITEMS
 #define EIK_CHECK_ITEMS 1
@@ -322,6 +342,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   const int stamp = iter + 1;
   const int count = kCheck ? ctl->nnew : ctl->nact;
   const int* list = kCheck ? a.list_new : act_list(a, iter);
+  const int f64all = kPrec ? ctl->f64_all : 0;
   int* nxt = next_list(a, iter);
   const int nsweeps = kCheck ? 1 : a.fim_sweeps;
   stamp_start(a, iter, kCheck ? 1 : 0);
@@ -420,9 +441,12 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
           if constexpr (kPrec) {
             // flagged tet: the same four updates again in FP64 from FP64 products
             // (the FP32 group above stays exactly the FP32 kernel's code)
+            // (polish: every slot, the unflagged ones from their FP32 products)
             const int f = a.slot_f64[bd.slot_begin + j];
-            if (f >= 0) {
-              const double* g = a.coef64 + 6 * (size_t)f;
+            if (f >= 0 || f64all) {
+              double g[6];
+#pragma unroll
+              for (int q = 0; q < 6; ++q) g[q] = (f >= 0) ? a.coef64[6 * (size_t)f + q] : (double)s.coef[q * np + j];
               const double dACBC = g[0], dBCCD = g[1], dACCD = g[2], dADBD = g[3], dACAD = g[4], dBCBD = g[5];
               const double dADBC = dACBC + dBCCD, dACBD = dACBC + dACCD;
               const double dCDBD = dADBD - dACBD, dADCD = dADBD - dADBC;
@@ -632,7 +656,7 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
-  __shared__ int s_cnt[4];
+  __shared__ int s_cnt[5];  // items per apex kind, then the next unclaimed item
   const SmemItems s0 = carve_items(sm, a);
   const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
   const int np = a.max_slots_pad;
@@ -676,7 +700,7 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
     int myconv = 1;
     for (int sw = 0; sw < nsweeps; ++sw) {
       const bool first = (sw == 0), last = (sw == nsweeps - 1);
-      if (tid < 4) s_cnt[tid] = 0;
+      if (tid < 5) s_cnt[tid] = 0;
       __syncthreads();
       // ---- list the apex updates this sweep must run ----
       for (int j0 = 0; j0 < ns; j0 += NT) {
@@ -699,12 +723,25 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
             own |= (o ? 1u : 0u) << q;
             if (!o && !last) s.h1[4 * j + q] = T;  // kept unless its update below changes it
           }
+          // sweep memo: an owned apex whose three other inputs equal (as bits) those
+          // of the last sweep of the block's previous visit repeats an update whose
+          // result its time has already absorbed (times only decrease)
+          unsigned same = 0;
+          if (first && a.fim_memo) {
+            const uint4 mm = a.fim_memo[bd.slot_begin + j];
+            same = (__float_as_uint(Tq[0]) == mm.x ? 1u : 0u) | (__float_as_uint(Tq[1]) == mm.y ? 2u : 0u) |
+                   (__float_as_uint(Tq[2]) == mm.z ? 4u : 0u) | (__float_as_uint(Tq[3]) == mm.w ? 8u : 0u);
+          }
+          if (last && a.fim_memo)
+            a.fim_memo[bd.slot_begin + j] = make_uint4(__float_as_uint(Tq[0]), __float_as_uint(Tq[1]),
+                                                       __float_as_uint(Tq[2]), __float_as_uint(Tq[3]));
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const unsigned others = 0xfu & ~(1u << k);
             const float m = fminf(fminf(Tq[(k + 1) & 3], Tq[(k + 2) & 3]), Tq[(k + 3) & 3]);
-            const bool run = ((big & others) != others) && (chg & others) && (!last || ((own >> k) & 1u)) &&
-                             !upwind_skip(Tq[k], m);
+            const bool ownk = ((own >> k) & 1u) != 0;
+            const bool run = ((big & others) != others) && (chg & others) && (!last || ownk) &&
+                             !(ownk && (same & others) == others) && !upwind_skip(Tq[k], m);
             need |= (run ? 1u : 0u) << k;
           }
         }
@@ -722,7 +759,17 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
       __syncthreads();
       // ---- run them ----
       const int c0 = s_cnt[0], c01 = c0 + s_cnt[1], c012 = c01 + s_cnt[2], total = c012 + s_cnt[3];
+#if EIK_ITEM_STEAL
+      for (;;) {
+        int i0 = 0;
+        if (lane == 0) i0 = atomicAdd(&s_cnt[4], 32);
+        i0 = __shfl_sync(0xffffffffu, i0, 0);
+        if (i0 >= total) break;
+        const int i = i0 + lane;
+        if (i >= total) continue;
+#else
       for (int i = tid; i < total; i += NT) {
+#endif
         const int k = (i < c0) ? 0 : (i < c01) ? 1 : (i < c012) ? 2 : 3;
         const int r = i - ((k == 0) ? 0 : (k == 1) ? c0 : (k == 2) ? c01 : c012);
         const int j = s.items[k * np + r];
@@ -829,7 +876,7 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
   __shared__ volatile int s_moved;
-  __shared__ int s_cnt[4];
+  __shared__ int s_cnt[5];  // items per apex kind, then the next unclaimed item
   size_t off[6];
   check_offsets(a.max_slots_pad, a.max_local, a.max_owned, off);
   SmemCheck s;
@@ -868,7 +915,7 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
       continue;
     }
     if (tid == 0) s_moved = 0;
-    if (tid < 4) s_cnt[tid] = 0;
+    if (tid < 5) s_cnt[tid] = 0;
     __syncthreads();
     const int ns = bd.nslots, nown = bd.nowned, pitch = bd.nslots_pad;
     for (int j0 = 0; j0 < ns; j0 += NT) {
@@ -908,8 +955,18 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
     }
     __syncthreads();
     const int c0 = s_cnt[0], c01 = c0 + s_cnt[1], c012 = c01 + s_cnt[2], total = c012 + s_cnt[3];
+#if EIK_ITEM_STEAL
+    for (;;) {
+      int i0 = 0;
+      if (lane == 0) i0 = s_moved ? total : atomicAdd(&s_cnt[4], 32);
+      i0 = __shfl_sync(0xffffffffu, i0, 0);
+      if (i0 >= total) break;
+      const int i = i0 + lane;
+      if (i >= total) continue;
+#else
     for (int i = tid; i < total; i += NT) {
       if (s_moved) break;
+#endif
       const int k = (i < c0) ? 0 : (i < c01) ? 1 : (i < c012) ? 2 : 3;
       const int r = i - ((k == 0) ? 0 : (k == 1) ? c0 : (k == 2) ? c01 : c012);
       const int j = s.items[k * np + r];
@@ -1531,17 +1588,62 @@ __global__ void k_residual3d(DevArgs a, unsigned long long* cand) {
   }
 }
 
-// out[0] = max |T - cand|, out[1] = max |T - cand| / T (as FP64 bits), out[2] =
-// vertices above 1e-5 relative; seeds (T = 0) and unreached vertices are skipped.
+// The residual split by sign (FP64 bits where not a count): out[0] = max (T - c) and
+// out[1] = max (T - c) / T over vertices whose FP64 update c lies below T (more
+// updates would lower T), out[2] = those above 1e-5 relative, out[3] = max (c - T) / T
+// over vertices lying below every FP64 update of their tets (the local update is
+// not monotone in its inputs, so a time can end below the update of its final
+// neighbour times; the FP64 run of the scheme ends so too).  Seeds (T = 0) and
+// unreached vertices are skipped.
 __global__ void k_residual_reduce(DevArgs a, const unsigned long long* cand, unsigned long long* out) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x) {
     const double T = (double)a.Ta[v];
     const double c = __longlong_as_double((long long)cand[v]);
     if (!(T > 0.0) || T >= (double)kLarge3DDev || c >= 1e300) continue;
-    const double d = fabs(T - c), rel = d / T;
-    atomicMax(&out[0], (unsigned long long)__double_as_longlong(d));
-    atomicMax(&out[1], (unsigned long long)__double_as_longlong(rel));
-    if (rel > 1e-5) atomicAdd(&out[2], 1ull);
+    if (c < T) {
+      const double d = T - c, rel = d / T;
+      atomicMax(&out[0], (unsigned long long)__double_as_longlong(d));
+      atomicMax(&out[1], (unsigned long long)__double_as_longlong(rel));
+      if (rel > 1e-5) atomicAdd(&out[2], 1ull);
+    } else if (c > T) {
+      atomicMax(&out[3], (unsigned long long)__double_as_longlong((c - T) / T));
+    }
+  }
+}
+
+// Precision mode's polish, start of a round: the loop continues from the current
+// times with every slot's update in FP64; every instance runs again for at most
+// `cap` iterations; the active list of the coming iteration is rebuilt by
+// k_polish_mark.
+__global__ void k_polish_begin(DevArgs a, int cap) {
+  Ctl* c = a.ctl;
+  for (int i = threadIdx.x; i < a.ninst; i += blockDim.x) {
+    a.inst_done[i] = 0;
+    a.inst_iters[i] = 0;
+    a.inst_nnext[i] = 0;
+    a.inst_fail[i] = 0;
+    const_cast<int*>(a.inst_maxit)[i] = cap;
+  }
+  if (threadIdx.x == 0) {
+    c->max_iters = c->iter + cap;
+    c->nact = c->nnext = c->nnew = 0;
+    c->work_a = c->work_c = 0;
+    c->done_d = 0;
+    c->stop = 0;
+    c->f64_all = EIK_POLISH_F64ALL;
+  }
+}
+
+// Queues (once each, `mark` holding `tag`) the blocks owning a vertex whose FP64
+// update `cand` lies below its time by more than tol relative.
+__global__ void k_polish_mark(DevArgs a, const unsigned long long* cand, int* mark, int tag, double tol) {
+  int* list = act_list(a, a.ctl->iter);
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x) {
+    const double T = (double)a.Ta[v];
+    const double c = __longlong_as_double((long long)cand[v]);
+    if (!(T > 0.0) || T >= (double)kLarge3DDev || !(c < T * (1.0 - tol))) continue;
+    const int b = a.vblock[v];
+    if (atomicExch(&mark[b], tag) != tag) list[atomicAdd(&a.ctl->nact, 1)] = b;
   }
 }
 
@@ -1604,13 +1706,18 @@ __device__ __forceinline__ float uMw_rn(const float* u, const float* m, const fl
   return __fadd_rn(__fadd_rn(__fmul_rn(x, w[0]), __fmul_rn(y, w[1])), __fmul_rn(z, w[2]));
 }
 
-// `memo` (optional): check memos of the same slots, cleared with the new coefficients
+// `memo` (optional): check memos of the same slots, followed `memo_stride` entries
+// later by their sweep memos, cleared with the new coefficients
 __global__ void k_admit_coef3d(const BlockDesc* blocks, int nb, float* coef, const int* slot_elem, const float* xyz,
-                               const int* tets, const float* M, int mcomp, float k, uint4* memo) {
+                               const int* tets, const float* M, int mcomp, float k, uint4* memo,
+                               size_t memo_stride) {
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const BlockDesc d = blocks[b];
     for (int j = threadIdx.x; j < d.nslots; j += blockDim.x) {
-      if (memo) memo[d.slot_begin + j] = make_uint4(~0u, ~0u, ~0u, ~0u);
+      if (memo) {
+        memo[d.slot_begin + j] = make_uint4(~0u, ~0u, ~0u, ~0u);
+        memo[memo_stride + d.slot_begin + j] = make_uint4(~0u, ~0u, ~0u, ~0u);
+      }
       const int t = slot_elem[d.slot_begin + j];
       float P[4][3], m[6];
       for (int q = 0; q < 4; ++q) {
@@ -1771,6 +1878,15 @@ cudaError_t raise_smem_limit(const void* func, size_t bytes) {
   return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// CTA size of the item sweep and check kernels when the caller gives none
+constexpr int kItemThreads = 384;
+
+// Precision mode's polish: rounds, iterations per round, and the relative gap
+// between a vertex's time and its FP64 update above which its block runs again.
+constexpr int kPolishRounds = 8;
+constexpr int kPolishIterations = 1000;
+constexpr double kPolishTol = EIK_POLISH_TOL;
+
 // CTA sizes of the 3D visit kernels when the caller gives none.  One thread per
 // element slot of the largest block (up to 1024) runs every slot's updates side by
 // side; 512 threads lets two CTAs (64 registers per thread) share an SM and overlap
@@ -1848,7 +1964,7 @@ struct DeviceSolve::Impl {
   // measured so far and their sweep-kernel time per slot visit
   int tune_n[2] = {0, 0};
   float tune_cost[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-  uint4* chk_memo = nullptr;  // 3D: coef_n / 6 slots
+  uint4* chk_memo = nullptr;  // 3D: check memos of the coef_n / 6 slots, then their sweep memos
   // host staging for the initial state
   std::vector<float> h_prev;  // caller's initial values (renumbered), empty when none
   std::vector<int> h_seed_ids, h_act, h_vblock, h_done, h_maxit;
@@ -1857,7 +1973,7 @@ struct DeviceSolve::Impl {
   // precision mode
   int* slot_f64 = nullptr;
   double* coef64 = nullptr;
-  unsigned long long* res_cand = nullptr;  // nv + 3 words: per-vertex FP64 minimum, then the reduction
+  unsigned long long* res_cand = nullptr;  // nv + 4 words: per-vertex FP64 minimum, then the reduction
   bool prec = false;
   // graph
   cudaGraph_t graph = nullptr;
@@ -2025,6 +2141,9 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
         if (!P.prec && si + 64 <= (size_t)maxsm) vsmem = si;
         else if (!P.prec) kv_fim = (void*)k_visit3d<false>;
 #endif
+#if EIK_SWEEP_MEMO
+        if (kv_fim == (void*)k_sweep3d && P.chk_memo) a.fim_memo = P.chk_memo + P.coef_n / 6;
+#endif
 #if EIK_CHECK_ITEMS
         if (!P.prec && sc + 64 <= (size_t)maxsm) vsmem_chk = sc;
         else if (!P.prec) kv_chk = (void*)k_visit3d<true>;
@@ -2182,7 +2301,7 @@ std::string DeviceSolve::upload_built(const Layout& L, Built3D& b) {
   P.free_all();
   P.free_serve();
   L_ = &L;
-  P.dim = 3;
+  P.dim = b.dim;
   P.nv = L.nv;
   P.nb = L.nb;
   // the device arrays change owner here
@@ -2198,12 +2317,80 @@ std::string DeviceSolve::upload_built(const Layout& L, Built3D& b) {
   P.src.assign(1, Impl::Source{});
   P.src[0].xyz = b.xyz;
   P.src[0].tets = b.tets;
-  P.src[0].M6 = b.M6;
-  P.src[0].mcomp = b.mcomp;
-  P.coef_n = 6 * (size_t)b.total_slots;
+  if (b.dim == 3) {
+    P.src[0].M6 = b.M6;
+    P.src[0].mcomp = b.mcomp;
+  } else {
+    P.src[0].speed = b.M6;  // 2D: the face speeds
+  }
+  P.coef_n = (b.dim == 3 ? 6 : 4) * (size_t)b.total_slots;
   P.built = true;
   b = Built3D();
   return finish_upload(L, true);
+}
+
+// dst[i] = src[i] + add
+__global__ void k_offset_copy(int* dst, const int* src, int n, int add) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i] + add;
+}
+
+std::string DeviceSolve::upload_replicas(const Layout& L, const std::vector<const Built3D*>& parts) {
+  NvtxRange nvtx("eikonal: replicate device-built layouts");
+  Impl& P = *p_;
+  if (!stream_) return "CUDA stream creation failed (no usable GPU?)";
+  if ((int)parts.size() != L.ninst || (int)L.inst_bbeg.size() != L.ninst + 1) return "one part per instance expected";
+  P.free_all();
+  P.free_serve();
+  L_ = &L;
+  P.dim = L.dim;
+  P.nv = L.nv;
+  P.nb = L.nb;
+  const int ncoef = (L.dim == 3) ? 6 : 4;
+  long long nhalo = 0, nnbr = 0;
+  for (const Built3D* b : parts) {
+    if (!b || b->dim != L.dim) return "device-built part missing or of another dimension";
+    nhalo += b->nhalo;
+    nnbr += b->nnbr;
+  }
+  if (nhalo > 0x7fffffffll || nnbr > 0x7fffffffll) return "arena too large";
+  std::string e;
+  if (!(e = dev_alloc(P.blocks, L.nb)).empty()) return e;
+  if (!(e = dev_alloc(P.coef, (size_t)ncoef * L.total_slots)).empty()) return e;
+  if (!(e = dev_alloc(P.lv, (size_t)L.total_slots)).empty()) return e;
+  if (!(e = dev_alloc(P.slot_elem, (size_t)std::max(L.total_slots, 1))).empty()) return e;
+  if (!(e = dev_alloc(P.halo, (size_t)std::max(nhalo, 1ll))).empty()) return e;
+  if (!(e = dev_alloc(P.nbr_off, (size_t)L.nb + 1)).empty()) return e;
+  if (!(e = dev_alloc(P.nbr, (size_t)std::max(nnbr, 1ll))).empty()) return e;
+  if (!(e = dev_alloc(P.vblock, (size_t)L.nv)).empty()) return e;
+  if (!(e = dev_alloc(P.perm, (size_t)L.nv)).empty()) return e;
+  cudaStream_t st = (cudaStream_t)stream_;
+  CK(cudaMemcpyAsync(P.blocks, L.blocks.data(), sizeof(BlockDesc) * L.nb, cudaMemcpyHostToDevice, st));
+  long long soff = 0, hoff = 0, noff = 0;
+  auto grid = [](long long n) { return (int)std::max(1ll, std::min(4096ll, (n + 255) / 256)); };
+  for (int i = 0; i < L.ninst; ++i) {
+    const Built3D& b = *parts[i];
+    const int boff = L.inst_bbeg[i], nbi = L.inst_bbeg[i + 1] - boff, voff = L.inst_vbeg[i];
+    // per-block SoA runs are relative to the block's slot_begin, so a part's
+    // arrays move as a whole
+    CK(cudaMemcpyAsync(P.coef + (size_t)ncoef * soff, b.coef, sizeof(float) * ncoef * (size_t)b.total_slots,
+                       cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(P.lv + soff, b.lv, sizeof(uint2) * (size_t)b.total_slots, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(P.slot_elem + soff, b.slot_elem, sizeof(int) * (size_t)b.total_slots, cudaMemcpyDeviceToDevice,
+                       st));
+    if (b.nhalo) k_offset_copy<<<grid(b.nhalo), 256, 0, st>>>(P.halo + hoff, b.halo, b.nhalo, voff);
+    k_offset_copy<<<grid(nbi), 256, 0, st>>>(P.nbr_off + boff, b.nbr_off, nbi, (int)noff);
+    if (b.nnbr) k_offset_copy<<<grid(b.nnbr), 256, 0, st>>>(P.nbr + noff, b.nbr, b.nnbr, boff);
+    CK(cudaGetLastError());
+    soff += b.total_slots;
+    hoff += b.nhalo;
+    noff += b.nnbr;
+  }
+  if (soff != L.total_slots) return "parts do not match the concatenated layout";
+  const int last = (int)noff;
+  CK(cudaMemcpyAsync(P.nbr_off + L.nb, &last, sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  P.coef_n = (size_t)ncoef * L.total_slots;
+  return finish_upload(L, false);
 }
 
 bool DeviceSolve::layout_built_on_device() const { return p_->built; }
@@ -2217,9 +2404,27 @@ std::string DeviceSolve::layout_arrays(std::vector<float>* coef, std::vector<int
   }
   if (slot_elem) {
     if (!P.built || !P.slot_elem) return "element ids of the slots are kept on the host for this layout";
-    slot_elem->resize(P.coef_n / 6);
+    slot_elem->resize(P.coef_n / (P.dim == 3 ? 6 : 4));
     CK(cudaMemcpy(slot_elem->data(), P.slot_elem, sizeof(int) * slot_elem->size(), cudaMemcpyDeviceToHost));
   }
+  return "";
+}
+
+std::string DeviceSolve::refresh_speed_built(const float* speed) {
+  Impl& P = *p_;
+  if (!L_ || !P.built || P.src.empty() || P.dim != 2 || !P.src[0].speed) return "no device-built 2D layout";
+  const Layout& L = *L_;
+  cudaStream_t st = (cudaStream_t)stream_;
+  std::vector<float> ones;
+  if (!speed) {
+    ones.assign((size_t)L.ne, 1.0f);
+    speed = ones.data();
+  }
+  CK(cudaMemcpyAsync(P.src[0].speed, speed, sizeof(float) * (size_t)L.ne, cudaMemcpyHostToDevice, st));
+  k_admit_coef2d<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.slot_elem,
+                                                                    P.src[0].speed, 1.0f);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
   return "";
 }
 
@@ -2238,7 +2443,7 @@ std::string DeviceSolve::refresh_coef_built(const float* M, int mcomp) {
   }
   CK(cudaMemcpyAsync(src.M6, M, sizeof(float) * mcomp * (size_t)L.ne, cudaMemcpyHostToDevice, st));
   k_admit_coef3d<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.slot_elem, src.xyz,
-                                                                    src.tets, src.M6, src.mcomp, 1.0f, nullptr);
+                                                                    src.tets, src.M6, src.mcomp, 1.0f, nullptr, 0);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   return "";
@@ -2271,7 +2476,7 @@ std::string DeviceSolve::finish_upload(const Layout& L, bool layout_on_device) {
     if (L.dim != 3 || L.slot_f64.size() != (size_t)L.total_slots) return "precision data does not match the layout";
     if (!(e = dev_alloc(P.slot_f64, L.slot_f64.size())).empty()) return e;
     if (!(e = dev_alloc(P.coef64, std::max<size_t>(L.coef64.size(), 6))).empty()) return e;
-    if (!(e = dev_alloc(P.res_cand, (size_t)L.nv + 3)).empty()) return e;
+    if (!(e = dev_alloc(P.res_cand, (size_t)L.nv + 4)).empty()) return e;
     CK(cudaMemcpyAsync(P.slot_f64, L.slot_f64.data(), sizeof(int) * L.slot_f64.size(), cudaMemcpyHostToDevice, st));
     if (!L.coef64.empty())
       CK(cudaMemcpyAsync(P.coef64, L.coef64.data(), sizeof(double) * L.coef64.size(), cudaMemcpyHostToDevice, st));
@@ -2371,7 +2576,18 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   int threads = given ? opt.threads : full_visit_threads(P.max_slots_pad);
   int tune_slot = -1;  // which candidate CTA size this solve measures
   const int tq = P.prec ? 1 : 0;
-  if (!given && L.dim == 3) {
+  bool items = false;  // the item sweep and check kernels run (their shared memory fits)
+  if (L.dim == 3 && !P.prec && EIK_SWEEP_ITEMS) {
+    int maxsm = 0, dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    items = smem_bytes_items(P.max_slots_pad, P.max_local, P.max_owned) + 64 <= (size_t)maxsm;
+  }
+  if (!given && items) {
+    // item kernels: 384-thread CTAs, three per SM where their shared memory allows
+    // (65^3 workload: solve 7.85 ms against 7.93 at 512 and 8.4 at one thread per slot)
+    threads = kItemThreads;
+  } else if (!given && L.dim == 3) {
     const int full = threads, half = auto_visit_threads(P.max_slots_pad);
     if (half < full) {
       if (P.tune_n[tq] < 3) {  // 0: warm-up, 1: measure 512, 2: measure the full size
@@ -2440,11 +2656,11 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   // 3D check memos (16 B per slot) hold only for this solve's coefficients and kernel
   if (L.dim == 3) {
     if (!P.chk_memo) {
-      std::string e = dev_alloc(P.chk_memo, P.coef_n / 6);
+      std::string e = dev_alloc(P.chk_memo, 2 * (P.coef_n / 6));
       if (!e.empty()) return e;
       P.drop_graph();
     }
-    CK(cudaMemsetAsync(P.chk_memo, 0xff, sizeof(uint4) * (P.coef_n / 6), st));
+    CK(cudaMemsetAsync(P.chk_memo, 0xff, sizeof(uint4) * 2 * (P.coef_n / 6), st));
   }
   {
     std::vector<int> done(P.h_done);
@@ -2471,10 +2687,12 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     std::string e = P.build_graph(L, sweeps, threads, hcap, false);
     if (!e.empty()) return e;
   }
-  CK(cudaEventRecord(P.ev0, st));
-  if (!opt.direct_launch) {
-    CK(cudaGraphLaunch(P.exec, st));
-  } else {
+  // the device loop from the control block's current state
+  auto run_loop = [&]() -> std::string {
+    if (!opt.direct_launch) {
+      CK(cudaGraphLaunch(P.exec, st));
+      return "";
+    }
     // the graph's kernels launched one by one, the host reading the control block
     // between iterations (profilers cannot see kernels inside conditional graphs)
     DevArgs d = P.args;
@@ -2483,12 +2701,46 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
       Ctl h{};
       CK(cudaMemcpyAsync(&h, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      if (h.stop || h.error || h.nact <= 0 || h.iter >= max_iters) break;
+      if (h.stop || h.error || h.nact <= 0 || h.iter >= h.max_iters) break;
       for (const Impl::Launch& l : P.body) {
         void* args[2] = {&d, (void*)&l.extra};
         CK(cudaLaunchKernel(l.func, dim3(l.grid), dim3(l.block), args, l.smem, st));
       }
       CK(cudaGetLastError());
+    }
+    return "";
+  };
+  CK(cudaEventRecord(P.ev0, st));
+  {
+    std::string e = run_loop();
+    if (!e.empty()) return e;
+  }
+  // Precision mode acts on its FP64 residual: the blocks owning a vertex that the
+  // FP64 update of its tets would lower run the loop again, every slot in FP64,
+  // until no such vertex is left (or kPolishRounds rounds).  With no tet flagged
+  // the caller asked for FP32 throughout, and nothing is re-visited.
+  stats_.polish_rounds = 0;
+  stats_.polish_blocks = 0;
+  if (P.prec && P.res_cand && L.flagged_tets > 0) {
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    for (int round = 0; round < kPolishRounds; ++round) {
+      CK(cudaMemsetAsync(P.res_cand, 0x7f, sizeof(unsigned long long) * L.nv, st));
+      k_residual3d<<<std::max(1, std::min(L.nb, 8 * nsm)), 256, 0, st>>>(P.args, P.res_cand);
+      k_polish_begin<<<1, 256, 0, st>>>(P.args, kPolishIterations);
+      k_polish_mark<<<std::max(1, std::min(4 * nsm, (L.nv + 255) / 256)), 256, 0, st>>>(P.args, P.res_cand, P.stampC,
+                                                                                      -(round + 1), kPolishTol);
+      CK(cudaGetLastError());
+      Ctl h{};
+      CK(cudaMemcpyAsync(&h, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      if (h.error || h.nact == 0) break;
+      if (P.chk_memo) CK(cudaMemsetAsync(P.chk_memo, 0xff, sizeof(uint4) * 2 * (P.coef_n / 6), st));
+      std::string e = run_loop();
+      if (!e.empty()) return e;
+      stats_.polish_rounds = round + 1;
+      stats_.polish_blocks += h.nact;
     }
   }
   CK(cudaEventRecord(P.ev1, st));
@@ -2536,12 +2788,12 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     stats_.fim_launches = nf;
     stats_.check_launches = nc;
   }
-  stats_.residual_max_abs = stats_.residual_max_rel = 0;
+  stats_.residual_max_abs = stats_.residual_max_rel = stats_.residual_below_rel = 0;
   stats_.residual_vertices = 0;
   if (P.prec && P.res_cand && !out.error) {
     // FP64 residual of the final travel times (after the timed region)
     CK(cudaMemsetAsync(P.res_cand, 0x7f, sizeof(unsigned long long) * L.nv, st));
-    CK(cudaMemsetAsync(P.res_cand + L.nv, 0, sizeof(unsigned long long) * 3, st));
+    CK(cudaMemsetAsync(P.res_cand + L.nv, 0, sizeof(unsigned long long) * 4, st));
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -2549,15 +2801,17 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     k_residual_reduce<<<std::max(1, std::min(4 * nsm, (L.nv + 255) / 256)), 256, 0, st>>>(P.args, P.res_cand,
                                                                                        P.res_cand + L.nv);
     CK(cudaGetLastError());
-    unsigned long long r[3];
+    unsigned long long r[4];
     CK(cudaMemcpyAsync(r, P.res_cand + L.nv, sizeof(r), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    double d0, d1;
+    double d0, d1, d3;
     std::memcpy(&d0, &r[0], sizeof(double));
     std::memcpy(&d1, &r[1], sizeof(double));
+    std::memcpy(&d3, &r[3], sizeof(double));
     stats_.residual_max_abs = d0;
     stats_.residual_max_rel = d1;
     stats_.residual_vertices = (long long)r[2];
+    stats_.residual_below_rel = d3;
   }
   if (out.error) return "device reported error flags " + std::to_string(out.error);
   return "";
@@ -2672,12 +2926,45 @@ std::string selftest_tri_blocks(const float* in, int n, bool check, float* out) 
   return ds.visit_once(check, T.data(), out);
 }
 
-size_t device_footprint(const Layout& L) {
+size_t device_footprint(const Layout& L, const Built3D* b) {
   const size_t nv = (size_t)L.nv, nb = (size_t)L.nb;
-  return nb * sizeof(BlockDesc) + L.coef.size() * sizeof(float) + (size_t)L.total_slots * (sizeof(uint2) + sizeof(int)) +
-         (L.dim == 3 ? (size_t)L.total_slots * sizeof(uint4) : 0) +
-         L.halo_ids.size() * sizeof(int) + (L.nbr_off.size() + L.nbr.size()) * sizeof(int) +
+  const size_t ncoef = b ? (size_t)(L.dim == 3 ? 6 : 4) * L.total_slots : L.coef.size();
+  const size_t nhalo = b ? (size_t)b->nhalo : L.halo_ids.size();
+  const size_t ngraph = b ? nb + 1 + (size_t)b->nnbr : L.nbr_off.size() + L.nbr.size();
+  return nb * sizeof(BlockDesc) + ncoef * sizeof(float) + (size_t)L.total_slots * (sizeof(uint2) + sizeof(int)) +
+         (L.dim == 3 ? 2 * (size_t)L.total_slots * sizeof(uint4) : 0) + nhalo * sizeof(int) + ngraph * sizeof(int) +
          nv * (2 * sizeof(int) + 5 * sizeof(float)) + nb * (7 * sizeof(int) + 1) + 5 * sizeof(int);
+}
+
+cudaStream_t new_stream() {
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  return st;
+}
+
+void free_stream(cudaStream_t st) {
+  if (st) cudaStreamDestroy(st);
+}
+
+std::string download_built(const Built3D& b, Layout& L) {
+  const int ncoef = (L.dim == 3) ? 6 : 4;
+  L.coef.resize((size_t)ncoef * L.total_slots);
+  L.lv.resize(4 * (size_t)L.total_slots);
+  L.slot_elem.resize((size_t)L.total_slots);
+  L.halo_ids.resize((size_t)b.nhalo);
+  L.nbr_off.resize((size_t)L.nb + 1);
+  L.nbr.resize((size_t)b.nnbr);
+  CK(cudaMemcpy(L.coef.data(), b.coef, sizeof(float) * L.coef.size(), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(L.lv.data(), b.lv, sizeof(uint16_t) * L.lv.size(), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(L.slot_elem.data(), b.slot_elem, sizeof(int) * L.slot_elem.size(), cudaMemcpyDeviceToHost));
+  if (b.nhalo) CK(cudaMemcpy(L.halo_ids.data(), b.halo, sizeof(int) * L.halo_ids.size(), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(L.nbr_off.data(), b.nbr_off, sizeof(int) * L.nbr_off.size(), cudaMemcpyDeviceToHost));
+  if (b.nnbr) CK(cudaMemcpy(L.nbr.data(), b.nbr, sizeof(int) * L.nbr.size(), cudaMemcpyDeviceToHost));
+  if (L.iperm.size() != (size_t)L.nv) {
+    L.iperm.assign(L.nv, 0);
+    for (int v = 0; v < L.nv; ++v) L.iperm[L.perm[v]] = v;
+  }
+  return "";
 }
 
 std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, const std::vector<int>& inst_mesh,
@@ -2689,7 +2976,12 @@ std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, con
   for (int m : inst_mesh)
     if (m < 0 || m >= (int)meshes.size()) return "pool mesh id out of range";
   cudaStream_t st = (cudaStream_t)stream_;
+  // an arena replicated on the device (upload_replicas) brings its slots' element
+  // ids; a host-built one has them in L
+  int* replica_elems = (L.slot_elem.empty() && P.slot_elem) ? P.slot_elem : nullptr;
+  if (replica_elems) P.slot_elem = nullptr;
   P.free_serve();
+  P.slot_elem = replica_elems;
   P.src.resize(meshes.size());
   for (size_t m = 0; m < meshes.size(); ++m) {
     const ServeSource& x = meshes[m];
@@ -2709,15 +3001,17 @@ std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, con
     }
   }
   P.inst_mesh = inst_mesh;
-  {
+  if (!replica_elems) {
+    if (L.slot_elem.size() != (size_t)L.total_slots) return "element ids of the slots missing";
     std::string e;
     if (!(e = dev_alloc(P.slot_elem, (size_t)std::max(L.total_slots, 1))).empty()) return e;
+    CK(cudaMemcpyAsync(P.slot_elem, L.slot_elem.data(), sizeof(int) * L.slot_elem.size(), cudaMemcpyHostToDevice,
+                       st));
   }
-  CK(cudaMemcpyAsync(P.slot_elem, L.slot_elem.data(), sizeof(int) * L.slot_elem.size(), cudaMemcpyHostToDevice, st));
   if (L.dim == 3) {
     std::string e;
-    if (!P.chk_memo && !(e = dev_alloc(P.chk_memo, P.coef_n / 6)).empty()) return e;
-    CK(cudaMemsetAsync(P.chk_memo, 0xff, sizeof(uint4) * (P.coef_n / 6), st));
+    if (!P.chk_memo && !(e = dev_alloc(P.chk_memo, 2 * (P.coef_n / 6))).empty()) return e;
+    CK(cudaMemsetAsync(P.chk_memo, 0xff, sizeof(uint4) * 2 * (P.coef_n / 6), st));
   }
   CK(cudaHostAlloc((void**)&P.host_res, sizeof(float) * std::max(L.nv, 1), cudaHostAllocDefault));
   if (!P.pending_host) {
@@ -2740,9 +3034,17 @@ std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, con
   Ctl c{};
   c.max_iters = 1 << 30;
   CK(cudaMemcpyAsync(P.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st));
-  const int th = (threads == 128 || threads == 256 || threads == 512 || threads == 1024)
-                     ? threads
-                     : auto_visit_threads(P.max_slots_pad);
+  const bool given = threads == 128 || threads == 256 || threads == 384 || threads == 512 || threads == 768 ||
+                     threads == 1024;
+  int th = given ? threads : auto_visit_threads(P.max_slots_pad);
+  if (!given && L.dim == 3 && EIK_SWEEP_ITEMS) {
+    // the item kernels run where their shared memory fits, at the CTA size a
+    // plain solve uses
+    int dev = 0, maxsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (smem_bytes_items(P.max_slots_pad, P.max_local, P.max_owned) + 64 <= (size_t)maxsm) th = kItemThreads;
+  }
   const int sw = (sweeps > 0) ? sweeps : (L.dim == 3 ? 2 : 7);
   std::string e = P.build_graph(L, sw, th, 0, true);
   if (!e.empty()) return e;
@@ -2800,7 +3102,7 @@ std::string DeviceSolve::serve_admit(const std::vector<Admission>& adm) {
     const int g = std::max(1, std::min(nbi, 4096));
     if (L.dim == 3)
       k_admit_coef3d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.xyz, src.tets, src.M6,
-                                        src.mcomp, x.coef_scale, P.chk_memo);
+                                        src.mcomp, x.coef_scale, P.chk_memo, P.coef_n / 6);
     else
       k_admit_coef2d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.speed, x.coef_scale);
     k_admit_seeds<<<1, 256, 0, st>>>(P.args, i, P.seed_ids + off[q], nsd[q], P.seed_ids + boff[q], nbk[q],

@@ -285,7 +285,7 @@ int eik_server_add_mesh(eik_server* s, eik_solver* h, int slots, int* mesh_id) {
   int rc = snapshot_for_server(h, m.snap, e);
   if (rc) return sfail(s, rc, e);
   m.slots_req = slots;
-  m.bytes = device_footprint(m.snap.layout);
+  m.bytes = device_footprint(m.snap.layout, m.snap.built.get());
   m.arena = (m.snap.dim == 2) ? 0 : 1;
   s->meshes.push_back(std::move(m));
   if (mesh_id) *mesh_id = (int)s->meshes.size() - 1;
@@ -362,13 +362,39 @@ int eik_server_start(eik_server* s) {
       A.bytes += (size_t)m.slots * m.bytes;
     }
     if (!A.used) continue;
-    std::string e = concat_layouts(parts, A.L);
-    if (!e.empty()) return sfail(s, EIK_ERR_ARG, e);
+    // pool meshes built on the device are replicated there; an arena that also
+    // holds host-built meshes is concatenated on the host
+    bool all_built = true;
+    for (const PoolMesh& m : s->meshes)
+      if (m.arena == ai && !m.snap.built) all_built = false;
+    std::string e;
     A.dev.reset(new DeviceSolve);
-    e = A.dev->upload(A.L);
+    if (all_built) {
+      std::vector<const Built3D*> bparts;
+      std::vector<int> nhalo;
+      for (int mi : A.inst_mesh) {
+        bparts.push_back(s->meshes[mi].snap.built.get());
+        nhalo.push_back(s->meshes[mi].snap.built->nhalo);
+      }
+      e = concat_layout_headers(parts, nhalo, A.L);
+      if (!e.empty()) return sfail(s, EIK_ERR_ARG, e);
+      e = A.dev->upload_replicas(A.L, bparts);
+    } else {
+      for (PoolMesh& m : s->meshes)
+        if (m.arena == ai && m.snap.built) {
+          e = download_built(*m.snap.built, m.snap.layout);
+          if (!e.empty()) return sfail(s, EIK_ERR_CUDA, e);
+          m.snap.built.reset();
+        }
+      e = concat_layouts(parts, A.L);
+      if (!e.empty()) return sfail(s, EIK_ERR_ARG, e);
+      e = A.dev->upload(A.L);
+    }
     if (!e.empty()) return sfail(s, e.find("shared memory") != std::string::npos ? EIK_ERR_LIMIT : EIK_ERR_CUDA, e);
     e = A.dev->serve_setup(src, local_mesh, sweeps, threads);
     if (!e.empty()) return sfail(s, EIK_ERR_CUDA, e);
+    for (PoolMesh& m : s->meshes)
+      if (m.arena == ai) m.snap.built.reset();  // replicated: the arena holds the arrays now
     A.inst_req.assign(parts.size(), -1);
     A.pending = A.dev->serve_pending();
   }

@@ -895,4 +895,42 @@ std::string concat_layouts(const std::vector<const Layout*>& parts, Layout& out)
   return "";
 }
 
+std::string concat_layout_headers(const std::vector<const Layout*>& parts, const std::vector<int>& nhalo,
+                                  Layout& out) {
+  out = Layout();
+  if (parts.empty()) return "no instances";
+  if (nhalo.size() != parts.size()) return "one halo length per instance expected";
+  const int dim = parts[0]->dim;
+  out.dim = dim;
+  out.inst_bbeg.push_back(0);
+  out.inst_vbeg.push_back(0);
+  long long hoff = 0;
+  for (size_t i = 0; i < parts.size(); ++i) {
+    const Layout* p = parts[i];
+    if (p->dim != dim) return "instances of different dimension";
+    const int voff = out.nv, soff = out.total_slots;
+    for (int v : p->perm) out.perm.push_back(v + voff);
+    for (BlockDesc d : p->blocks) {
+      d.slot_begin += soff;
+      d.vbase += voff;
+      d.halo_begin += (int)hoff;
+      out.blocks.push_back(d);
+    }
+    hoff += nhalo[i];
+    if (hoff > 0x7fffffffll) return "halo lists too long";
+    out.nb += p->nb;
+    out.nv += p->nv;
+    out.ne += p->ne;
+    out.total_slots += p->total_slots;
+    out.inst_bbeg.push_back(out.nb);
+    out.inst_vbeg.push_back(out.nv);
+  }
+  out.ninst = (int)parts.size();
+  out.blk_inst.assign(out.nb, 0);
+  for (int i = 0; i < out.ninst; ++i)
+    for (int b = out.inst_bbeg[i]; b < out.inst_bbeg[i + 1]; ++b) out.blk_inst[b] = i;
+  finish_stats(out);
+  return "";
+}
+
 }  // namespace eikgb

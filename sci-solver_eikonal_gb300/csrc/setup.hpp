@@ -124,6 +124,13 @@ struct Layout {
 // One layout holding several independent meshes (same dimension), instance by
 // instance; the neighbour graph never crosses instances.
 std::string concat_layouts(const std::vector<const Layout*>& parts, Layout& out);
+// The host part of concat_layouts for layouts whose arrays live on the device:
+// block descriptors (offset), renumbering, instance ranges and statistics; the
+// per-slot arrays, halo lists and neighbour graph stay empty.  nhalo[i] is the
+// halo list length of part i (its blocks' halo ranges are offset by the sum of
+// the earlier ones).
+std::string concat_layout_headers(const std::vector<const Layout*>& parts, const std::vector<int>& nhalo,
+                                  Layout& out);
 
 // 3D layout; gram terms computed from xyz and per-tet metrics.
 std::string build_layout3d(int nv, const float* xyz, int nt, const int* tets, const float* M,

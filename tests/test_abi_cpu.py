@@ -190,6 +190,13 @@ def test_server_host_side_and_no_gpu_failure(eik, mg):
     xyz, faces = mg.icosphere(2)
     a = eik.Eikonal(True)
     a.set_mesh(xyz, faces)
+    if not gpu_available():
+        # a handle that builds its layout on the device needs the GPU already
+        srv = eik.EikonalServer(hbm_budget_bytes=1 << 26)
+        with pytest.raises(eik.EikonalError):
+            srv.add_mesh(a)
+        srv.close()
+    a.deviceSetup_ = 0  # host build: adding a mesh is host work
     srv = eik.EikonalServer(hbm_budget_bytes=1 << 26)
     mid = srv.add_mesh(a)
     info = srv.mesh_info(mid)
@@ -241,6 +248,7 @@ def test_server_rejects_pool_over_budget(eik, mg):
     xyz, faces = mg.icosphere(3)
     a = eik.Eikonal(True)
     a.set_mesh(xyz, faces)
+    a.deviceSetup_ = 0  # host build: the budget check needs no GPU
     srv = eik.EikonalServer(hbm_budget_bytes=1000)
     srv.add_mesh(a)
     with pytest.raises(eik.EikonalError) as ei:

@@ -121,3 +121,40 @@ def test_autotuner_picks_a_measured_shape_and_keeps_results(need_gpu, eik, mg):
         assert e.maxVertsPerBlock_ == res.verts_per_block
         want, it = _alone(e)
         assert bits_equal(batch.getFinalResult(i), want)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_batch_device_build_equals_host_build(need_gpu, eik, mg, dim):
+    """A batch whose handles build on the device builds one layout for all
+    instances there (the meshes as one disconnected mesh); it equals the
+    concatenated host layouts, and every instance its standalone solve."""
+    rng = np.random.default_rng(30 + dim)
+    if dim == 2:
+        solvers = [_sphere_solver(eik, mg, lv, rng.choice(10 * 4 ** lv + 2, size=3, replace=False))
+                   for lv in (3, 1, 4, 2, 3)]
+        solvers[2].initSpeedMtxMultipliers(np.ones(0, np.float32))  # default speeds on one instance
+    else:
+        solvers = [_cube_solver(eik, mg, n, 40 + n, rng.choice(n ** 3, size=2, replace=False)) for n in (9, 13, 11)]
+        # one instance with 6-entry metrics: the device pass expands the others' scalars
+        xyz, tets = mg.kuhn_cube(10, 0.2, seed=7)
+        e = eik.Eikonal(False)
+        e.set_mesh(xyz, tets)
+        e.initSpeedMtxMultipliers(mg.anisotropic_metrics(tets.shape[0], seed=8).ravel())
+        e.setSeeds([3])
+        solvers.insert(1, e)
+    runs = {}
+    for dev in (1, 0):
+        for e in solvers:
+            e.deviceSetup_ = dev
+        b = eik.EikonalBatch(solvers)
+        b.solveEikonal()
+        runs[dev] = (b.getFinalResults(), [b.numIterations(i) for i in range(len(solvers))], b.stats())
+    for i in range(len(solvers)):
+        assert bits_equal(runs[1][0][i], runs[0][0][i]), i
+    assert runs[1][1] == runs[0][1]
+    for k in ("num_blocks", "total_slots", "vertex_updates", "fim_visits", "check_visits", "max_slots_per_block"):
+        assert runs[1][2][k] == runs[0][2][k], (k, runs[1][2][k], runs[0][2][k])
+    for i, e in enumerate(solvers):
+        e.deviceSetup_ = 1
+        res, it = _alone(e)
+        assert it == runs[1][1][i] and bits_equal(res, runs[1][0][i]), i

@@ -84,3 +84,45 @@ def test_device_layout_user_partition_and_speed_change(need_gpu, eik, mg):
     a.deviceSetup_ = 1
     a.solveEikonal()
     _same(a, c)
+
+
+def _solve2d(eik, xyz, faces, speeds, seeds, device, opts):
+    e = eik.Eikonal(True)
+    e.set_mesh(xyz, faces)
+    if speeds is not None:
+        e.initSpeedMtxMultipliers(speeds)
+    e.setSeeds(list(seeds))
+    for k, v in opts.items():
+        setattr(e, k, v)
+    e.deviceSetup_ = 1 if device else 0
+    e.solveEikonal()
+    return e
+
+
+@pytest.mark.parametrize("case", ["grid", "ico", "sphere_speed", "square_structured"])
+def test_device_layout_2d_equals_host_layout(need_gpu, eik, mg, golden, case):
+    # triangle meshes: slots (inside, shared, virtual faces of obtuse corners),
+    # halo lists, inverse face speeds and the copies the reference never refreshes
+    if case == "grid":
+        xyz, f = mg.grid2d(41)
+        args = (None, [0, 700], {"maxVertsPerBlock_": 16})
+    elif case == "ico":
+        xyz, f = mg.icosphere(5)
+        args = (mg.batch_speed(xyz, f), [0, 7], {"maxVertsPerBlock_": 32})
+    elif case == "sphere_speed":
+        xyz, f = golden["sphere_1154verts_xyz"], golden["sphere_1154verts_faces"]
+        args = (mg.batch_speed(xyz, f), [0, 500], {"maxVertsPerBlock_": 32})
+    else:
+        xyz, f = golden["SquareMesh_size16_xyz"], golden["SquareMesh_size16_faces"]
+        args = (None, [0], {"isStructured_": 1, "squareBlockLength_": 4, "squareBlockWidth_": 4})
+    sp, seeds, opts = args
+    a = _solve2d(eik, xyz, f, sp, seeds, True, opts)
+    b = _solve2d(eik, xyz, f, sp, seeds, False, opts)
+    _same(a, b)
+    # new face speeds on the same handles: the device path recomputes them on the GPU
+    sp2 = np.random.default_rng(len(f)).uniform(0.5, 2.0, len(f)).astype(np.float32)
+    for e in (a, b):
+        e.initSpeedMtxMultipliers(sp2)
+        e.solveEikonal()
+    _same(a, b)
+    _same(a, _solve2d(eik, xyz, f, sp2, seeds, True, opts))

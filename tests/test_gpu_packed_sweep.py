@@ -1,7 +1,8 @@
-"""The 3D sweep kernel runs the last sweep of a visit from a packed list of the slots
-that can still change an owned vertex; the precision kernel keeps the plain loop over
-every slot.  With nothing flagged the precision kernel computes the FP32 updates, so
-the two must agree bit for bit for any number of sweeps per visit."""
+"""The 3D sweep kernel runs a visit's sweeps from lists of the apex updates that can
+change something (exact skips: inputs at LARGENUM, unchanged inputs, upwind apexes,
+non-owned apexes in the last sweep); the precision kernel keeps the loop over every
+slot.  With nothing flagged the precision kernel computes the FP32 updates, so the
+two must agree bit for bit for any number of sweeps per visit."""
 import numpy as np
 import pytest
 
@@ -41,13 +42,14 @@ def test_packed_last_sweep_equals_plain_loop(need_gpu, eik, mg, O, sweeps):
 
 
 def test_cta_size_does_not_change_results(need_gpu, eik, mg):
-    """Blocks larger than the CTA run several slots per thread in every loop (the
-    packed list, the check memo, the copies); the results must not depend on it."""
+    """Blocks larger than the CTA run several slots or apex items per thread in
+    every loop (the item lists, the check memo, the copies); the results must not
+    depend on the CTA size."""
     xyz, tets = mg.kuhn_cube(25, 0.2, seed=31)
     sp = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=32)
     metric = (1.0 / sp.astype(np.float64) ** 2).astype(np.float32)
     out = []
-    for threads in (0, 256, 128):
+    for threads in (0, 256, 128, 384, 512, 768, 1024):
         e = eik.Eikonal(False)
         e.set_mesh(xyz, tets)
         e.initSpeedMtxMultipliers(metric)
@@ -64,8 +66,8 @@ def test_cta_size_does_not_change_results(need_gpu, eik, mg):
 
 
 def test_cta_size_choice_over_the_first_solves_keeps_the_bits(need_gpu, eik, mg):
-    """With no CTA size given, a handle's first solves run 512 and one thread per
-    slot to pick the faster; every solve gives the same bits."""
+    """With no CTA size given a handle runs the item kernels' size (or, in precision
+    mode, tries two sizes over its first solves); every solve gives the same bits."""
     xyz, tets = mg.kuhn_cube(25, 0.2, seed=41)
     sp = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=42)
     metric = (1.0 / sp.astype(np.float64) ** 2).astype(np.float32)

@@ -133,3 +133,29 @@ def test_submit_rejects_bad_requests(need_gpu, eik, mg):
     c = srv.poll()
     assert len(c) == 1 and c[0]["id"] == r and c[0]["status"] == 0
     srv.close()
+
+
+def test_device_and_host_built_arenas_agree(need_gpu, eik, mg):
+    """Pool meshes whose handles build on the device are replicated into the arena
+    on the device; host-built ones are concatenated on the host; an arena holding
+    both brings the device-built ones back to the host first.  All three give the
+    same slot sizes and the same bits."""
+    reqs = None
+    runs = []
+    for mode in ("device", "host", "mixed"):
+        pool = _pool(eik, mg)
+        for k, p in enumerate(pool):
+            p["solver"].deviceSetup_ = {"device": 1, "host": 0, "mixed": k % 2}[mode]
+        if reqs is None:
+            reqs = _requests(pool, 16, seed=9)
+        srv = eik.EikonalServer(hbm_budget_bytes=1 << 30)
+        ids = [srv.add_mesh(p["solver"]) for p in pool]
+        info = [srv.mesh_info(i) for i in ids]
+        srv.close()
+        out, st = _serve(eik, pool, reqs, max_inflight=0)
+        runs.append((info, out))
+    for info, out in runs[1:]:
+        assert [x["device_bytes"] for x in info] == [x["device_bytes"] for x in runs[0][0]]
+        for i, ((ra, ia), (rb, ib)) in enumerate(zip(runs[0][1], out)):
+            assert ia == ib, i
+            assert bits_equal(ra, rb), i
