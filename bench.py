@@ -402,9 +402,9 @@ def launch_dram(name):
 def sweep_bytes(it):
     """Algorithmic bytes of one sweep-kernel launch from its iteration's counters
     (Eikonal.iterationStats columns): per slot 6 float metric terms + 4 u16 corner
-    ids (32 B), owned + halo travel times read (4 B each), owned times written (4 B),
-    one block flag (4 B) per visit."""
-    return 32 * it[3] + 4 * (it[5] + it[4]) + 4 * it[5] + 4 * it[2]
+    ids (32 B) and its sweep memo read and written (16 B each), owned + halo travel
+    times read (4 B each), owned times written (4 B), one block flag (4 B) per visit."""
+    return 64 * it[3] + 4 * (it[5] + it[4]) + 4 * it[5] + 4 * it[2]
 
 
 def check_bytes(it):
@@ -1024,7 +1024,11 @@ def pattern_summaries(args, E, torch, local):
                          "ratio_at_top_rate": sv["served_over_plain"],
                          "ratio_per_rate": sv["served_over_plain_per_rate"], "slots": sv["served"]["slots"],
                          "device_bytes": sv["served"]["device_bytes"], "hbm_budget_gb": args.serve_budget_gb,
-                         "setup_s": sv["served"]["setup_s"], "startup": sv["startup"]}
+                         "setup_s": sv["served"]["setup_s"], "startup": sv["startup"],
+                         "device_loops": {m: sv[m]["device_loops"] for m in ("served", "plain")},
+                         "arena_busy_s": {m: sv[m]["arena_busy_s"] for m in ("served", "plain")},
+                         "arena_vertex_updates_per_busy_s": {m: sv[m]["arena_vertex_updates_per_busy_s"]
+                                                             for m in ("served", "plain")}}
     except Exception as ex:
         out["served"] = {"error": repr(ex)}
     try:

@@ -232,25 +232,41 @@ constexpr unsigned long long kFuseApexB = 0x6301902630000ull;  // B from A, D, C
 constexpr unsigned long long kFuseApexC = 0x4203182420002ull;  // C from A, B, D
 constexpr unsigned long long kFuseApexD = 0x0000001100000000ull;  // D from A, B, C
 
-template <unsigned long long M, int S>
-__device__ __forceinline__ float x_ms(float x, float y, float z, float w) {  // x*y - z*w
-  if constexpr (((M >> S) & 1ull) != 0) return __fmaf_rn(-z, w, __fmul_rn(x, y));
-  else return __fmaf_rn(x, y, -__fmul_rn(z, w));
+// Sites in R take their choice from the runtime mask m instead of M (one body
+// serving several masks): the same two operations, operands picked by selects.
+template <unsigned long long M, unsigned long long R, int S>
+__device__ __forceinline__ float x_ms(unsigned long long m, float x, float y, float z, float w) {  // x*y - z*w
+  if constexpr (((R >> S) & 1ull) != 0) {
+    const bool b = ((m >> S) & 1ull) != 0;
+    const float pr = __fmul_rn(b ? x : z, b ? y : w);
+    return __fmaf_rn(b ? -z : x, b ? w : y, b ? pr : -pr);
+  } else if constexpr (((M >> S) & 1ull) != 0) {
+    return __fmaf_rn(-z, w, __fmul_rn(x, y));
+  } else {
+    return __fmaf_rn(x, y, -__fmul_rn(z, w));
+  }
 }
-template <unsigned long long M, int S>
-__device__ __forceinline__ float x_ma(float x, float y, float z, float w) {  // x*y + z*w
-  if constexpr (((M >> S) & 1ull) != 0) return __fmaf_rn(z, w, __fmul_rn(x, y));
-  else return __fmaf_rn(x, y, __fmul_rn(z, w));
+template <unsigned long long M, unsigned long long R, int S>
+__device__ __forceinline__ float x_ma(unsigned long long m, float x, float y, float z, float w) {  // x*y + z*w
+  if constexpr (((R >> S) & 1ull) != 0) {
+    const bool b = ((m >> S) & 1ull) != 0;
+    const float pr = __fmul_rn(b ? x : z, b ? y : w);
+    return __fmaf_rn(b ? z : x, b ? w : y, pr);
+  } else if constexpr (((M >> S) & 1ull) != 0) {
+    return __fmaf_rn(z, w, __fmul_rn(x, y));
+  } else {
+    return __fmaf_rn(x, y, __fmul_rn(z, w));
+  }
 }
 // (l1*XX + l2*XY + XZ)*l1 + (l1*XY + l2*YY + YZ)*l2 + (l1*XZ + l2*YZ + ZZ): the metric
 // length of the path from the apex to the point l1 A + l2 B + l3 C (sites S..S+3)
-template <unsigned long long M, int S>
-__device__ __forceinline__ float x_dist3(float l1, float l2, float ACAC, float ACBC, float ACCD, float BCBC,
-                                         float BCCD, float CDCD) {
-  const float X = __fadd_rn(x_ma<M, S>(l1, ACAC, l2, ACBC), ACCD);
-  const float Y = __fadd_rn(x_ma<M, S + 1>(l1, ACBC, l2, BCBC), BCCD);
-  const float Z = __fadd_rn(x_ma<M, S + 2>(l1, ACCD, l2, BCCD), CDCD);
-  return __fadd_rn(x_ma<M, S + 3>(X, l1, Y, l2), Z);
+template <unsigned long long M, unsigned long long R, int S>
+__device__ __forceinline__ float x_dist3(unsigned long long m, float l1, float l2, float ACAC, float ACBC,
+                                         float ACCD, float BCBC, float BCCD, float CDCD) {
+  const float X = __fadd_rn(x_ma<M, R, S>(m, l1, ACAC, l2, ACBC), ACCD);
+  const float Y = __fadd_rn(x_ma<M, R, S + 1>(m, l1, ACBC, l2, BCBC), BCCD);
+  const float Z = __fadd_rn(x_ma<M, R, S + 2>(m, l1, ACCD, l2, BCCD), CDCD);
+  return __fadd_rn(x_ma<M, R, S + 3>(m, X, l1, Y, l2), Z);
 }
 // (l*XX + XY)*l + (l*XY + YY): the same on an edge
 __device__ __forceinline__ float x_dist2(float l, float XX, float XY, float YY) {
@@ -261,111 +277,141 @@ __device__ __forceinline__ float x_root(float num, float p) {
   return root_quot_slow(num, p);
 }
 
+// Every candidate of a face with corner times x, y (its point a convex combination
+// of them, formed in rounded non-negative steps whose weights sum to at least
+// 1 - 2^-22, plus a square root that is >= 0 or NaN) is at least
+// min(x, y) (1 - 2^-20) when rounded; a face whose bound is not below the best value
+// already known cannot change the minimum, and its quadratic is skipped.
+__device__ __forceinline__ bool face_may_lower(float x, float y, float bnd) {
+  return __fmul_rn(fminf(x, y), 0x1.ffffep-1f) < bnd;
+}
+
 // localSolverTet1 (CUDA_kernels.cu:69-225) with the roundings of mask M: the update
-// of apex D from A, B, C; the candidate order and every expression tree are the
-// reference's.
-template <unsigned long long M>
+// of apex D from A, B, C; every expression tree is the reference's.  The edge
+// candidates come first and faces that cannot go below them or below the apex's
+// current time Tcur are skipped; the minimum does not depend on the order of its
+// operands, so the result is the reference's bits.
+template <unsigned long long M, unsigned long long R = 0>
 __device__ __forceinline__ float tet_update_x(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                              float BCBC, float BCCD, float CDCD) {
+                                              float BCBC, float BCCD, float CDCD, unsigned long long m = 0,
+                                              float Tcur = kLarge3DDev) {
   if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
   float p, q, r, l1, l2, l3, delta;
   float fBC = kLarge3DDev, fAB = kLarge3DDev, fAC = kLarge3DDev, TD = kLarge3DDev;
   const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
-  // ---- face BC (lambda1 = 0) ----
-  p = x_ms<M, 0>(__fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
-  q = x_ms<M, 1>(__fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
-  r = x_ms<M, 2>(__fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
-  delta = x_ms<M, 3>(q, q, __fmul_rn(4.0f, p), r);
-  if (delta >= 0.0f) {
-    const float sd = __fsqrt_rn(delta);
-    l2 = x_root(__fadd_rn(-q, sd), p);
-    l3 = __fsub_rn(1.0f, l2);
-    if (l2 >= 0 && l2 <= 1)
-      fBC = fminf(fBC, __fadd_rn(x_ma<M, 4>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
-    l2 = x_root(__fsub_rn(-q, sd), p);
-    l3 = __fsub_rn(1.0f, l2);
-    if (l2 >= 0 && l2 <= 1)
-      fBC = fminf(fBC, __fadd_rn(x_ma<M, 5>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
-  }
+  // the edge candidates, which always enter the minimum, and the bound below which a
+  // face candidate must lie to change the result (its own minimum with the apex's
+  // current time Tcur, taken by the caller)
+  const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
   const float eB = __fadd_rn(TB, __fsqrt_rn(__fadd_rn(__fadd_rn(BCBC, BCCD), __fadd_rn(BCCD, CDCD))));
   const float eC = __fadd_rn(TC, __fsqrt_rn(CDCD));
+  const float bnd = fminf(Tcur, fminf(eA, fminf(eB, eC)));
+  // ---- face BC (lambda1 = 0) ----
+  if (face_may_lower(TB, TC, bnd)) {
+    p = x_ms<M, R, 0>(m, __fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
+    q = x_ms<M, R, 1>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
+    r = x_ms<M, R, 2>(m, __fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
+    delta = x_ms<M, R, 3>(m, q, q, __fmul_rn(4.0f, p), r);
+    if (delta >= 0.0f) {
+      const float sd = __fsqrt_rn(delta);
+      l2 = x_root(__fadd_rn(-q, sd), p);
+      l3 = __fsub_rn(1.0f, l2);
+      if (l2 >= 0 && l2 <= 1)
+        fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 4>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+      l2 = x_root(__fsub_rn(-q, sd), p);
+      l3 = __fsub_rn(1.0f, l2);
+      if (l2 >= 0 && l2 <= 1)
+        fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 5>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+    }
+  }
   fBC = fminf(fBC, fminf(eB, eC));
   // ---- face AB (lambda3 = 0) ----
-  const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
-  const float TAB2 = __fmul_rn(TAB, TAB);
-  const float P1 = x_ms<M, 6>(TAB2, ACAC, gx, gx);
-  const float P2 = x_ms<M, 7>(__fmul_rn(BCBC, TAB), TAB, gy, gy);
-  const float P3 = x_ms<M, 8>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
-  p = __fsub_rn(__fadd_rn(P1, P2), P3);
-  const float P4 = x_ms<M, 9>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
-  const float P5 = x_ms<M, 10>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
-  q = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3), P4), P5);
-  r = __fadd_rn(__fadd_rn(x_ms<M, 11>(TAB2, BCBC, gy, gy), P5), x_ms<M, 12>(TAB2, CDCD, gz, gz));
-  delta = x_ms<M, 13>(q, q, __fmul_rn(4.0f, p), r);
-  if (delta >= 0.0f) {
-    const float sd = __fsqrt_rn(delta);
-    l1 = x_root(__fadd_rn(-q, sd), p);
-    l2 = __fsub_rn(1.0f, l1);
-    if (l1 >= 0 && l1 <= 1)
-      fAB = fminf(fAB, __fadd_rn(x_ma<M, 14>(TA, l1, TB, l2),
-                                 __fsqrt_rn(x_dist3<M, 15>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
-    l1 = x_root(__fsub_rn(-q, sd), p);
-    l2 = __fsub_rn(1.0f, l1);
-    if (l1 >= 0 && l1 <= 1)
-      fAB = fminf(fAB, __fadd_rn(x_ma<M, 19>(TA, l1, TB, l2),
-                                 __fsqrt_rn(x_dist3<M, 20>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+  if (face_may_lower(TA, TB, bnd)) {
+    const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
+    const float TAB2 = __fmul_rn(TAB, TAB);
+    const float P1 = x_ms<M, R, 6>(m, TAB2, ACAC, gx, gx);
+    const float P2 = x_ms<M, R, 7>(m, __fmul_rn(BCBC, TAB), TAB, gy, gy);
+    const float P3 = x_ms<M, R, 8>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
+    p = __fsub_rn(__fadd_rn(P1, P2), P3);
+    const float P4 = x_ms<M, R, 9>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
+    const float P5 = x_ms<M, R, 10>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
+    q = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3), P4), P5);
+    r = __fadd_rn(__fadd_rn(x_ms<M, R, 11>(m, TAB2, BCBC, gy, gy), P5), x_ms<M, R, 12>(m, TAB2, CDCD, gz, gz));
+    delta = x_ms<M, R, 13>(m, q, q, __fmul_rn(4.0f, p), r);
+    if (delta >= 0.0f) {
+      const float sd = __fsqrt_rn(delta);
+      l1 = x_root(__fadd_rn(-q, sd), p);
+      l2 = __fsub_rn(1.0f, l1);
+      if (l1 >= 0 && l1 <= 1)
+        fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 14>(m, TA, l1, TB, l2),
+                                   __fsqrt_rn(x_dist3<M, R, 15>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      l1 = x_root(__fsub_rn(-q, sd), p);
+      l2 = __fsub_rn(1.0f, l1);
+      if (l1 >= 0 && l1 <= 1)
+        fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 19>(m, TA, l1, TB, l2),
+                                   __fsqrt_rn(x_dist3<M, R, 20>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    }
   }
-  const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
   fAB = fminf(fAB, fminf(eB, eA));
-  // ---- face AC (lambda2 = 0) ----
-  const float TAC2 = __fmul_rn(TAC, TAC);
-  p = x_ms<M, 24>(__fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
-  const float qAC = x_ms<M, 25>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
-  const float rAC = x_ms<M, 26>(TAC2, CDCD, ACCD, ACCD);
-  delta = x_ms<M, 27>(qAC, qAC, __fmul_rn(4.0f, p), rAC);
-  if (delta >= 0.0f) {
-    const float sd = __fsqrt_rn(delta);
-    l1 = x_root(__fadd_rn(-qAC, sd), p);
-    l3 = __fsub_rn(1.0f, l1);
-    if (l1 >= 0 && l1 <= 1)
-      fAC = fminf(fAC, __fadd_rn(x_ma<M, 28>(TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
-    l1 = x_root(__fsub_rn(-qAC, sd), p);
-    l3 = __fsub_rn(1.0f, l1);
-    // the second candidate keeps a zero-weight TB term, as the reference does
-    if (l1 >= 0 && l1 <= 1)
-      fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 29>(TA, l1, TB, 0.0f)),
-                                 __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+  // ---- face AC (lambda2 = 0), and the inside of face ABC, which reuses its terms ----
+  const bool runAC = face_may_lower(TA, TC, bnd);
+  const bool runIn = face_may_lower(fminf(TA, TB), TC, bnd);
+  if (runAC || runIn) {
+    const float TAC2 = __fmul_rn(TAC, TAC);
+    p = x_ms<M, R, 24>(m, __fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
+    const float qAC = x_ms<M, R, 25>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
+    const float rAC = x_ms<M, R, 26>(m, TAC2, CDCD, ACCD, ACCD);
+    if (runAC) {
+      delta = x_ms<M, R, 27>(m, qAC, qAC, __fmul_rn(4.0f, p), rAC);
+      if (delta >= 0.0f) {
+        const float sd = __fsqrt_rn(delta);
+        l1 = x_root(__fadd_rn(-qAC, sd), p);
+        l3 = __fsub_rn(1.0f, l1);
+        if (l1 >= 0 && l1 <= 1)
+          fAC = fminf(fAC, __fadd_rn(x_ma<M, R, 28>(m, TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+        l1 = x_root(__fsub_rn(-qAC, sd), p);
+        l3 = __fsub_rn(1.0f, l1);
+        // the second candidate keeps a zero-weight TB term, as the reference does
+        if (l1 >= 0 && l1 <= 1)
+          fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 29>(m, TA, l1, TB, 0.0f)),
+                                     __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+      }
+    }
+    if (runIn) {
+      // ---- inside face ABC: lambda2 = (s*lambda1 + t)/(h + 1e-8) ----
+      const float s = x_ms<M, R, 30>(m, TAC, ACBC, TBC, ACAC);
+      const float t = x_ms<M, R, 31>(m, TAC, BCCD, TBC, ACCD);
+      const float h = -x_ms<M, R, 32>(m, TAC, BCBC, TBC, ACBC);
+      const float A1 = x_ms<M, R, 33>(m, TAC2, ACAC, ACAC, ACAC);
+      const float A2 = x_ms<M, R, 34>(m, __fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
+      const float A3 = x_ms<M, R, 35>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
+      const float A4 = x_ms<M, R, 37>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
+      p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, R, 36>(m, __fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
+      q = __fmaf_rn(__fmul_rn(A4, s), h,
+                    __fmaf_rn(__fmul_rn(qAC, h), h,
+                              x_ma<M, R, 38>(m, __fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
+      r = __fmaf_rn(__fmul_rn(rAC, h), h,
+                    x_ma<M, R, 40>(m, __fmul_rn(x_ms<M, R, 39>(m, TAC2, BCBC, ACBC, ACBC), t), t,
+                                   __fmul_rn(A4, t), h));
+      delta = x_ms<M, R, 41>(m, q, q, __fmul_rn(4.0f, p), r);
+      if (delta >= 0.0f) {
+        const float sd = __fsqrt_rn(delta);
+        l1 = x_root(__fadd_rn(-q, sd), p);
+        l2 = small_quot(__fmaf_rn(s, l1, t), h);
+        l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+        if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+          TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 42>(m, TA, l1, TB, l2)),
+                                   __fsqrt_rn(x_dist3<M, R, 43>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+        l1 = x_root(__fsub_rn(-q, sd), p);
+        l2 = small_quot(__fmaf_rn(s, l1, t), h);
+        l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+        if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+          TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 47>(m, TA, l1, TB, l2)),
+                                   __fsqrt_rn(x_dist3<M, R, 48>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      }
+    }
   }
   fAC = fminf(fAC, fminf(eA, eC));
-  // ---- inside face ABC: lambda2 = (s*lambda1 + t)/(h + 1e-8) ----
-  const float s = x_ms<M, 30>(TAC, ACBC, TBC, ACAC);
-  const float t = x_ms<M, 31>(TAC, BCCD, TBC, ACCD);
-  const float h = -x_ms<M, 32>(TAC, BCBC, TBC, ACBC);
-  const float A1 = x_ms<M, 33>(TAC2, ACAC, ACAC, ACAC);
-  const float A2 = x_ms<M, 34>(__fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
-  const float A3 = x_ms<M, 35>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
-  const float A4 = x_ms<M, 37>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
-  p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, 36>(__fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
-  q = __fmaf_rn(__fmul_rn(A4, s), h,
-                __fmaf_rn(__fmul_rn(qAC, h), h, x_ma<M, 38>(__fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
-  r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, 40>(__fmul_rn(x_ms<M, 39>(TAC2, BCBC, ACBC, ACBC), t), t,
-                                                   __fmul_rn(A4, t), h));
-  delta = x_ms<M, 41>(q, q, __fmul_rn(4.0f, p), r);
-  if (delta >= 0.0f) {
-    const float sd = __fsqrt_rn(delta);
-    l1 = x_root(__fadd_rn(-q, sd), p);
-    l2 = small_quot(__fmaf_rn(s, l1, t), h);
-    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
-    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 42>(TA, l1, TB, l2)),
-                               __fsqrt_rn(x_dist3<M, 43>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
-    l1 = x_root(__fsub_rn(-q, sd), p);
-    l2 = small_quot(__fmaf_rn(s, l1, t), h);
-    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
-    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 47>(TA, l1, TB, l2)),
-                               __fsqrt_rn(x_dist3<M, 48>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
-  }
   return fminf(TD, fminf(fBC, fminf(fAB, fAC)));
 }
 
@@ -377,25 +423,26 @@ __device__ __forceinline__ float tet_update_x(float TA, float TB, float TC, floa
 // the minimum does not depend on the order of its operands, so the result is the
 // same bits; the interior face keeps its branch (its second quotient has a slow
 // path that a NaN input would take).
-template <unsigned long long M>
+template <unsigned long long M, unsigned long long R = 0>
 __device__ __forceinline__ float tet_update_xb(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                               float BCBC, float BCCD, float CDCD) {
+                                               float BCBC, float BCCD, float CDCD, unsigned long long m = 0,
+                                               float /*Tcur: unused here*/ = kLarge3DDev) {
   if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
   const float L = kLarge3DDev;
   const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
   // ---- face BC (lambda1 = 0) ----
   float fBC;
   {
-    const float p = x_ms<M, 0>(__fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
-    const float q = x_ms<M, 1>(__fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
-    const float r = x_ms<M, 2>(__fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
-    const float delta = x_ms<M, 3>(q, q, __fmul_rn(4.0f, p), r);
+    const float p = x_ms<M, R, 0>(m, __fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
+    const float q = x_ms<M, R, 1>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
+    const float r = x_ms<M, R, 2>(m, __fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
+    const float delta = x_ms<M, R, 3>(m, q, q, __fmul_rn(4.0f, p), r);
     const bool ok = delta >= 0.0f;
     const float sd = __fsqrt_rn(delta);
     const float a2 = x_root(__fadd_rn(-q, sd), p), a3 = __fsub_rn(1.0f, a2);
     const float b2 = x_root(__fsub_rn(-q, sd), p), b3 = __fsub_rn(1.0f, b2);
-    const float ca = __fadd_rn(x_ma<M, 4>(TB, a2, TC, a3), __fsqrt_rn(x_dist2(a2, BCBC, BCCD, CDCD)));
-    const float cb = __fadd_rn(x_ma<M, 5>(TB, b2, TC, b3), __fsqrt_rn(x_dist2(b2, BCBC, BCCD, CDCD)));
+    const float ca = __fadd_rn(x_ma<M, R, 4>(m, TB, a2, TC, a3), __fsqrt_rn(x_dist2(a2, BCBC, BCCD, CDCD)));
+    const float cb = __fadd_rn(x_ma<M, R, 5>(m, TB, b2, TC, b3), __fsqrt_rn(x_dist2(b2, BCBC, BCCD, CDCD)));
     // seeded with LARGENUM as the branching form (a NaN candidate is ignored)
     fBC = fminf(fminf(L, (ok && a2 >= 0 && a2 <= 1) ? ca : L), (ok && b2 >= 0 && b2 <= 1) ? cb : L);
   }
@@ -407,61 +454,61 @@ __device__ __forceinline__ float tet_update_xb(float TA, float TB, float TC, flo
   {
     const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
     const float TAB2 = __fmul_rn(TAB, TAB);
-    const float P1 = x_ms<M, 6>(TAB2, ACAC, gx, gx);
-    const float P2 = x_ms<M, 7>(__fmul_rn(BCBC, TAB), TAB, gy, gy);
-    const float P3 = x_ms<M, 8>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
+    const float P1 = x_ms<M, R, 6>(m, TAB2, ACAC, gx, gx);
+    const float P2 = x_ms<M, R, 7>(m, __fmul_rn(BCBC, TAB), TAB, gy, gy);
+    const float P3 = x_ms<M, R, 8>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
     const float p = __fsub_rn(__fadd_rn(P1, P2), P3);
-    const float P4 = x_ms<M, 9>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
-    const float P5 = x_ms<M, 10>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
+    const float P4 = x_ms<M, R, 9>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
+    const float P5 = x_ms<M, R, 10>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
     const float q = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3), P4), P5);
-    const float r = __fadd_rn(__fadd_rn(x_ms<M, 11>(TAB2, BCBC, gy, gy), P5), x_ms<M, 12>(TAB2, CDCD, gz, gz));
-    const float delta = x_ms<M, 13>(q, q, __fmul_rn(4.0f, p), r);
+    const float r = __fadd_rn(__fadd_rn(x_ms<M, R, 11>(m, TAB2, BCBC, gy, gy), P5), x_ms<M, R, 12>(m, TAB2, CDCD, gz, gz));
+    const float delta = x_ms<M, R, 13>(m, q, q, __fmul_rn(4.0f, p), r);
     const bool ok = delta >= 0.0f;
     const float sd = __fsqrt_rn(delta);
     const float a1 = x_root(__fadd_rn(-q, sd), p), a2 = __fsub_rn(1.0f, a1);
     const float b1 = x_root(__fsub_rn(-q, sd), p), b2 = __fsub_rn(1.0f, b1);
-    const float ca = __fadd_rn(x_ma<M, 14>(TA, a1, TB, a2),
-                               __fsqrt_rn(x_dist3<M, 15>(a1, a2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD)));
-    const float cb = __fadd_rn(x_ma<M, 19>(TA, b1, TB, b2),
-                               __fsqrt_rn(x_dist3<M, 20>(b1, b2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD)));
+    const float ca = __fadd_rn(x_ma<M, R, 14>(m, TA, a1, TB, a2),
+                               __fsqrt_rn(x_dist3<M, R, 15>(m, a1, a2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD)));
+    const float cb = __fadd_rn(x_ma<M, R, 19>(m, TA, b1, TB, b2),
+                               __fsqrt_rn(x_dist3<M, R, 20>(m, b1, b2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD)));
     // seeded with LARGENUM as the branching form (a NaN candidate is ignored)
     fAB = fminf(fminf(L, (ok && a1 >= 0 && a1 <= 1) ? ca : L), (ok && b1 >= 0 && b1 <= 1) ? cb : L);
   }
   // ---- face AC (lambda2 = 0) ----
   const float TAC2 = __fmul_rn(TAC, TAC);
-  const float qAC = x_ms<M, 25>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
-  const float rAC = x_ms<M, 26>(TAC2, CDCD, ACCD, ACCD);
+  const float qAC = x_ms<M, R, 25>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
+  const float rAC = x_ms<M, R, 26>(m, TAC2, CDCD, ACCD, ACCD);
   float fAC;
   {
-    const float p = x_ms<M, 24>(__fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
-    const float delta = x_ms<M, 27>(qAC, qAC, __fmul_rn(4.0f, p), rAC);
+    const float p = x_ms<M, R, 24>(m, __fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
+    const float delta = x_ms<M, R, 27>(m, qAC, qAC, __fmul_rn(4.0f, p), rAC);
     const bool ok = delta >= 0.0f;
     const float sd = __fsqrt_rn(delta);
     const float a1 = x_root(__fadd_rn(-qAC, sd), p), a3 = __fsub_rn(1.0f, a1);
     const float b1 = x_root(__fsub_rn(-qAC, sd), p), b3 = __fsub_rn(1.0f, b1);
-    const float ca = __fadd_rn(x_ma<M, 28>(TA, a1, TC, a3), __fsqrt_rn(x_dist2(a1, ACAC, ACCD, CDCD)));
+    const float ca = __fadd_rn(x_ma<M, R, 28>(m, TA, a1, TC, a3), __fsqrt_rn(x_dist2(a1, ACAC, ACCD, CDCD)));
     // the second candidate keeps a zero-weight TB term, as the reference does
-    const float cb = __fadd_rn(__fmaf_rn(TC, b3, x_ma<M, 29>(TA, b1, TB, 0.0f)),
+    const float cb = __fadd_rn(__fmaf_rn(TC, b3, x_ma<M, R, 29>(m, TA, b1, TB, 0.0f)),
                                __fsqrt_rn(x_dist2(b1, ACAC, ACCD, CDCD)));
     // seeded with LARGENUM as the branching form (a NaN candidate is ignored)
     fAC = fminf(fminf(L, (ok && a1 >= 0 && a1 <= 1) ? ca : L), (ok && b1 >= 0 && b1 <= 1) ? cb : L);
   }
   const float edges = fminf(fminf(fBC, fminf(eB, eC)), fminf(fminf(fAB, fminf(eB, eA)), fminf(fAC, fminf(eA, eC))));
   // ---- inside face ABC: lambda2 = (s*lambda1 + t)/(h + 1e-8) ----
-  const float s = x_ms<M, 30>(TAC, ACBC, TBC, ACAC);
-  const float t = x_ms<M, 31>(TAC, BCCD, TBC, ACCD);
-  const float h = -x_ms<M, 32>(TAC, BCBC, TBC, ACBC);
-  const float A1 = x_ms<M, 33>(TAC2, ACAC, ACAC, ACAC);
-  const float A2 = x_ms<M, 34>(__fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
-  const float A3 = x_ms<M, 35>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
-  const float A4 = x_ms<M, 37>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
-  const float p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, 36>(__fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
+  const float s = x_ms<M, R, 30>(m, TAC, ACBC, TBC, ACAC);
+  const float t = x_ms<M, R, 31>(m, TAC, BCCD, TBC, ACCD);
+  const float h = -x_ms<M, R, 32>(m, TAC, BCBC, TBC, ACBC);
+  const float A1 = x_ms<M, R, 33>(m, TAC2, ACAC, ACAC, ACAC);
+  const float A2 = x_ms<M, R, 34>(m, __fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
+  const float A3 = x_ms<M, R, 35>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
+  const float A4 = x_ms<M, R, 37>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
+  const float p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, R, 36>(m, __fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
   const float q = __fmaf_rn(__fmul_rn(A4, s), h,
                             __fmaf_rn(__fmul_rn(qAC, h), h,
-                                      x_ma<M, 38>(__fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
-  const float r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, 40>(__fmul_rn(x_ms<M, 39>(TAC2, BCBC, ACBC, ACBC), t), t,
+                                      x_ma<M, R, 38>(m, __fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
+  const float r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, R, 40>(m, __fmul_rn(x_ms<M, R, 39>(m, TAC2, BCBC, ACBC, ACBC), t), t,
                                                                __fmul_rn(A4, t), h));
-  const float delta = x_ms<M, 41>(q, q, __fmul_rn(4.0f, p), r);
+  const float delta = x_ms<M, R, 41>(m, q, q, __fmul_rn(4.0f, p), r);
   float TD = L;
   if (delta >= 0.0f) {
     const float sd = __fsqrt_rn(delta);
@@ -469,14 +516,14 @@ __device__ __forceinline__ float tet_update_xb(float TA, float TB, float TC, flo
     float l2 = small_quot(__fmaf_rn(s, l1, t), h);
     float l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
     if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 42>(TA, l1, TB, l2)),
-                               __fsqrt_rn(x_dist3<M, 43>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 42>(m, TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, R, 43>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
     l1 = x_root(__fsub_rn(-q, sd), p);
     l2 = small_quot(__fmaf_rn(s, l1, t), h);
     l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
     if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 47>(TA, l1, TB, l2)),
-                               __fsqrt_rn(x_dist3<M, 48>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 47>(m, TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, R, 48>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
   }
   return fminf(TD, edges);
 }
@@ -484,50 +531,51 @@ __device__ __forceinline__ float tet_update_xb(float TA, float TB, float TC, flo
 // tet_update_x with the four faces' quadratic coefficients and discriminants
 // formed before any root is taken: the four chains are independent and can
 // interleave; the roots keep their branches.  Same operations, same bits.
-template <unsigned long long M>
+template <unsigned long long M, unsigned long long R = 0>
 __device__ __forceinline__ float tet_update_xd(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                               float BCBC, float BCCD, float CDCD) {
+                                               float BCBC, float BCCD, float CDCD, unsigned long long m = 0,
+                                               float /*Tcur: unused here*/ = kLarge3DDev) {
   if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
   const float L = kLarge3DDev;
   const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
   // face BC
-  const float pBC = x_ms<M, 0>(__fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
-  const float qBC = x_ms<M, 1>(__fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
-  const float rBC = x_ms<M, 2>(__fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
-  const float dBC = x_ms<M, 3>(qBC, qBC, __fmul_rn(4.0f, pBC), rBC);
+  const float pBC = x_ms<M, R, 0>(m, __fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
+  const float qBC = x_ms<M, R, 1>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
+  const float rBC = x_ms<M, R, 2>(m, __fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
+  const float dBC = x_ms<M, R, 3>(m, qBC, qBC, __fmul_rn(4.0f, pBC), rBC);
   // face AB
   const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
   const float TAB2 = __fmul_rn(TAB, TAB);
-  const float P2 = x_ms<M, 7>(__fmul_rn(BCBC, TAB), TAB, gy, gy);
-  const float P3 = x_ms<M, 8>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
-  const float pAB = __fsub_rn(__fadd_rn(x_ms<M, 6>(TAB2, ACAC, gx, gx), P2), P3);
-  const float P5 = x_ms<M, 10>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
+  const float P2 = x_ms<M, R, 7>(m, __fmul_rn(BCBC, TAB), TAB, gy, gy);
+  const float P3 = x_ms<M, R, 8>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
+  const float pAB = __fsub_rn(__fadd_rn(x_ms<M, R, 6>(m, TAB2, ACAC, gx, gx), P2), P3);
+  const float P5 = x_ms<M, R, 10>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
   const float qAB = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3),
-                                        x_ms<M, 9>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz)),
+                                        x_ms<M, R, 9>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz)),
                               P5);
-  const float rAB = __fadd_rn(__fadd_rn(x_ms<M, 11>(TAB2, BCBC, gy, gy), P5), x_ms<M, 12>(TAB2, CDCD, gz, gz));
-  const float dAB = x_ms<M, 13>(qAB, qAB, __fmul_rn(4.0f, pAB), rAB);
+  const float rAB = __fadd_rn(__fadd_rn(x_ms<M, R, 11>(m, TAB2, BCBC, gy, gy), P5), x_ms<M, R, 12>(m, TAB2, CDCD, gz, gz));
+  const float dAB = x_ms<M, R, 13>(m, qAB, qAB, __fmul_rn(4.0f, pAB), rAB);
   // face AC
   const float TAC2 = __fmul_rn(TAC, TAC);
-  const float pAC = x_ms<M, 24>(__fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
-  const float qAC = x_ms<M, 25>(__fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
-  const float rAC = x_ms<M, 26>(TAC2, CDCD, ACCD, ACCD);
-  const float dAC = x_ms<M, 27>(qAC, qAC, __fmul_rn(4.0f, pAC), rAC);
+  const float pAC = x_ms<M, R, 24>(m, __fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
+  const float qAC = x_ms<M, R, 25>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
+  const float rAC = x_ms<M, R, 26>(m, TAC2, CDCD, ACCD, ACCD);
+  const float dAC = x_ms<M, R, 27>(m, qAC, qAC, __fmul_rn(4.0f, pAC), rAC);
   // face ABC
-  const float s = x_ms<M, 30>(TAC, ACBC, TBC, ACAC);
-  const float t = x_ms<M, 31>(TAC, BCCD, TBC, ACCD);
-  const float h = -x_ms<M, 32>(TAC, BCBC, TBC, ACBC);
-  const float A1 = x_ms<M, 33>(TAC2, ACAC, ACAC, ACAC);
-  const float A2 = x_ms<M, 34>(__fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
-  const float A3 = x_ms<M, 35>(__fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
-  const float A4 = x_ms<M, 37>(__fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
-  const float p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, 36>(__fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
+  const float s = x_ms<M, R, 30>(m, TAC, ACBC, TBC, ACAC);
+  const float t = x_ms<M, R, 31>(m, TAC, BCCD, TBC, ACCD);
+  const float h = -x_ms<M, R, 32>(m, TAC, BCBC, TBC, ACBC);
+  const float A1 = x_ms<M, R, 33>(m, TAC2, ACAC, ACAC, ACAC);
+  const float A2 = x_ms<M, R, 34>(m, __fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
+  const float A3 = x_ms<M, R, 35>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
+  const float A4 = x_ms<M, R, 37>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
+  const float p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, R, 36>(m, __fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
   const float q = __fmaf_rn(__fmul_rn(A4, s), h,
                             __fmaf_rn(__fmul_rn(qAC, h), h,
-                                      x_ma<M, 38>(__fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
-  const float r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, 40>(__fmul_rn(x_ms<M, 39>(TAC2, BCBC, ACBC, ACBC), t), t,
+                                      x_ma<M, R, 38>(m, __fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
+  const float r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, R, 40>(m, __fmul_rn(x_ms<M, R, 39>(m, TAC2, BCBC, ACBC, ACBC), t), t,
                                                                __fmul_rn(A4, t), h));
-  const float delta = x_ms<M, 41>(q, q, __fmul_rn(4.0f, p), r);
+  const float delta = x_ms<M, R, 41>(m, q, q, __fmul_rn(4.0f, p), r);
   const float eB = __fadd_rn(TB, __fsqrt_rn(__fadd_rn(__fadd_rn(BCBC, BCCD), __fadd_rn(BCCD, CDCD))));
   const float eC = __fadd_rn(TC, __fsqrt_rn(CDCD));
   const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
@@ -537,11 +585,11 @@ __device__ __forceinline__ float tet_update_xd(float TA, float TB, float TC, flo
     l2 = x_root(__fadd_rn(-qBC, sd), pBC);
     l3 = __fsub_rn(1.0f, l2);
     if (l2 >= 0 && l2 <= 1)
-      fBC = fminf(fBC, __fadd_rn(x_ma<M, 4>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 4>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
     l2 = x_root(__fsub_rn(-qBC, sd), pBC);
     l3 = __fsub_rn(1.0f, l2);
     if (l2 >= 0 && l2 <= 1)
-      fBC = fminf(fBC, __fadd_rn(x_ma<M, 5>(TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 5>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
   }
   fBC = fminf(fBC, fminf(eB, eC));
   if (dAB >= 0.0f) {
@@ -549,13 +597,13 @@ __device__ __forceinline__ float tet_update_xd(float TA, float TB, float TC, flo
     l1 = x_root(__fadd_rn(-qAB, sd), pAB);
     l2 = __fsub_rn(1.0f, l1);
     if (l1 >= 0 && l1 <= 1)
-      fAB = fminf(fAB, __fadd_rn(x_ma<M, 14>(TA, l1, TB, l2),
-                                 __fsqrt_rn(x_dist3<M, 15>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 14>(m, TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, R, 15>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
     l1 = x_root(__fsub_rn(-qAB, sd), pAB);
     l2 = __fsub_rn(1.0f, l1);
     if (l1 >= 0 && l1 <= 1)
-      fAB = fminf(fAB, __fadd_rn(x_ma<M, 19>(TA, l1, TB, l2),
-                                 __fsqrt_rn(x_dist3<M, 20>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 19>(m, TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, R, 20>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
   }
   fAB = fminf(fAB, fminf(eB, eA));
   if (dAC >= 0.0f) {
@@ -563,11 +611,11 @@ __device__ __forceinline__ float tet_update_xd(float TA, float TB, float TC, flo
     l1 = x_root(__fadd_rn(-qAC, sd), pAC);
     l3 = __fsub_rn(1.0f, l1);
     if (l1 >= 0 && l1 <= 1)
-      fAC = fminf(fAC, __fadd_rn(x_ma<M, 28>(TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+      fAC = fminf(fAC, __fadd_rn(x_ma<M, R, 28>(m, TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
     l1 = x_root(__fsub_rn(-qAC, sd), pAC);
     l3 = __fsub_rn(1.0f, l1);
     if (l1 >= 0 && l1 <= 1)
-      fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 29>(TA, l1, TB, 0.0f)),
+      fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 29>(m, TA, l1, TB, 0.0f)),
                                  __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
   }
   fAC = fminf(fAC, fminf(eA, eC));
@@ -577,14 +625,14 @@ __device__ __forceinline__ float tet_update_xd(float TA, float TB, float TC, flo
     l2 = small_quot(__fmaf_rn(s, l1, t), h);
     l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
     if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 42>(TA, l1, TB, l2)),
-                               __fsqrt_rn(x_dist3<M, 43>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 42>(m, TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, R, 43>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
     l1 = x_root(__fsub_rn(-q, sd), p);
     l2 = small_quot(__fmaf_rn(s, l1, t), h);
     l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
     if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, 47>(TA, l1, TB, l2)),
-                               __fsqrt_rn(x_dist3<M, 48>(l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 47>(m, TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, R, 48>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
   }
   return fminf(TD, fminf(fBC, fminf(fAB, fAC)));
 }
@@ -626,28 +674,55 @@ __device__ __forceinline__ TetGram tet_gram9(float ACBC, float BCCD, float ACCD,
 #ifndef EIK_TET_NOINLINE
 #define EIK_TET_NOINLINE 1
 #endif
-#if EIK_TET_NOINLINE
+#ifndef EIK_TET_ONEBODY
+#define EIK_TET_ONEBODY 0
+#endif
+#if EIK_TET_ONEBODY
+// one out-of-line body for all four apex kinds: the sites where their masks agree
+// are fixed at compile time, the others (kFuseRt) follow the kind's mask at run time
+constexpr unsigned long long kFuseAll = kFuseApexA & kFuseApexB & kFuseApexC & kFuseApexD;
+constexpr unsigned long long kFuseRt =
+    (kFuseApexA ^ kFuseApexB) | (kFuseApexA ^ kFuseApexC) | (kFuseApexA ^ kFuseApexD);
+__device__ __noinline__ float tet_update_rt(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                            float BCBC, float BCCD, float CDCD, unsigned long long m, float Tcur) {
+  return EIK_TET_UPDATE<kFuseAll, kFuseRt>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, m, Tcur);
+}
+template <unsigned long long M>
+__device__ __forceinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                                 float BCBC, float BCCD, float CDCD, float Tcur) {
+  return tet_update_rt(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, M, Tcur);
+}
+#elif EIK_TET_NOINLINE
 // one out-of-line body per mask (apexes A and B share theirs): less code for the
 // instruction cache than four inlined copies (the item sweep kernel ran 6% faster on
 // the 65^3 workload, same bits)
 template <unsigned long long M>
 __device__ __noinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                              float BCBC, float BCCD, float CDCD) {
-  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+                                              float BCBC, float BCCD, float CDCD, float Tcur) {
+  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, 0, Tcur);
 }
-#define EIK_TET_APEX tet_update_call
 #else
-#define EIK_TET_APEX EIK_TET_UPDATE
+template <unsigned long long M>
+__device__ __forceinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                                 float BCBC, float BCCD, float CDCD, float Tcur) {
+  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, 0, Tcur);
+}
 #endif
 
 // The update of apex k (0..3 = A, B, C, D) of a slot with corner times T, as the
-// reference's FIMCuda computes it for that apex (its arguments and its roundings).
+// reference's FIMCuda computes it for that apex (its arguments and its roundings);
+// candidates at or above the apex's own time T[k] do not change min(T[k], update)
+// and may be left out.
 template <int K>
 __device__ __forceinline__ float apex_update(const float T[4], const TetGram& g) {
-  if constexpr (K == 3) return EIK_TET_APEX<kFuseApexD>(T[0], T[1], T[2], g.ACAC, g.ACBC, g.ACCD, g.BCBC, g.BCCD, g.CDCD);
-  if constexpr (K == 0) return EIK_TET_APEX<kFuseApexA>(T[1], T[3], T[2], g.BCBC, -g.BCCD, -g.ACBC, g.CDCD, g.ACCD, g.ACAC);
-  if constexpr (K == 1) return EIK_TET_APEX<kFuseApexB>(T[0], T[3], T[2], g.ACAC, -g.ACCD, -g.ACBC, g.CDCD, g.BCCD, g.BCBC);
-  if constexpr (K == 2) return EIK_TET_APEX<kFuseApexC>(T[0], T[1], T[3], g.ADAD, g.ADBD, -g.ADCD, g.BDBD, -g.CDBD, g.CDCD);
+  if constexpr (K == 3)
+    return tet_update_call<kFuseApexD>(T[0], T[1], T[2], g.ACAC, g.ACBC, g.ACCD, g.BCBC, g.BCCD, g.CDCD, T[3]);
+  if constexpr (K == 0)
+    return tet_update_call<kFuseApexA>(T[1], T[3], T[2], g.BCBC, -g.BCCD, -g.ACBC, g.CDCD, g.ACCD, g.ACAC, T[0]);
+  if constexpr (K == 1)
+    return tet_update_call<kFuseApexB>(T[0], T[3], T[2], g.ACAC, -g.ACCD, -g.ACBC, g.CDCD, g.BCCD, g.BCBC, T[1]);
+  if constexpr (K == 2)
+    return tet_update_call<kFuseApexC>(T[0], T[1], T[3], g.ADAD, g.ADBD, -g.ADCD, g.BDBD, -g.CDBD, g.CDCD, T[2]);
   return kLarge3DDev;
 }
 
