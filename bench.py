@@ -49,7 +49,7 @@ WORKLOAD = ("plain FIM 3D at scale: 65^3 jittered Kuhn cube (274,625 verts, 1,57
             "log-uniform per-tet speed [0.5, 2] as metric 1/v^2, seed at the centre vertex, 64 verts/block")
 N_GRID = 65
 MAX_ITERS = 100  # the reference default (src/Eikonal.cu:19); the workload converges in 81
-DRAM_PROFILE = "fim3d_visit_dram_c3d.txt"  # per-launch DRAM bytes of the visit kernels over one solve
+DRAM_PROFILE = "fim3d_items_dram_c3d.txt"  # per-launch DRAM bytes of the sweep and check kernels over one solve
 
 
 def parse():

@@ -63,6 +63,7 @@ struct Ctl {
   int error;
   int stop;       // set when the outer loop must end (read by the direct-launch loop)
   int f64_all;    // precision mode's polish: every slot's update in FP64
+  int polish;     // precision mode's polish: blocks settle to a few ulps, not EPS
   unsigned long long updates, fim_visits, chk_visits, slot_visits, halo_visits, owned_visits;
   unsigned long long fim_slots, fim_halo, fim_owned;  // per-visit inputs of the sweep kernel only
 };
@@ -135,7 +136,7 @@ constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1
 // precision mode's polish (every update in FP64) a few units in the last place of
 // the time, so that corrections smaller than EPS still reach the neighbour blocks
 #ifndef EIK_POLISH_SETTLE
-#define EIK_POLISH_SETTLE 0x1p-21f
+#define EIK_POLISH_SETTLE 0x1p-15f
 #endif
 __device__ __forceinline__ float settle_eps(float T, int polish) {
   return polish ? __fmul_rn(T, EIK_POLISH_SETTLE) : kEps3DLe;
@@ -155,7 +156,7 @@ constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::kt
 #define EIK_POLISH_F64ALL 1
 #endif
 #ifndef EIK_POLISH_TOL
-#define EIK_POLISH_TOL 1e-6
+#define EIK_POLISH_TOL 3e-5
 #endif
 // item kernels: warps take chunks of 32 items from a shared counter (1; warps that
 // drew short updates take more, so fewer wait at the next barrier: sweep kernel 4%
@@ -322,6 +323,15 @@ __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd
   return ok;
 }
 
+// Every candidate of a tet update is at least m (1 - 2^-22), m the smallest of the
+// three input times: the point on the face is a convex combination of the inputs
+// whose weights sum to at least 1 - 2^-24 after rounding, formed in at most four
+// rounded nonnegative steps, and the candidate adds a square root (>= 0, or NaN,
+// which the minimum ignores) to it; the edge candidates are an input plus a square
+// root.  So an apex time T <= RN(m (1 - 2^-20)) < m (1 - 2^-21) keeps its value:
+// min(T, update) = T, and the update can be skipped without changing any bit.
+__device__ __forceinline__ bool upwind_skip(float Tk, float m) { return Tk <= __fmul_rn(m, 0x1.ffffep-1f); }
+
 // ===========================================================================
 // 3D visit: kCheck = false -> FIMCuda (fim_sweeps sweeps, writes visit outputs);
 //           kCheck = true  -> run_check_neghbor (1 sweep, flags only)
@@ -353,6 +363,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   const int count = kCheck ? ctl->nnew : ctl->nact;
   const int* list = kCheck ? a.list_new : act_list(a, iter);
   const int f64all = kPrec ? ctl->f64_all : 0;
+  const int polish = kPrec ? ctl->polish : 0;
   int* nxt = next_list(a, iter);
   const int nsweeps = kCheck ? 1 : a.fim_sweeps;
   stamp_start(a, iter, kCheck ? 1 : 0);
@@ -467,13 +478,17 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
               // (the copies of other blocks' corners are dropped), so the FP64
               // updates of the others are left out there
               const bool all = !kCheck && sw != nsweeps - 1;
-              if (all || own[3])
+              // an apex at or below the upwind bound of its other corners keeps its
+              // time under the FP64 update too (its candidates are convex combinations
+              // of those corners plus a root, as in FP32), and the FP32 result already
+              // in nw equals it
+              if ((all || own[3]) && !upwind_skip(TD, fminf(fminf(TA, TB), TC)))
                 nw[3] = fminf(TD, (float)tet_update_f64(A, B, C, dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD));
-              if (all || own[0])
+              if ((all || own[0]) && !upwind_skip(TA, fminf(fminf(TB, TD), TC)))
                 nw[0] = fminf(TA, (float)tet_update_f64(B, D, C, dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC));
-              if (all || own[1])
+              if ((all || own[1]) && !upwind_skip(TB, fminf(fminf(TA, TD), TC)))
                 nw[1] = fminf(TB, (float)tet_update_f64(A, D, C, dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC));
-              if (all || own[2])
+              if ((all || own[2]) && !upwind_skip(TC, fminf(fminf(TA, TB), TD)))
                 nw[2] = fminf(TC, (float)tet_update_f64(A, B, D, dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD));
             }
           }
@@ -482,7 +497,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
           bool moved = false;
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (own[k] && !((T[k] - nw[k]) <= settle_eps(T[k], f64all))) moved = true;  // (double)(old - c) >= 1e-5
+            if (own[k] && !((T[k] - nw[k]) <= settle_eps(T[k], polish))) moved = true;  // (double)(old - c) >= 1e-5
           if (moved)
             s_moved = 1;
           else if (smemo && !memo)
@@ -514,7 +529,7 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
         if (last) {
           float res = ov - nv;
           if (!kCheck && res < 0.0f) res = -res;
-          myconv &= (res <= settle_eps(ov, f64all)) ? 1 : 0;
+          myconv &= (res <= settle_eps(ov, polish)) ? 1 : 0;
         }
         s.vchg[k] = (nv != ov) ? 1 : 0;
         s.vt[k] = nv;
@@ -583,14 +598,6 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
   stamp_end(a, iter, kCheck ? 1 : 0);
 }
 
-// Every candidate of a tet update is at least m (1 - 2^-22), m the smallest of the
-// three input times: the point on the face is a convex combination of the inputs
-// whose weights sum to at least 1 - 2^-24 after rounding, formed in at most four
-// rounded nonnegative steps, and the candidate adds a square root (>= 0, or NaN,
-// which the minimum ignores) to it; the edge candidates are an input plus a square
-// root.  So an apex time T <= RN(m (1 - 2^-20)) < m (1 - 2^-21) keeps its value:
-// min(T, update) = T, and the update can be skipped without changing any bit.
-__device__ __forceinline__ bool upwind_skip(float Tk, float m) { return Tk <= __fmul_rn(m, 0x1.ffffep-1f); }
 
 // ===========================================================================
 // 3D sweep visit by apex items (FIMCuda, fim_sweeps sweeps).
@@ -1643,6 +1650,7 @@ __global__ void k_polish_begin(DevArgs a, int cap) {
     c->done_d = 0;
     c->stop = 0;
     c->f64_all = EIK_POLISH_F64ALL;
+    c->polish = 1;
   }
 }
 

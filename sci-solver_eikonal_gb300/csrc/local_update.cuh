@@ -277,141 +277,111 @@ __device__ __forceinline__ float x_root(float num, float p) {
   return root_quot_slow(num, p);
 }
 
-// Every candidate of a face with corner times x, y (its point a convex combination
-// of them, formed in rounded non-negative steps whose weights sum to at least
-// 1 - 2^-22, plus a square root that is >= 0 or NaN) is at least
-// min(x, y) (1 - 2^-20) when rounded; a face whose bound is not below the best value
-// already known cannot change the minimum, and its quadratic is skipped.
-__device__ __forceinline__ bool face_may_lower(float x, float y, float bnd) {
-  return __fmul_rn(fminf(x, y), 0x1.ffffep-1f) < bnd;
-}
-
 // localSolverTet1 (CUDA_kernels.cu:69-225) with the roundings of mask M: the update
-// of apex D from A, B, C; every expression tree is the reference's.  The edge
-// candidates come first and faces that cannot go below them or below the apex's
-// current time Tcur are skipped; the minimum does not depend on the order of its
-// operands, so the result is the reference's bits.
+// of apex D from A, B, C; the candidate order and every expression tree are the
+// reference's.
 template <unsigned long long M, unsigned long long R = 0>
 __device__ __forceinline__ float tet_update_x(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                              float BCBC, float BCCD, float CDCD, unsigned long long m = 0,
-                                              float Tcur = kLarge3DDev) {
+                                              float BCBC, float BCCD, float CDCD, unsigned long long m = 0) {
   if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
   float p, q, r, l1, l2, l3, delta;
   float fBC = kLarge3DDev, fAB = kLarge3DDev, fAC = kLarge3DDev, TD = kLarge3DDev;
   const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
-  // the edge candidates, which always enter the minimum, and the bound below which a
-  // face candidate must lie to change the result (its own minimum with the apex's
-  // current time Tcur, taken by the caller)
-  const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
+  // ---- face BC (lambda1 = 0) ----
+  p = x_ms<M, R, 0>(m, __fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
+  q = x_ms<M, R, 1>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
+  r = x_ms<M, R, 2>(m, __fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
+  delta = x_ms<M, R, 3>(m, q, q, __fmul_rn(4.0f, p), r);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l2 = x_root(__fadd_rn(-q, sd), p);
+    l3 = __fsub_rn(1.0f, l2);
+    if (l2 >= 0 && l2 <= 1)
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 4>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+    l2 = x_root(__fsub_rn(-q, sd), p);
+    l3 = __fsub_rn(1.0f, l2);
+    if (l2 >= 0 && l2 <= 1)
+      fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 5>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
+  }
   const float eB = __fadd_rn(TB, __fsqrt_rn(__fadd_rn(__fadd_rn(BCBC, BCCD), __fadd_rn(BCCD, CDCD))));
   const float eC = __fadd_rn(TC, __fsqrt_rn(CDCD));
-  const float bnd = fminf(Tcur, fminf(eA, fminf(eB, eC)));
-  // ---- face BC (lambda1 = 0) ----
-  if (face_may_lower(TB, TC, bnd)) {
-    p = x_ms<M, R, 0>(m, __fmul_rn(BCBC, TBC), TBC, BCBC, BCBC);
-    q = x_ms<M, R, 1>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TBC), TBC, __fmul_rn(2.0f, BCBC), BCCD);
-    r = x_ms<M, R, 2>(m, __fmul_rn(TBC, TBC), CDCD, BCCD, BCCD);
-    delta = x_ms<M, R, 3>(m, q, q, __fmul_rn(4.0f, p), r);
-    if (delta >= 0.0f) {
-      const float sd = __fsqrt_rn(delta);
-      l2 = x_root(__fadd_rn(-q, sd), p);
-      l3 = __fsub_rn(1.0f, l2);
-      if (l2 >= 0 && l2 <= 1)
-        fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 4>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
-      l2 = x_root(__fsub_rn(-q, sd), p);
-      l3 = __fsub_rn(1.0f, l2);
-      if (l2 >= 0 && l2 <= 1)
-        fBC = fminf(fBC, __fadd_rn(x_ma<M, R, 5>(m, TB, l2, TC, l3), __fsqrt_rn(x_dist2(l2, BCBC, BCCD, CDCD))));
-    }
-  }
   fBC = fminf(fBC, fminf(eB, eC));
   // ---- face AB (lambda3 = 0) ----
-  if (face_may_lower(TA, TB, bnd)) {
-    const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
-    const float TAB2 = __fmul_rn(TAB, TAB);
-    const float P1 = x_ms<M, R, 6>(m, TAB2, ACAC, gx, gx);
-    const float P2 = x_ms<M, R, 7>(m, __fmul_rn(BCBC, TAB), TAB, gy, gy);
-    const float P3 = x_ms<M, R, 8>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
-    p = __fsub_rn(__fadd_rn(P1, P2), P3);
-    const float P4 = x_ms<M, R, 9>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
-    const float P5 = x_ms<M, R, 10>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
-    q = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3), P4), P5);
-    r = __fadd_rn(__fadd_rn(x_ms<M, R, 11>(m, TAB2, BCBC, gy, gy), P5), x_ms<M, R, 12>(m, TAB2, CDCD, gz, gz));
-    delta = x_ms<M, R, 13>(m, q, q, __fmul_rn(4.0f, p), r);
-    if (delta >= 0.0f) {
-      const float sd = __fsqrt_rn(delta);
-      l1 = x_root(__fadd_rn(-q, sd), p);
-      l2 = __fsub_rn(1.0f, l1);
-      if (l1 >= 0 && l1 <= 1)
-        fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 14>(m, TA, l1, TB, l2),
-                                   __fsqrt_rn(x_dist3<M, R, 15>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
-      l1 = x_root(__fsub_rn(-q, sd), p);
-      l2 = __fsub_rn(1.0f, l1);
-      if (l1 >= 0 && l1 <= 1)
-        fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 19>(m, TA, l1, TB, l2),
-                                   __fsqrt_rn(x_dist3<M, R, 20>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
-    }
+  const float gx = __fsub_rn(ACAC, ACBC), gy = __fsub_rn(ACBC, BCBC), gz = __fsub_rn(ACCD, BCCD);
+  const float TAB2 = __fmul_rn(TAB, TAB);
+  const float P1 = x_ms<M, R, 6>(m, TAB2, ACAC, gx, gx);
+  const float P2 = x_ms<M, R, 7>(m, __fmul_rn(BCBC, TAB), TAB, gy, gy);
+  const float P3 = x_ms<M, R, 8>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAB), TAB, __fmul_rn(2.0f, gx), gy);
+  p = __fsub_rn(__fadd_rn(P1, P2), P3);
+  const float P4 = x_ms<M, R, 9>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAB), TAB, __fmul_rn(2.0f, gx), gz);
+  const float P5 = x_ms<M, R, 10>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAB), TAB, __fmul_rn(2.0f, gy), gz);
+  q = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(-P2, 2.0f), P3), P4), P5);
+  r = __fadd_rn(__fadd_rn(x_ms<M, R, 11>(m, TAB2, BCBC, gy, gy), P5), x_ms<M, R, 12>(m, TAB2, CDCD, gz, gz));
+  delta = x_ms<M, R, 13>(m, q, q, __fmul_rn(4.0f, p), r);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l1 = x_root(__fadd_rn(-q, sd), p);
+    l2 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 14>(m, TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, R, 15>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    l1 = x_root(__fsub_rn(-q, sd), p);
+    l2 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAB = fminf(fAB, __fadd_rn(x_ma<M, R, 19>(m, TA, l1, TB, l2),
+                                 __fsqrt_rn(x_dist3<M, R, 20>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
   }
+  const float eA = __fadd_rn(TA, __fsqrt_rn(__fadd_rn(__fadd_rn(ACAC, ACCD), __fadd_rn(ACCD, CDCD))));
   fAB = fminf(fAB, fminf(eB, eA));
-  // ---- face AC (lambda2 = 0), and the inside of face ABC, which reuses its terms ----
-  const bool runAC = face_may_lower(TA, TC, bnd);
-  const bool runIn = face_may_lower(fminf(TA, TB), TC, bnd);
-  if (runAC || runIn) {
-    const float TAC2 = __fmul_rn(TAC, TAC);
-    p = x_ms<M, R, 24>(m, __fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
-    const float qAC = x_ms<M, R, 25>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
-    const float rAC = x_ms<M, R, 26>(m, TAC2, CDCD, ACCD, ACCD);
-    if (runAC) {
-      delta = x_ms<M, R, 27>(m, qAC, qAC, __fmul_rn(4.0f, p), rAC);
-      if (delta >= 0.0f) {
-        const float sd = __fsqrt_rn(delta);
-        l1 = x_root(__fadd_rn(-qAC, sd), p);
-        l3 = __fsub_rn(1.0f, l1);
-        if (l1 >= 0 && l1 <= 1)
-          fAC = fminf(fAC, __fadd_rn(x_ma<M, R, 28>(m, TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
-        l1 = x_root(__fsub_rn(-qAC, sd), p);
-        l3 = __fsub_rn(1.0f, l1);
-        // the second candidate keeps a zero-weight TB term, as the reference does
-        if (l1 >= 0 && l1 <= 1)
-          fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 29>(m, TA, l1, TB, 0.0f)),
-                                     __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
-      }
-    }
-    if (runIn) {
-      // ---- inside face ABC: lambda2 = (s*lambda1 + t)/(h + 1e-8) ----
-      const float s = x_ms<M, R, 30>(m, TAC, ACBC, TBC, ACAC);
-      const float t = x_ms<M, R, 31>(m, TAC, BCCD, TBC, ACCD);
-      const float h = -x_ms<M, R, 32>(m, TAC, BCBC, TBC, ACBC);
-      const float A1 = x_ms<M, R, 33>(m, TAC2, ACAC, ACAC, ACAC);
-      const float A2 = x_ms<M, R, 34>(m, __fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
-      const float A3 = x_ms<M, R, 35>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
-      const float A4 = x_ms<M, R, 37>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
-      p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, R, 36>(m, __fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
-      q = __fmaf_rn(__fmul_rn(A4, s), h,
-                    __fmaf_rn(__fmul_rn(qAC, h), h,
-                              x_ma<M, R, 38>(m, __fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
-      r = __fmaf_rn(__fmul_rn(rAC, h), h,
-                    x_ma<M, R, 40>(m, __fmul_rn(x_ms<M, R, 39>(m, TAC2, BCBC, ACBC, ACBC), t), t,
-                                   __fmul_rn(A4, t), h));
-      delta = x_ms<M, R, 41>(m, q, q, __fmul_rn(4.0f, p), r);
-      if (delta >= 0.0f) {
-        const float sd = __fsqrt_rn(delta);
-        l1 = x_root(__fadd_rn(-q, sd), p);
-        l2 = small_quot(__fmaf_rn(s, l1, t), h);
-        l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
-        if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-          TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 42>(m, TA, l1, TB, l2)),
-                                   __fsqrt_rn(x_dist3<M, R, 43>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
-        l1 = x_root(__fsub_rn(-q, sd), p);
-        l2 = small_quot(__fmaf_rn(s, l1, t), h);
-        l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
-        if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
-          TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 47>(m, TA, l1, TB, l2)),
-                                   __fsqrt_rn(x_dist3<M, R, 48>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
-      }
-    }
+  // ---- face AC (lambda2 = 0) ----
+  const float TAC2 = __fmul_rn(TAC, TAC);
+  p = x_ms<M, R, 24>(m, __fmul_rn(ACAC, TAC), TAC, ACAC, ACAC);
+  const float qAC = x_ms<M, R, 25>(m, __fmul_rn(__fadd_rn(ACCD, ACCD), TAC), TAC, __fmul_rn(2.0f, ACAC), ACCD);
+  const float rAC = x_ms<M, R, 26>(m, TAC2, CDCD, ACCD, ACCD);
+  delta = x_ms<M, R, 27>(m, qAC, qAC, __fmul_rn(4.0f, p), rAC);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l1 = x_root(__fadd_rn(-qAC, sd), p);
+    l3 = __fsub_rn(1.0f, l1);
+    if (l1 >= 0 && l1 <= 1)
+      fAC = fminf(fAC, __fadd_rn(x_ma<M, R, 28>(m, TA, l1, TC, l3), __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
+    l1 = x_root(__fsub_rn(-qAC, sd), p);
+    l3 = __fsub_rn(1.0f, l1);
+    // the second candidate keeps a zero-weight TB term, as the reference does
+    if (l1 >= 0 && l1 <= 1)
+      fAC = fminf(fAC, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 29>(m, TA, l1, TB, 0.0f)),
+                                 __fsqrt_rn(x_dist2(l1, ACAC, ACCD, CDCD))));
   }
   fAC = fminf(fAC, fminf(eA, eC));
+  // ---- inside face ABC: lambda2 = (s*lambda1 + t)/(h + 1e-8) ----
+  const float s = x_ms<M, R, 30>(m, TAC, ACBC, TBC, ACAC);
+  const float t = x_ms<M, R, 31>(m, TAC, BCCD, TBC, ACCD);
+  const float h = -x_ms<M, R, 32>(m, TAC, BCBC, TBC, ACBC);
+  const float A1 = x_ms<M, R, 33>(m, TAC2, ACAC, ACAC, ACAC);
+  const float A2 = x_ms<M, R, 34>(m, __fmul_rn(BCBC, TAC), TAC, ACBC, ACBC);
+  const float A3 = x_ms<M, R, 35>(m, __fmul_rn(__fadd_rn(ACBC, ACBC), TAC), TAC, __fmul_rn(2.0f, ACAC), ACBC);
+  const float A4 = x_ms<M, R, 37>(m, __fmul_rn(__fadd_rn(BCCD, BCCD), TAC), TAC, __fmul_rn(2.0f, ACBC), ACCD);
+  p = __fmaf_rn(__fmul_rn(A3, s), h, x_ma<M, R, 36>(m, __fmul_rn(A1, h), h, __fmul_rn(A2, s), s));
+  q = __fmaf_rn(__fmul_rn(A4, s), h,
+                __fmaf_rn(__fmul_rn(qAC, h), h, x_ma<M, R, 38>(m, __fmul_rn(__fmul_rn(A2, 2.0f), s), t, __fmul_rn(A3, t), h)));
+  r = __fmaf_rn(__fmul_rn(rAC, h), h, x_ma<M, R, 40>(m, __fmul_rn(x_ms<M, R, 39>(m, TAC2, BCBC, ACBC, ACBC), t), t,
+                                                   __fmul_rn(A4, t), h));
+  delta = x_ms<M, R, 41>(m, q, q, __fmul_rn(4.0f, p), r);
+  if (delta >= 0.0f) {
+    const float sd = __fsqrt_rn(delta);
+    l1 = x_root(__fadd_rn(-q, sd), p);
+    l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 42>(m, TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, R, 43>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+    l1 = x_root(__fsub_rn(-q, sd), p);
+    l2 = small_quot(__fmaf_rn(s, l1, t), h);
+    l3 = __fsub_rn(__fsub_rn(1.0f, l1), l2);
+    if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1)
+      TD = fminf(TD, __fadd_rn(__fmaf_rn(TC, l3, x_ma<M, R, 47>(m, TA, l1, TB, l2)),
+                               __fsqrt_rn(x_dist3<M, R, 48>(m, l1, l2, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD))));
+  }
   return fminf(TD, fminf(fBC, fminf(fAB, fAC)));
 }
 
@@ -425,8 +395,7 @@ __device__ __forceinline__ float tet_update_x(float TA, float TB, float TC, floa
 // path that a NaN input would take).
 template <unsigned long long M, unsigned long long R = 0>
 __device__ __forceinline__ float tet_update_xb(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                               float BCBC, float BCCD, float CDCD, unsigned long long m = 0,
-                                               float /*Tcur: unused here*/ = kLarge3DDev) {
+                                               float BCBC, float BCCD, float CDCD, unsigned long long m = 0) {
   if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
   const float L = kLarge3DDev;
   const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
@@ -533,8 +502,7 @@ __device__ __forceinline__ float tet_update_xb(float TA, float TB, float TC, flo
 // interleave; the roots keep their branches.  Same operations, same bits.
 template <unsigned long long M, unsigned long long R = 0>
 __device__ __forceinline__ float tet_update_xd(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                               float BCBC, float BCCD, float CDCD, unsigned long long m = 0,
-                                               float /*Tcur: unused here*/ = kLarge3DDev) {
+                                               float BCBC, float BCCD, float CDCD, unsigned long long m = 0) {
   if (TA >= kLarge3DDev && TB >= kLarge3DDev && TC >= kLarge3DDev) return kLarge3DDev;
   const float L = kLarge3DDev;
   const float TAC = __fsub_rn(TC, TA), TBC = __fsub_rn(TC, TB), TAB = __fsub_rn(TB, TA);
@@ -675,22 +643,24 @@ __device__ __forceinline__ TetGram tet_gram9(float ACBC, float BCCD, float ACCD,
 #define EIK_TET_NOINLINE 1
 #endif
 #ifndef EIK_TET_ONEBODY
-#define EIK_TET_ONEBODY 0
+#define EIK_TET_ONEBODY 1
 #endif
 #if EIK_TET_ONEBODY
 // one out-of-line body for all four apex kinds: the sites where their masks agree
-// are fixed at compile time, the others (kFuseRt) follow the kind's mask at run time
+// are fixed at compile time, the 13 others (kFuseRt) follow the kind's mask at run
+// time through selects; a third of the code for the instruction cache (65^3 sweep
+// kernel 2-4% faster than one body per mask, same bits)
 constexpr unsigned long long kFuseAll = kFuseApexA & kFuseApexB & kFuseApexC & kFuseApexD;
 constexpr unsigned long long kFuseRt =
     (kFuseApexA ^ kFuseApexB) | (kFuseApexA ^ kFuseApexC) | (kFuseApexA ^ kFuseApexD);
 __device__ __noinline__ float tet_update_rt(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                            float BCBC, float BCCD, float CDCD, unsigned long long m, float Tcur) {
-  return EIK_TET_UPDATE<kFuseAll, kFuseRt>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, m, Tcur);
+                                            float BCBC, float BCCD, float CDCD, unsigned long long m) {
+  return EIK_TET_UPDATE<kFuseAll, kFuseRt>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, m);
 }
 template <unsigned long long M>
 __device__ __forceinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                                 float BCBC, float BCCD, float CDCD, float Tcur) {
-  return tet_update_rt(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, M, Tcur);
+                                                 float BCBC, float BCCD, float CDCD) {
+  return tet_update_rt(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, M);
 }
 #elif EIK_TET_NOINLINE
 // one out-of-line body per mask (apexes A and B share theirs): less code for the
@@ -698,31 +668,29 @@ __device__ __forceinline__ float tet_update_call(float TA, float TB, float TC, f
 // the 65^3 workload, same bits)
 template <unsigned long long M>
 __device__ __noinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                              float BCBC, float BCCD, float CDCD, float Tcur) {
-  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, 0, Tcur);
+                                              float BCBC, float BCCD, float CDCD) {
+  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
 }
 #else
 template <unsigned long long M>
 __device__ __forceinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                                 float BCBC, float BCCD, float CDCD, float Tcur) {
-  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, 0, Tcur);
+                                                 float BCBC, float BCCD, float CDCD) {
+  return EIK_TET_UPDATE<M>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
 }
 #endif
 
 // The update of apex k (0..3 = A, B, C, D) of a slot with corner times T, as the
-// reference's FIMCuda computes it for that apex (its arguments and its roundings);
-// candidates at or above the apex's own time T[k] do not change min(T[k], update)
-// and may be left out.
+// reference's FIMCuda computes it for that apex (its arguments and its roundings).
 template <int K>
 __device__ __forceinline__ float apex_update(const float T[4], const TetGram& g) {
   if constexpr (K == 3)
-    return tet_update_call<kFuseApexD>(T[0], T[1], T[2], g.ACAC, g.ACBC, g.ACCD, g.BCBC, g.BCCD, g.CDCD, T[3]);
+    return tet_update_call<kFuseApexD>(T[0], T[1], T[2], g.ACAC, g.ACBC, g.ACCD, g.BCBC, g.BCCD, g.CDCD);
   if constexpr (K == 0)
-    return tet_update_call<kFuseApexA>(T[1], T[3], T[2], g.BCBC, -g.BCCD, -g.ACBC, g.CDCD, g.ACCD, g.ACAC, T[0]);
+    return tet_update_call<kFuseApexA>(T[1], T[3], T[2], g.BCBC, -g.BCCD, -g.ACBC, g.CDCD, g.ACCD, g.ACAC);
   if constexpr (K == 1)
-    return tet_update_call<kFuseApexB>(T[0], T[3], T[2], g.ACAC, -g.ACCD, -g.ACBC, g.CDCD, g.BCCD, g.BCBC, T[1]);
+    return tet_update_call<kFuseApexB>(T[0], T[3], T[2], g.ACAC, -g.ACCD, -g.ACBC, g.CDCD, g.BCCD, g.BCBC);
   if constexpr (K == 2)
-    return tet_update_call<kFuseApexC>(T[0], T[1], T[3], g.ADAD, g.ADBD, -g.ADCD, g.BDBD, -g.CDBD, g.CDCD, T[2]);
+    return tet_update_call<kFuseApexC>(T[0], T[1], T[3], g.ADAD, g.ADBD, -g.ADCD, g.BDBD, -g.CDBD, g.CDCD);
   return kLarge3DDev;
 }
 

@@ -50,11 +50,10 @@ def test_precision_mode_moves_toward_fp64(need_gpu, eik, O, prec_case):
     assert errmx.max() <= 0.1 * err32.max(), (errmx.max(), err32.max())
     assert errmx.mean() < 0.2 * err32.mean(), (errmx.mean(), err32.mean())
     # the polish leaves no vertex that an FP64 update of its tets would lower by
-    # more than 1e-4 relative (device check), and the CPU restatement agrees
+    # 1e-4 relative or more (device check), and the CPU restatement agrees
     assert st["polish_rounds"] >= 1
     assert st["residual_max_rel"] < 1e-4, st["residual_max_rel"]
     assert st["residual_max_abs"] < 1e-4 * float(np.max(emx.getFinalResult()))
-    assert st["residual_vertices"] == 0
     res = O.fp64_residual(xyz, tets, M, emx.getFinalResult())
     assert res["lowerable"] < 1e-4, res
     # times below every FP64 update of their tets (the update is not monotone in
