@@ -135,6 +135,21 @@ constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1
 // The change below which a vertex counts as settled: the reference's EPS, or in
 // precision mode's polish (every update in FP64) a few units in the last place of
 // the time, so that corrections smaller than EPS still reach the neighbour blocks
+// Programmatic dependent launch between the kernels of the loop body: wait for the
+// grid this one depends on to complete (a no-op without such a dependency, as in
+// the kernel-by-kernel loop), then let the next grid begin launching, so its CTAs
+// are scheduled while this one runs instead of after it.  Every kernel of the body
+// starts with it, before touching global memory.
+#ifndef EIK_PDL
+#define EIK_PDL 1
+#endif
+__device__ __forceinline__ void pdl_begin() {
+#if EIK_PDL
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 #ifndef EIK_POLISH_SETTLE
 #define EIK_POLISH_SETTLE 0x1p-15f
 #endif
@@ -143,6 +158,8 @@ __device__ __forceinline__ float settle_eps(float T, int polish) {
 }
 constexpr float kEps2D = 1e-5f;
 constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
+// whether the driver accepted programmatic edges in a conditional loop body
+bool g_pdl_ok = true;
 constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::ktime)
 #ifndef EIK_SWEEP_ITEMS
 #define EIK_SWEEP_ITEMS 1
@@ -338,6 +355,7 @@ __device__ __forceinline__ bool upwind_skip(float Tk, float m) { return Tk <= __
 // ===========================================================================
 template <bool kCheck, bool kPrec = false>
 __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
@@ -670,6 +688,7 @@ __device__ __forceinline__ SmemItems carve_items(unsigned char* sm, const DevArg
 
 // at most 56 registers: three CTAs of 384 threads fit one SM's register file
 __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
@@ -687,10 +706,17 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
   if (tid == 0) mbar_init(&bar, 1);
   __syncthreads();
   unsigned parity = 0;
+  // the first block of a CTA is its own index; later ones come from the counter
+  // (a CTA without a first block exits without touching it)
+  int first_item = blockIdx.x;
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(&a.ctl->work_a, 1);
-    __syncthreads();
-    const int item = s_item;
+    int item = first_item;
+    if (item < 0) {
+      if (tid == 0) s_item = (int)gridDim.x + atomicAdd(&a.ctl->work_a, 1);
+      __syncthreads();
+      item = s_item;
+    }
+    first_item = -1;
     if (item >= count) break;
     const int b = list[item];
     if (a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
@@ -889,6 +915,7 @@ __host__ __device__ inline size_t smem_bytes_check(int np, int max_local, int ma
 }
 
 __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
@@ -914,10 +941,17 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
   if (tid == 0) mbar_init(&bar, 1);
   __syncthreads();
   unsigned parity = 0;
+  // the first block of a CTA is its own index; later ones come from the counter
+  // (a CTA without a first block exits without touching it)
+  int first_item = blockIdx.x;
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(&a.ctl->work_c, 1);
-    __syncthreads();
-    const int item = s_item;
+    int item = first_item;
+    if (item < 0) {
+      if (tid == 0) s_item = (int)gridDim.x + atomicAdd(&a.ctl->work_c, 1);
+      __syncthreads();
+      item = s_item;
+    }
+    first_item = -1;
     if (item >= count) break;
     const int b = a.list_new[item];
     if (a.inst_done[a.blk_inst[b]]) {
@@ -1039,6 +1073,7 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
 // ===========================================================================
 template <bool kCheck>
 __global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
@@ -1200,6 +1235,7 @@ __global__ void __launch_bounds__(256) k_visit2d(DevArgs a) {
 // ===========================================================================
 template <bool kCheck, int kSweeps>
 __global__ void __launch_bounds__(1024) k_visit2d_slot(DevArgs a) {
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
@@ -1372,6 +1408,7 @@ size_t smem_bytes_slot2d(int max_slots_pad, int max_local, int max_owned) {
 // One warp per active block.
 // ===========================================================================
 __global__ void k_commit3d(DevArgs a) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   const int iter = a.ctl->iter, stamp = iter + 1;
   const int count = a.ctl->nact;
@@ -1400,6 +1437,7 @@ __global__ void k_commit3d(DevArgs a) {
 
 // 2D: queue the neighbours of converged active blocks that are not active.
 __global__ void k_activate2d(DevArgs a) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   const int iter = a.ctl->iter, stamp = iter + 1;
   const int count = a.ctl->nact;
@@ -1474,6 +1512,7 @@ __device__ __forceinline__ bool last_cta(int* counter) {
 constexpr int kVertexChunk = 2048;  // vertices per chunk of the 2D all-vertex test
 
 __global__ void k_vertex_test2d(DevArgs a, int copy) {
+  pdl_begin();
   // a later copy of the iteration in the graph body, after the loop stopped
   if (copy > 0 && a.ctl->stop) return;
   // chunks of the running instances only (a server's idle slots and finished
@@ -1517,6 +1556,7 @@ __global__ void k_vertex_test2d(DevArgs a, int copy) {
 // stopped when an earlier copy ended it, and leaves the state alone.  (A copy's close
 // returns only after an earlier copy of the same pass set the loop's condition to 0.)
 __global__ void k_close3d(DevArgs a, int copy) {
+  pdl_begin();
   if (copy > 0 && a.ctl->stop) return;
   finish_iteration_cta(a, false);
 }
@@ -1556,6 +1596,7 @@ __global__ void k_start(DevArgs a) {
 
 // per-iteration snapshot in renumbered order (iteration index = iter - 1)
 __global__ void k_snapshot(DevArgs a, int dim) {
+  pdl_begin();
   const int slot = a.ctl->iter - 1;
   if (slot < 0 || slot >= a.hist_cap) return;
   float* dst = a.hist + (size_t)slot * a.nv;
@@ -2215,12 +2256,26 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     cudaGraphNode_t prevn = nullptr, n;
     P.body.clear();
     bool record = true;  // the direct-launch loop replays the body's first copy
+    // consecutive kernels of the body are joined by programmatic edges (every body
+    // kernel begins with pdl_begin); where the driver refuses them, ordinary edges
+    const bool pdl = EIK_PDL && g_pdl_ok;
     auto add = [&](void* f, int grid, int block, size_t sm, void** params) -> std::string {
       if (record) P.body.push_back(Impl::Launch{f, grid, block, sm, (f == (void*)k_snapshot) ? L.dim : 0});
       cudaKernelNodeParams q{};
       q.func = f; q.gridDim = dim3(grid); q.blockDim = dim3(block); q.sharedMemBytes = (unsigned)sm;
       q.kernelParams = params;
-      CK(cudaGraphAddKernelNode(&n, body, prevn ? &prevn : nullptr, prevn ? 1 : 0, &q));
+      if (prevn && pdl) {
+        CK(cudaGraphAddKernelNode(&n, body, nullptr, 0, &q));
+        cudaGraphEdgeData ed{};
+        ed.from_port = cudaGraphKernelNodePortProgrammatic;
+        ed.type = cudaGraphDependencyTypeProgrammatic;
+        if (cudaGraphAddDependencies(body, &prevn, &n, &ed, 1) != cudaSuccess) {
+          (void)cudaGetLastError();
+          CK(cudaGraphAddDependencies(body, &prevn, &n, nullptr, 1));
+        }
+      } else {
+        CK(cudaGraphAddKernelNode(&n, body, prevn ? &prevn : nullptr, prevn ? 1 : 0, &q));
+      }
       prevn = n;
       return "";
     };
@@ -2252,7 +2307,13 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
       if (want_hist)
         if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
     }
-    CK(cudaGraphInstantiate(&P.exec, P.graph, 0));
+    if (cudaGraphInstantiate(&P.exec, P.graph, 0) != cudaSuccess) {
+      if (!pdl) CK(cudaGetLastError());
+      // programmatic edges inside the loop body refused: build it again without
+      (void)cudaGetLastError();
+      g_pdl_ok = false;
+      return build_graph(L, sweeps, threads, hcap, serve);
+    }
     P.g_sweeps = sweeps;
     P.g_threads = threads;
     P.g_hist = want_hist;
