@@ -164,6 +164,9 @@ constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::kt
 #ifndef EIK_SWEEP_ITEMS
 #define EIK_SWEEP_ITEMS 1
 #endif
+#ifndef EIK_MEMO_PREFETCH
+#define EIK_MEMO_PREFETCH 0
+#endif
 #ifndef EIK_SWEEP_MEMO
 #define EIK_SWEEP_MEMO 1
 #endif
@@ -709,6 +712,9 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
   // the first block of a CTA is its own index; later ones come from the counter
   // (a CTA without a first block exits without touching it)
   int first_item = blockIdx.x;
+  // a single instance's finished flag, read once (it changes only between launches):
+  // spares every visit the instance lookup
+  const int done1 = (a.ninst == 1) ? a.inst_done[0] : -1;
   for (;;) {
     int item = first_item;
     if (item < 0) {
@@ -719,12 +725,18 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
     first_item = -1;
     if (item >= count) break;
     const int b = list[item];
-    if (a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
+    const BlockDesc bd = a.blocks[b];
+    if (done1 >= 0 ? done1 : a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
       __syncthreads();
       continue;
     }
-    const BlockDesc bd = a.blocks[b];
     SmemItems s = s0;
+#if EIK_MEMO_PREFETCH
+    // the first sweep reads every slot's memo: start those loads with the block's
+    if (a.fim_memo)
+      for (int j = tid * 8; j < bd.nslots; j += NT * 8)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(a.fim_memo + bd.slot_begin + j));
+#endif
     if (!load_block(a, bd, 6, s, &bar, parity, a.Ta)) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);
@@ -733,13 +745,9 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
     }
     __syncthreads();
     const int ns = bd.nslots, nown = bd.nowned, pitch = bd.nslots_pad;
-    // per-slot copies of corners owned by other blocks start from the halo values
-    for (int j = bd.ninside + tid; j < ns; j += NT) {
-      const uint2 l = s.lv[j];
-      const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
-#pragma unroll
-      for (int k = 0; k < 4; ++k) s.h0[4 * j + k] = (id[k] < nown) ? 0.0f : s.vt[id[k]];
-    }
+    // per-slot copies of corners owned by other blocks start from the halo values,
+    // which stay in vt for the whole visit: the first sweep reads them there, and
+    // the second compares its copies with them
     int myconv = 1;
     for (int sw = 0; sw < nsweeps; ++sw) {
       const bool first = (sw == 0), last = (sw == nsweeps - 1);
@@ -757,12 +765,16 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             const bool o = id[q] < nown;
-            const float T = o ? s.vt[id[q]] : s.h0[4 * j + q];
+            const float T = (o || first) ? s.vt[id[q]] : s.h0[4 * j + q];
             Tq[q] = T;
             big |= (T >= kLarge3DDev ? 1u : 0u) << q;
             // a copy changed in the previous sweep when it differs from that sweep's
-            // input, still held in h1 (the buffers swap after every sweep)
-            chg |= (first ? 1u : (o ? (unsigned)s.vchg[id[q]] : (T != s.h1[4 * j + q] ? 1u : 0u))) << q;
+            // input: the halo value after the first sweep, else still held in h1 (the
+            // buffers swap after every sweep)
+            chg |= (first ? 1u
+                          : (o ? (unsigned)s.vchg[id[q]]
+                               : (T != (sw == 1 ? s.vt[id[q]] : s.h1[4 * j + q]) ? 1u : 0u)))
+                   << q;
             own |= (o ? 1u : 0u) << q;
             if (!o && !last) s.h1[4 * j + q] = T;  // kept unless its update below changes it
           }
@@ -820,7 +832,7 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
         const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
         float T[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) T[q] = (id[q] < nown) ? s.vt[id[q]] : s.h0[4 * j + q];
+        for (int q = 0; q < 4; ++q) T[q] = (id[q] < nown || sw == 0) ? s.vt[id[q]] : s.h0[4 * j + q];
         const TetGram gm = tet_gram9(s.coef[0 * pitch + j], s.coef[1 * pitch + j], s.coef[2 * pitch + j],
                                      s.coef[3 * pitch + j], s.coef[4 * pitch + j], s.coef[5 * pitch + j]);
         float u;
@@ -944,6 +956,9 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
   // the first block of a CTA is its own index; later ones come from the counter
   // (a CTA without a first block exits without touching it)
   int first_item = blockIdx.x;
+  // a single instance's finished flag, read once (it changes only between launches):
+  // spares every visit the instance lookup
+  const int done1 = (a.ninst == 1) ? a.inst_done[0] : -1;
   for (;;) {
     int item = first_item;
     if (item < 0) {
@@ -954,11 +969,11 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
     first_item = -1;
     if (item >= count) break;
     const int b = a.list_new[item];
-    if (a.inst_done[a.blk_inst[b]]) {
+    const BlockDesc bd = a.blocks[b];
+    if (done1 >= 0 ? done1 : a.inst_done[a.blk_inst[b]]) {
       __syncthreads();
       continue;
     }
-    const BlockDesc bd = a.blocks[b];
     if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo)) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);

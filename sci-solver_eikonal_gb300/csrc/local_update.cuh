@@ -645,7 +645,26 @@ __device__ __forceinline__ TetGram tet_gram9(float ACBC, float BCCD, float ACCD,
 #ifndef EIK_TET_ONEBODY
 #define EIK_TET_ONEBODY 1
 #endif
-#if EIK_TET_ONEBODY
+#if EIK_TET_ONEBODY == 2
+// two out-of-line bodies: apexes A, B and C share one (their masks differ at 8
+// sites, taken at run time), apex D has its own
+constexpr unsigned long long kFuseAll = kFuseApexA & kFuseApexB & kFuseApexC;
+constexpr unsigned long long kFuseRt = (kFuseApexA ^ kFuseApexB) | (kFuseApexA ^ kFuseApexC);
+__device__ __noinline__ float tet_update_rt(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                            float BCBC, float BCCD, float CDCD, unsigned long long m) {
+  return EIK_TET_UPDATE<kFuseAll, kFuseRt>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, m);
+}
+__device__ __noinline__ float tet_update_d(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                           float BCBC, float BCCD, float CDCD) {
+  return EIK_TET_UPDATE<kFuseApexD>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+}
+template <unsigned long long M>
+__device__ __forceinline__ float tet_update_call(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                                 float BCBC, float BCCD, float CDCD) {
+  if constexpr (M == kFuseApexD) return tet_update_d(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+  else return tet_update_rt(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, M);
+}
+#elif EIK_TET_ONEBODY
 // one out-of-line body for all four apex kinds: the sites where their masks agree
 // are fixed at compile time, the 13 others (kFuseRt) follow the kind's mask at run
 // time through selects; a third of the code for the instruction cache (65^3 sweep
