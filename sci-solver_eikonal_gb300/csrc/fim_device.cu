@@ -129,6 +129,9 @@ struct DevArgs {
   // 3D sweep visits (k_sweep3d): per slot the four input times of the last sweep
   // of the block's latest visit in this solve (all ones: none recorded)
   uint4* fim_memo;
+  // 3D: per slot four fp16 lower bounds, one per apex, on every candidate's
+  // distance term (plane_skip); null: none
+  const uint2* hsb;
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -317,17 +320,19 @@ __host__ __device__ inline size_t smem_bytes(int ncoef, int max_slots_pad, int m
 template <class S>
 __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd, int ncoef, const S& s,
                                            unsigned long long* bar, unsigned& parity, const float* Tsrc,
-                                           uint4* smemo = nullptr) {
+                                           uint4* smemo = nullptr, uint2* shs = nullptr) {
   const int tid = threadIdx.x, NT = blockDim.x;
   if (tid == 0) {
     fence_proxy_async();
     const unsigned bc = 4u * ncoef * bd.nslots_pad, bl = 8u * bd.nslots_pad;
     const unsigned bm = smemo ? 16u * bd.nslots_pad : 0u;
-    if (bc + bl + bm > 0) {
-      mbar_expect_tx(bar, bc + bl + bm);
+    const unsigned bh = (shs && a.hsb) ? 8u * bd.nslots_pad : 0u;
+    if (bc + bl + bm + bh > 0) {
+      mbar_expect_tx(bar, bc + bl + bm + bh);
       bulk_g2s(s.coef, a.coef + (size_t)ncoef * bd.slot_begin, bc, bar);
       bulk_g2s(s.lv, a.lv + bd.slot_begin, bl, bar);
       if (bm) bulk_g2s(smemo, a.chk_memo + bd.slot_begin, bm, bar);
+      if (bh) bulk_g2s(shs, a.hsb + bd.slot_begin, bh, bar);
     } else {
       mbar_expect_tx(bar, 0);
     }
@@ -351,6 +356,89 @@ __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd
 // root.  So an apex time T <= RN(m (1 - 2^-20)) < m (1 - 2^-21) keeps its value:
 // min(T, update) = T, and the update can be skipped without changing any bit.
 __device__ __forceinline__ bool upwind_skip(float Tk, float m) { return Tk <= __fmul_rn(m, 0x1.ffffep-1f); }
+
+// The same with a lower bound hs on the distance term of every candidate: each
+// candidate is a convex combination of the three other times (>= m (1 - 2^-22)) plus
+// the rounded square root of a computed metric distance from the apex to a point of
+// the opposite face's plane, which k_plane_bounds shows is >= hs^2; the rounded sum
+// is then > RN(RN(m + hs) (1 - 2^-20)), and an apex at or below that keeps its time.
+// hs = 0 gives upwind_skip.
+__device__ __forceinline__ bool plane_skip(float Tk, float m, float hs) {
+  return Tk <= __fmul_rn(__fadd_rn(m, hs), 0x1.ffffep-1f);
+}
+// fp16 bit patterns (non-negative, normal or zero) to float, exactly
+__device__ __forceinline__ float half_bits_value(unsigned h) {
+  h &= 0xffffu;
+  return (h >> 10) ? __uint_as_float((((h >> 10) + 112u) << 23) | ((h & 1023u) << 13)) : 0.0f;
+}
+// bound of apex k of slot j (the k-th fp16 of hsb[j])
+__device__ __forceinline__ float slot_bound(const uint2* hs, int j, int k) {
+  if (!hs) return 0.0f;
+  const uint2 w = hs[j];
+  return half_bits_value((k < 2 ? w.x : w.y) >> (16 * (k & 1)));
+}
+// Largest fp16 (non-negative, normal or zero) at or below x >= 0.
+__device__ __forceinline__ unsigned half_bits_down(float x) {
+  if (!(x > 0.0f)) return 0u;
+  const unsigned b = __float_as_uint(x);
+  const int e = (int)((b >> 23) & 255u) - 112;
+  if (e <= 0) return 0u;
+  if (e >= 31) return 0x7bffu;
+  return ((unsigned)e << 10) | ((b >> 13) & 1023u);
+}
+// Lower bound on the metric distance terms of one apex update with inputs
+// (XX, XY, XZ, YY, YZ, ZZ) as tet_update_x takes them (ACAC, ACBC, ACCD, BCBC, BCCD,
+// CDCD).  Every distance the update computes is the quadratic form
+// Q(l1, l2) = XX l1^2 + 2 XY l1 l2 + YY l2^2 + 2 XZ l1 + 2 YZ l2 + ZZ at a point of the
+// face's plane (l1, l2 in [0, 1] or a corner), evaluated with at most ~36 u G of
+// rounding error (u = 2^-24, G the largest input magnitude: at most three products
+// and sums of terms <= 3 G feed each rounding); where the 2x2 block is positive
+// definite, Q >= ZZ - (YY XZ^2 - 2 XY XZ YZ + XX YZ^2) / det everywhere on the plane.
+// Evaluated in FP64 with directed rounding: the result is <= sqrt(min Q - 64 u G).
+__device__ unsigned plane_bound_bits(float XXf, float XYf, float XZf, float YYf, float YZf, float ZZf) {
+  const double XX = XXf, XY = XYf, XZ = XZf, YY = YYf, YZ = YZf, ZZ = ZZf;
+  if (!(XX > 0.0)) return 0u;
+  const double det = __dsub_rd(XX * YY, XY * XY);  // the products are exact
+  if (!(det > 0.0)) return 0u;
+  const double t = XY * XZ;  // exact
+  const double num = __dadd_ru(__dadd_ru(__dmul_ru(YY, XZ * XZ), __dmul_ru(XX, YZ * YZ)), __dmul_ru(-2.0 * t, YZ));
+  if (!(num >= 0.0)) return 0u;
+  const double G = fmax(fmax(fmax(fabs(XX), fabs(XY)), fmax(fabs(XZ), fabs(YY))), fmax(fabs(YZ), fabs(ZZ)));
+  const double h2 = __dsub_rd(__dsub_rd(ZZ, __ddiv_ru(num, det)), 0x1p-18 * G);
+  if (!(h2 > 0.0)) return 0u;
+  return half_bits_down(__fmul_rd(__double2float_rd(__dsqrt_rd(h2)), 0x1.ffep-1f));
+}
+// k_plane_bounds: the bounds of every slot of blocks [0, nb) from its stored metric
+// products, with the remaining products formed as tet_gram9 forms them and the
+// argument order of apex_update.
+__global__ void k_plane_bounds(const BlockDesc* blocks, int nb, const float* coef, uint2* hsb) {
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    const BlockDesc d = blocks[b];
+    const size_t np = (size_t)d.nslots_pad;
+    for (int j = threadIdx.x; j < d.nslots_pad; j += blockDim.x) {
+      uint2 w = make_uint2(0u, 0u);
+      if (j < d.nslots) {
+        const float* c = coef + 6 * (size_t)d.slot_begin + j;
+        const TetGram g = tet_gram9(c[0], c[np], c[2 * np], c[3 * np], c[4 * np], c[5 * np]);
+        const unsigned hA = plane_bound_bits(g.BCBC, -g.BCCD, -g.ACBC, g.CDCD, g.ACCD, g.ACAC);
+        const unsigned hB = plane_bound_bits(g.ACAC, -g.ACCD, -g.ACBC, g.CDCD, g.BCCD, g.BCBC);
+        const unsigned hC = plane_bound_bits(g.ADAD, g.ADBD, -g.ADCD, g.BDBD, -g.CDBD, g.CDCD);
+        const unsigned hD = plane_bound_bits(g.ACAC, g.ACBC, g.ACCD, g.BCBC, g.BCCD, g.CDCD);
+        w = make_uint2(hA | (hB << 16), hC | (hD << 16));
+      }
+      hsb[(size_t)d.slot_begin + j] = w;
+    }
+  }
+}
+
+// (Re)computes the apex distance bounds of blocks [b0, b0 + nb) from their
+// coefficients (3D layouts).
+std::string plane_bounds(const BlockDesc* blocks, int b0, int nb, const float* coef, uint2* hsb, cudaStream_t st) {
+  if (!hsb || nb <= 0) return "";
+  k_plane_bounds<<<std::max(1, std::min(nb, 4096)), 256, 0, st>>>(blocks + b0, nb, coef, hsb);
+  const cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? std::string() : std::string("CUDA error: ") + cudaGetErrorString(err);
+}
 
 // ===========================================================================
 // 3D visit: kCheck = false -> FIMCuda (fim_sweeps sweeps, writes visit outputs);
@@ -650,9 +738,10 @@ struct SmemItems {
   int* vnew;            // max_owned keys
   unsigned char* vchg;  // max_owned
   unsigned short* items;  // 4 lists of max_slots_pad slot indices (one per apex)
+  uint2* hs;              // max_slots_pad: the apexes' distance bounds (plane_skip)
 };
 
-__host__ __device__ inline size_t items_offsets(int np, int max_local, int max_owned, size_t off[8]) {
+__host__ __device__ inline size_t items_offsets(int np, int max_local, int max_owned, size_t off[9]) {
   size_t o = 0;
   auto take = [&](size_t bytes, size_t align) {
     o = (o + align - 1) & ~(align - 1);
@@ -668,14 +757,15 @@ __host__ __device__ inline size_t items_offsets(int np, int max_local, int max_o
   off[5] = take(4 * (size_t)max_owned, 4);  // vnew
   off[6] = take((size_t)max_owned, 1);      // vchg
   off[7] = take(8 * (size_t)np, 2);         // items
+  off[8] = take(8 * (size_t)np, 16);        // hs
   return (o + 15) & ~(size_t)15;
 }
 __host__ __device__ inline size_t smem_bytes_items(int np, int max_local, int max_owned) {
-  size_t off[8];
+  size_t off[9];
   return items_offsets(np, max_local, max_owned, off);
 }
 __device__ __forceinline__ SmemItems carve_items(unsigned char* sm, const DevArgs& a) {
-  size_t off[8];
+  size_t off[9];
   items_offsets(a.max_slots_pad, a.max_local, a.max_owned, off);
   SmemItems s;
   s.coef = reinterpret_cast<float*>(sm + off[0]);
@@ -686,6 +776,7 @@ __device__ __forceinline__ SmemItems carve_items(unsigned char* sm, const DevArg
   s.vnew = reinterpret_cast<int*>(sm + off[5]);
   s.vchg = sm + off[6];
   s.items = reinterpret_cast<unsigned short*>(sm + off[7]);
+  s.hs = reinterpret_cast<uint2*>(sm + off[8]);
   return s;
 }
 
@@ -737,7 +828,7 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
       for (int j = tid * 8; j < bd.nslots; j += NT * 8)
         asm volatile("prefetch.global.L1 [%0];" ::"l"(a.fim_memo + bd.slot_begin + j));
 #endif
-    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta)) {
+    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, nullptr, a.hsb ? s.hs : nullptr)) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);
       __syncthreads();
@@ -796,7 +887,8 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
             const float m = fminf(fminf(Tq[(k + 1) & 3], Tq[(k + 2) & 3]), Tq[(k + 3) & 3]);
             const bool ownk = ((own >> k) & 1u) != 0;
             const bool run = ((big & others) != others) && (chg & others) && (!last || ownk) &&
-                             !(ownk && (same & others) == others) && !upwind_skip(Tq[k], m);
+                             !(ownk && (same & others) == others) &&
+                             !plane_skip(Tq[k], m, slot_bound(a.hsb ? s.hs : nullptr, j, k));
             need |= (run ? 1u : 0u) << k;
           }
         }
@@ -904,8 +996,9 @@ struct SmemCheck {
   float* vt;              // max_local
   int* vnew;              // max_owned (filled by load_block, unused here)
   unsigned short* items;  // 4 lists of max_slots_pad
+  uint2* hs;              // max_slots_pad: the apexes' distance bounds (plane_skip)
 };
-__host__ __device__ inline size_t check_offsets(int np, int max_local, int max_owned, size_t off[6]) {
+__host__ __device__ inline size_t check_offsets(int np, int max_local, int max_owned, size_t off[7]) {
   size_t o = 0;
   auto take = [&](size_t bytes, size_t align) {
     o = (o + align - 1) & ~(align - 1);
@@ -919,10 +1012,11 @@ __host__ __device__ inline size_t check_offsets(int np, int max_local, int max_o
   off[3] = take(4 * (size_t)max_local, 4);
   off[4] = take(4 * (size_t)max_owned, 4);
   off[5] = take(8 * (size_t)np, 2);
+  off[6] = take(8 * (size_t)np, 16);
   return (o + 15) & ~(size_t)15;
 }
 __host__ __device__ inline size_t smem_bytes_check(int np, int max_local, int max_owned) {
-  size_t off[6];
+  size_t off[7];
   return check_offsets(np, max_local, max_owned, off);
 }
 
@@ -933,7 +1027,7 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
   __shared__ int s_item;
   __shared__ volatile int s_moved;
   __shared__ int s_cnt[5];  // items per apex kind, then the next unclaimed item
-  size_t off[6];
+  size_t off[7];
   check_offsets(a.max_slots_pad, a.max_local, a.max_owned, off);
   SmemCheck s;
   s.coef = reinterpret_cast<float*>(sm + off[0]);
@@ -942,7 +1036,9 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
   s.vt = reinterpret_cast<float*>(sm + off[3]);
   s.vnew = reinterpret_cast<int*>(sm + off[4]);
   s.items = reinterpret_cast<unsigned short*>(sm + off[5]);
+  s.hs = reinterpret_cast<uint2*>(sm + off[6]);
   uint4* const smemo = a.chk_memo ? s.memo : nullptr;
+  const uint2* const shs = a.hsb ? s.hs : nullptr;
   const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
   const int np = a.max_slots_pad;
   const Ctl* ctl = a.ctl;
@@ -974,7 +1070,7 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
       __syncthreads();
       continue;
     }
-    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo)) {
+    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo, const_cast<uint2*>(shs))) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);
       __syncthreads();
@@ -1003,7 +1099,7 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const float m = fminf(fminf(T[(k + 1) & 3], T[(k + 2) & 3]), T[(k + 3) & 3]);
-            const bool run = id[k] < nown && m < kLarge3DDev && !upwind_skip(T[k], m);
+            const bool run = id[k] < nown && m < kLarge3DDev && !plane_skip(T[k], m, slot_bound(shs, j, k));
             need |= (run ? 1u : 0u) << k;
           }
         }
@@ -2040,7 +2136,8 @@ struct DeviceSolve::Impl {
   // measured so far and their sweep-kernel time per slot visit
   int tune_n[2] = {0, 0};
   float tune_cost[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-  uint4* chk_memo = nullptr;  // 3D: check memos of the coef_n / 6 slots, then their sweep memos
+  uint4* chk_memo = nullptr;
+  uint2* hsb = nullptr;  // 3D: coef_n / 6 slots of apex distance bounds (k_plane_bounds)  // 3D: check memos of the coef_n / 6 slots, then their sweep memos
   // host staging for the initial state
   std::vector<float> h_prev;  // caller's initial values (renumbered), empty when none
   std::vector<int> h_seed_ids, h_act, h_vblock, h_done, h_maxit;
@@ -2105,9 +2202,10 @@ struct DeviceSolve::Impl {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
                   blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids,
-                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo};
+                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo, hsb};
     for (void* p : ps)
       if (p) cudaFree(p);
+    hsb = nullptr;
     slot_f64 = nullptr;
     coef64 = nullptr;
     res_cand = nullptr;
@@ -2166,6 +2264,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.coef64 = P.coef64;
     // (serving clears an instance's memos when admission rewrites its coefficients)
     a.chk_memo = (L.dim == 3) ? P.chk_memo : nullptr;
+    a.hsb = (L.dim == 3) ? P.hsb : nullptr;
     if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
@@ -2541,6 +2640,10 @@ std::string DeviceSolve::refresh_coef_built(const float* M, int mcomp) {
   k_admit_coef3d<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.slot_elem, src.xyz,
                                                                     src.tets, src.M6, src.mcomp, 1.0f, nullptr, 0);
   CK(cudaGetLastError());
+  {
+    std::string e = plane_bounds(P.blocks, 0, L.nb, P.coef, P.hsb, st);
+    if (!e.empty()) return e;
+  }
   CK(cudaStreamSynchronize(st));
   return "";
 }
@@ -2548,6 +2651,10 @@ std::string DeviceSolve::refresh_coef_built(const float* M, int mcomp) {
 std::string DeviceSolve::finish_upload(const Layout& L, bool layout_on_device) {
   Impl& P = *p_;
   std::string e;
+  if (L.dim == 3) {
+    if (!(e = dev_alloc(P.hsb, std::max<size_t>(P.coef_n / 6, 1))).empty()) return e;
+    if (!(e = plane_bounds(P.blocks, 0, L.nb, P.coef, P.hsb, (cudaStream_t)stream_)).empty()) return e;
+  }
   for (float** t : {&P.Ta, &P.Tb, &P.Tinit, &P.prev, &P.out_tmp})
     if (!(e = dev_alloc(*t, (size_t)L.nv)).empty()) return e;
   for (int** t : {&P.conv, &P.stampA, &P.stampC, &P.list0, &P.list1, &P.list_new})
@@ -2613,6 +2720,10 @@ std::string DeviceSolve::upload_coef(const Layout& L) {
   if (L.coef.size() != P.coef_n) return "coefficient size changed; upload the layout again";
   CK(cudaMemcpyAsync(P.coef, L.coef.data(), sizeof(float) * L.coef.size(), cudaMemcpyHostToDevice,
                      (cudaStream_t)stream_));
+  if (L.dim == 3) {
+    std::string e = plane_bounds(P.blocks, 0, L.nb, P.coef, P.hsb, (cudaStream_t)stream_);
+    if (!e.empty()) return e;
+  }
   CK(cudaStreamSynchronize((cudaStream_t)stream_));
   return "";
 }
@@ -3028,7 +3139,8 @@ size_t device_footprint(const Layout& L, const Built3D* b) {
   const size_t nhalo = b ? (size_t)b->nhalo : L.halo_ids.size();
   const size_t ngraph = b ? nb + 1 + (size_t)b->nnbr : L.nbr_off.size() + L.nbr.size();
   return nb * sizeof(BlockDesc) + ncoef * sizeof(float) + (size_t)L.total_slots * (sizeof(uint2) + sizeof(int)) +
-         (L.dim == 3 ? 2 * (size_t)L.total_slots * sizeof(uint4) : 0) + nhalo * sizeof(int) + ngraph * sizeof(int) +
+         (L.dim == 3 ? (size_t)L.total_slots * (2 * sizeof(uint4) + sizeof(uint2)) : 0) + nhalo * sizeof(int) +
+         ngraph * sizeof(int) +
          nv * (2 * sizeof(int) + 5 * sizeof(float)) + nb * (7 * sizeof(int) + 1) + 5 * sizeof(int);
 }
 
@@ -3196,11 +3308,14 @@ std::string DeviceSolve::serve_admit(const std::vector<Admission>& adm) {
         P.args, v0, nvi, b0, nbi, large);
     const Impl::Source& src = P.src[P.inst_mesh[i]];
     const int g = std::max(1, std::min(nbi, 4096));
-    if (L.dim == 3)
+    if (L.dim == 3) {
       k_admit_coef3d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.xyz, src.tets, src.M6,
                                         src.mcomp, x.coef_scale, P.chk_memo, P.coef_n / 6);
-    else
+      std::string e = plane_bounds(P.blocks, b0, nbi, P.coef, P.hsb, st);
+      if (!e.empty()) return e;
+    } else {
       k_admit_coef2d<<<g, 256, 0, st>>>(P.blocks + b0, nbi, P.coef, P.slot_elem, src.speed, x.coef_scale);
+    }
     k_admit_seeds<<<1, 256, 0, st>>>(P.args, i, P.seed_ids + off[q], nsd[q], P.seed_ids + boff[q], nbk[q],
                                      x.max_iterations, L.dim);
   }

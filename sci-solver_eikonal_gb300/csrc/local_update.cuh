@@ -643,11 +643,13 @@ __device__ __forceinline__ TetGram tet_gram9(float ACBC, float BCCD, float ACCD,
 #define EIK_TET_NOINLINE 1
 #endif
 #ifndef EIK_TET_ONEBODY
-#define EIK_TET_ONEBODY 1
+#define EIK_TET_ONEBODY 2
 #endif
 #if EIK_TET_ONEBODY == 2
 // two out-of-line bodies: apexes A, B and C share one (their masks differ at 8
-// sites, taken at run time), apex D has its own
+// sites, taken at run time through selects), apex D has its own: little code for
+// the instruction cache, few selects (65^3 sweep kernel 2% faster than one body for
+// all four kinds, 4-6% faster than one body per mask; same bits)
 constexpr unsigned long long kFuseAll = kFuseApexA & kFuseApexB & kFuseApexC;
 constexpr unsigned long long kFuseRt = (kFuseApexA ^ kFuseApexB) | (kFuseApexA ^ kFuseApexC);
 __device__ __noinline__ float tet_update_rt(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
