@@ -402,15 +402,17 @@ def launch_dram(name):
 def sweep_bytes(it):
     """Algorithmic bytes of one sweep-kernel launch from its iteration's counters
     (Eikonal.iterationStats columns): per slot 6 float metric terms + 4 u16 corner
-    ids (32 B) and its sweep memo read and written (16 B each), owned + halo travel
-    times read (4 B each), owned times written (4 B), one block flag (4 B) per visit."""
-    return 64 * it[3] + 4 * (it[5] + it[4]) + 4 * it[5] + 4 * it[2]
+    ids (32 B), its sweep memo read and written (16 B each) and its four fp16 apex
+    bounds (8 B), owned + halo travel times read (4 B each), owned times written
+    (4 B), one block flag (4 B) per visit."""
+    return 72 * it[3] + 4 * (it[5] + it[4]) + 4 * it[5] + 4 * it[2]
 
 
 def check_bytes(it):
     """Algorithmic bytes of one check-kernel launch: per slot the metric terms and
-    ids (32 B) and its check memo (16 B), owned + halo times read, one list entry."""
-    return 48 * it[7] + 4 * (it[9] + it[8]) + 4 * it[6]
+    ids (32 B), its check memo (16 B) and apex bounds (8 B), owned + halo times read,
+    one list entry."""
+    return 56 * it[7] + 4 * (it[9] + it[8]) + 4 * it[6]
 
 
 def traffic_vs_algorithmic(its, profile):
