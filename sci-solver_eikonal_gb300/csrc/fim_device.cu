@@ -132,6 +132,9 @@ struct DevArgs {
   // 3D: per slot four fp16 lower bounds, one per apex, on every candidate's
   // distance term (plane_skip); null: none
   const uint2* hsb;
+  // precision mode: the same bounds for the FP64 updates of flagged tets, one uint2
+  // per FP64 product set (k_plane_bounds64); null: none
+  const uint2* hs64;
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -433,6 +436,42 @@ __global__ void k_plane_bounds(const BlockDesc* blocks, int nb, const float* coe
 
 // (Re)computes the apex distance bounds of blocks [b0, b0 + nb) from their
 // coefficients (3D layouts).
+// The bound for one FP64 apex update (precision mode: FP64 products, FP64
+// arithmetic, FP32 square roots of the distance terms).  h^2 is formed in FP64 with
+// round-to-nearest where the 2x2 block is well conditioned (det > 2^-30 XX YY), which
+// keeps its relative error below 2^-22 of the quotient, covered by a 2^-20 margin;
+// the update's FP64 distance terms carry at most ~40 2^-53 G of rounding, covered by
+// 2^-40 G; the FP32 square root costs at most 2^-23 relative, covered by 2^-20.
+__device__ unsigned plane_bound_bits64(double XX, double XY, double XZ, double YY, double YZ, double ZZ) {
+  if (!(XX > 0.0) || !(YY > 0.0)) return 0u;
+  const double det = XX * YY - XY * XY;
+  if (!(det > 0x1p-30 * XX * YY)) return 0u;
+  const double num = YY * XZ * XZ - 2.0 * XY * XZ * YZ + XX * YZ * YZ;
+  if (!(num >= 0.0)) return 0u;
+  const double q = num / det;
+  const double G = fmax(fmax(fmax(fabs(XX), fabs(XY)), fmax(fabs(XZ), fabs(YY))), fmax(fabs(YZ), fabs(ZZ)));
+  const double h2 = ZZ - q - 0x1p-20 * q - 0x1p-40 * G;
+  if (!(h2 > 0.0)) return 0u;
+  return half_bits_down(__fmul_rd(__double2float_rd(__dsqrt_rd(h2)), 0x1.ffffep-1f));
+}
+// k_plane_bounds64: the bounds of the FP64 updates of flagged tets [0, n), with the
+// remaining products formed in FP64 as the precision kernel forms them.
+__global__ void k_plane_bounds64(const double* coef64, int n, uint2* hs64) {
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+    const double* g = coef64 + 6 * (size_t)f;
+    const double dACBC = g[0], dBCCD = g[1], dACCD = g[2], dADBD = g[3], dACAD = g[4], dBCBD = g[5];
+    const double dADBC = dACBC + dBCCD, dACBD = dACBC + dACCD;
+    const double dCDBD = dADBD - dACBD, dADCD = dADBD - dADBC;
+    const double dCDCD = dADCD - dACCD, dADAD = dADCD + dACAD, dACAC = dACAD - dACCD;
+    const double dBDBD = dBCBD + dCDBD, dBCBC = dBCBD - dBCCD;
+    const unsigned hA = plane_bound_bits64(dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC);
+    const unsigned hB = plane_bound_bits64(dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC);
+    const unsigned hC = plane_bound_bits64(dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD);
+    const unsigned hD = plane_bound_bits64(dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD);
+    hs64[f] = make_uint2(hA | (hB << 16), hC | (hD << 16));
+  }
+}
+
 std::string plane_bounds(const BlockDesc* blocks, int b0, int nb, const float* coef, uint2* hsb, cudaStream_t st) {
   if (!hsb || nb <= 0) return "";
   k_plane_bounds<<<std::max(1, std::min(nb, 4096)), 256, 0, st>>>(blocks + b0, nb, coef, hsb);
@@ -564,16 +603,26 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
         // previous candidates exactly and is skipped.
         if (ch) {
           const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
-          nw[3] = fminf(TD, apex_update<3>(T, gm));
-          nw[0] = fminf(TA, apex_update<0>(T, gm));
-          nw[1] = fminf(TB, apex_update<1>(T, gm));
-          nw[2] = fminf(TC, apex_update<2>(T, gm));
+          // flagged tets (and every slot in the polish) take FP64 updates instead
+          const int f = kPrec ? a.slot_f64[bd.slot_begin + j] : -1;
+          const bool fp64 = kPrec && (f >= 0 || f64all);
+          if (!fp64) {
+            // apexes at or below the plane-distance bound of their update keep their
+            // time (plane_skip)
+            const uint2* hs = a.hsb ? a.hsb + bd.slot_begin : nullptr;
+            if (!plane_skip(TD, fminf(fminf(TA, TB), TC), slot_bound(hs, j, 3)))
+              nw[3] = fminf(TD, apex_update<3>(T, gm));
+            if (!plane_skip(TA, fminf(fminf(TB, TD), TC), slot_bound(hs, j, 0)))
+              nw[0] = fminf(TA, apex_update<0>(T, gm));
+            if (!plane_skip(TB, fminf(fminf(TA, TD), TC), slot_bound(hs, j, 1)))
+              nw[1] = fminf(TB, apex_update<1>(T, gm));
+            if (!plane_skip(TC, fminf(fminf(TA, TB), TD), slot_bound(hs, j, 2)))
+              nw[2] = fminf(TC, apex_update<2>(T, gm));
+          }
           if constexpr (kPrec) {
-            // flagged tet: the same four updates again in FP64 from FP64 products
-            // (the FP32 group above stays exactly the FP32 kernel's code)
+            // flagged tet: the four updates in FP64 from FP64 products
             // (polish: every slot, the unflagged ones from their FP32 products)
-            const int f = a.slot_f64[bd.slot_begin + j];
-            if (f >= 0 || f64all) {
+            if (fp64) {
               double g[6];
 #pragma unroll
               for (int q = 0; q < 6; ++q) g[q] = (f >= 0) ? a.coef64[6 * (size_t)f + q] : (double)s.coef[q * np + j];
@@ -587,17 +636,17 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
               // (the copies of other blocks' corners are dropped), so the FP64
               // updates of the others are left out there
               const bool all = !kCheck && sw != nsweeps - 1;
-              // an apex at or below the upwind bound of its other corners keeps its
-              // time under the FP64 update too (its candidates are convex combinations
-              // of those corners plus a root, as in FP32), and the FP32 result already
-              // in nw equals it
-              if ((all || own[3]) && !upwind_skip(TD, fminf(fminf(TA, TB), TC)))
+              // an apex at or below the plane-distance bound of its FP64 update (the
+              // upwind bound where the tet has none: polish of unflagged tets) keeps
+              // its time, which nw already holds
+              const uint2* hs = (f >= 0 && a.hs64) ? a.hs64 + f : nullptr;
+              if ((all || own[3]) && !plane_skip(TD, fminf(fminf(TA, TB), TC), slot_bound(hs, 0, 3)))
                 nw[3] = fminf(TD, (float)tet_update_f64(A, B, C, dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD));
-              if ((all || own[0]) && !upwind_skip(TA, fminf(fminf(TB, TD), TC)))
+              if ((all || own[0]) && !plane_skip(TA, fminf(fminf(TB, TD), TC), slot_bound(hs, 0, 0)))
                 nw[0] = fminf(TA, (float)tet_update_f64(B, D, C, dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC));
-              if ((all || own[1]) && !upwind_skip(TB, fminf(fminf(TA, TD), TC)))
+              if ((all || own[1]) && !plane_skip(TB, fminf(fminf(TA, TD), TC), slot_bound(hs, 0, 1)))
                 nw[1] = fminf(TB, (float)tet_update_f64(A, D, C, dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC));
-              if ((all || own[2]) && !upwind_skip(TC, fminf(fminf(TA, TB), TD)))
+              if ((all || own[2]) && !plane_skip(TC, fminf(fminf(TA, TB), TD), slot_bound(hs, 0, 2)))
                 nw[2] = fminf(TC, (float)tet_update_f64(A, B, D, dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD));
             }
           }
@@ -2137,7 +2186,8 @@ struct DeviceSolve::Impl {
   int tune_n[2] = {0, 0};
   float tune_cost[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
   uint4* chk_memo = nullptr;
-  uint2* hsb = nullptr;  // 3D: coef_n / 6 slots of apex distance bounds (k_plane_bounds)  // 3D: check memos of the coef_n / 6 slots, then their sweep memos
+  uint2* hsb = nullptr;  // 3D: coef_n / 6 slots of apex distance bounds (k_plane_bounds)
+  uint2* hs64 = nullptr;  // precision mode: bounds of the FP64 updates (k_plane_bounds64)  // 3D: check memos of the coef_n / 6 slots, then their sweep memos
   // host staging for the initial state
   std::vector<float> h_prev;  // caller's initial values (renumbered), empty when none
   std::vector<int> h_seed_ids, h_act, h_vblock, h_done, h_maxit;
@@ -2202,10 +2252,11 @@ struct DeviceSolve::Impl {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
                   blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids,
-                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo, hsb};
+                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo, hsb, hs64};
     for (void* p : ps)
       if (p) cudaFree(p);
     hsb = nullptr;
+    hs64 = nullptr;
     slot_f64 = nullptr;
     coef64 = nullptr;
     res_cand = nullptr;
@@ -2265,6 +2316,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     // (serving clears an instance's memos when admission rewrites its coefficients)
     a.chk_memo = (L.dim == 3) ? P.chk_memo : nullptr;
     a.hsb = (L.dim == 3) ? P.hsb : nullptr;
+    a.hs64 = P.hs64;
     if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
@@ -2683,6 +2735,12 @@ std::string DeviceSolve::finish_upload(const Layout& L, bool layout_on_device) {
     CK(cudaMemcpyAsync(P.slot_f64, L.slot_f64.data(), sizeof(int) * L.slot_f64.size(), cudaMemcpyHostToDevice, st));
     if (!L.coef64.empty())
       CK(cudaMemcpyAsync(P.coef64, L.coef64.data(), sizeof(double) * L.coef64.size(), cudaMemcpyHostToDevice, st));
+    const int nf64 = (int)(L.coef64.size() / 6);
+    if (!(e = dev_alloc(P.hs64, std::max<size_t>((size_t)nf64, 1))).empty()) return e;
+    if (nf64 > 0) {
+      k_plane_bounds64<<<std::max(1, std::min(4096, (nf64 + 255) / 256)), 256, 0, st>>>(P.coef64, nf64, P.hs64);
+      CK(cudaGetLastError());
+    }
     P.prec = true;
   }
   std::vector<int> bi(L.blk_inst);

@@ -184,10 +184,15 @@ def _ref3d_cases(mg, golden):
     M6 = mg.anisotropic_metrics(tets.shape[0], seed=6).ravel()
     seeds = np.random.default_rng(9).choice(xyz.shape[0], 4, replace=False).tolist()
     out.append(("sliver17_anisotropic", xyz, tets, M6, seeds, {"maxIterations_": 1000}))
+    # harder for the skip bounds: more slivers, anisotropy ratios up to 1e4
+    xyz, tets, _ = mg.sliver_cube(13, 0.25, seed=11)
+    M6 = mg.anisotropic_metrics(tets.shape[0], seed=12, lo=1.0, hi=1e4).ravel()
+    seeds = np.random.default_rng(13).choice(xyz.shape[0], 3, replace=False).tolist()
+    out.append(("sliver13_strongly_anisotropic", xyz, tets, M6, seeds, {"maxIterations_": 1000}))
     return out
 
 
-@pytest.mark.parametrize("idx", range(9))
+@pytest.mark.parametrize("idx", range(10))
 def test_3d_bitwise_vs_reference_kernels(need_gpu, eik, O, mg, golden, idx):
     need_ref(O)
     name, xyz, tets, sp, seeds, opts = _ref3d_cases(mg, golden)[idx]
