@@ -135,6 +135,10 @@ struct DevArgs {
   // precision mode: the same bounds for the FP64 updates of flagged tets, one uint2
   // per FP64 product set (k_plane_bounds64); null: none
   const uint2* hs64;
+  // precision mode's polish: the bounds of the FP64 updates of slots without FP64
+  // products, per slot (k_plane_bounds_u64); null: none
+  const uint2* hsu64;
+  int sweep_split;  // active blocks from which the large-grid sweep launch runs
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -164,11 +168,24 @@ __device__ __forceinline__ float settle_eps(float T, int polish) {
 }
 constexpr float kEps2D = 1e-5f;
 constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
+#if EIK_PREC_DS
+typedef dsf PrecWide;
+#else
+typedef double PrecWide;
+#endif
 // whether the driver accepted programmatic edges in a conditional loop body
 bool g_pdl_ok = true;
 constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::ktime)
 #ifndef EIK_SWEEP_ITEMS
 #define EIK_SWEEP_ITEMS 1
+#endif
+// active blocks below which the 3D sweep runs as 1024-thread CTAs (0: never)
+#ifndef EIK_SWEEP_SPLIT
+#define EIK_SWEEP_SPLIT 0
+#endif
+// precision mode's wide updates: double-float (1) or FP64 (0)
+#ifndef EIK_PREC_DS
+#define EIK_PREC_DS 0
 #endif
 #ifndef EIK_MEMO_PREFETCH
 #define EIK_MEMO_PREFETCH 0
@@ -454,6 +471,34 @@ __device__ unsigned plane_bound_bits64(double XX, double XY, double XZ, double Y
   if (!(h2 > 0.0)) return 0u;
   return half_bits_down(__fmul_rd(__double2float_rd(__dsqrt_rd(h2)), 0x1.ffffep-1f));
 }
+// k_plane_bounds_u64: the bounds of the polish's FP64 updates of every slot of
+// blocks [0, nb) from its FP32 products, formed in FP64 as the precision kernel
+// forms them for slots without FP64 products.
+__global__ void k_plane_bounds_u64(const BlockDesc* blocks, int nb, const float* coef, uint2* out) {
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    const BlockDesc d = blocks[b];
+    const size_t np = (size_t)d.nslots_pad;
+    for (int j = threadIdx.x; j < d.nslots_pad; j += blockDim.x) {
+      uint2 w = make_uint2(0u, 0u);
+      if (j < d.nslots) {
+        const float* c = coef + 6 * (size_t)d.slot_begin + j;
+        const double dACBC = c[0], dBCCD = c[np], dACCD = c[2 * np], dADBD = c[3 * np], dACAD = c[4 * np],
+                     dBCBD = c[5 * np];
+        const double dADBC = dACBC + dBCCD, dACBD = dACBC + dACCD;
+        const double dCDBD = dADBD - dACBD, dADCD = dADBD - dADBC;
+        const double dCDCD = dADCD - dACCD, dADAD = dADCD + dACAD, dACAC = dACAD - dACCD;
+        const double dBDBD = dBCBD + dCDBD, dBCBC = dBCBD - dBCCD;
+        const unsigned hA = plane_bound_bits64(dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC);
+        const unsigned hB = plane_bound_bits64(dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC);
+        const unsigned hC = plane_bound_bits64(dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD);
+        const unsigned hD = plane_bound_bits64(dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD);
+        w = make_uint2(hA | (hB << 16), hC | (hD << 16));
+      }
+      out[(size_t)d.slot_begin + j] = w;
+    }
+  }
+}
+
 // k_plane_bounds64: the bounds of the FP64 updates of flagged tets [0, n), with the
 // remaining products formed in FP64 as the precision kernel forms them.
 __global__ void k_plane_bounds64(const double* coef64, int n, uint2* hs64) {
@@ -623,15 +668,18 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
             // flagged tet: the four updates in FP64 from FP64 products
             // (polish: every slot, the unflagged ones from their FP32 products)
             if (fp64) {
-              double g[6];
+              typedef PrecWide W;
+              W g[6];
 #pragma unroll
-              for (int q = 0; q < 6; ++q) g[q] = (f >= 0) ? a.coef64[6 * (size_t)f + q] : (double)s.coef[q * np + j];
-              const double dACBC = g[0], dBCCD = g[1], dACCD = g[2], dADBD = g[3], dACAD = g[4], dBCBD = g[5];
-              const double dADBC = dACBC + dBCCD, dACBD = dACBC + dACCD;
-              const double dCDBD = dADBD - dACBD, dADCD = dADBD - dADBC;
-              const double dCDCD = dADCD - dACCD, dADAD = dADCD + dACAD, dACAC = dACAD - dACCD;
-              const double dBDBD = dBCBD + dCDBD, dBCBC = dBCBD - dBCCD;
-              const double A = TA, B = TB, C = TC, D = TD;
+              for (int q = 0; q < 6; ++q)
+                g[q] = (f >= 0) ? w_make(a.coef64[6 * (size_t)f + q], W{}) : w_make((double)s.coef[q * np + j], W{});
+              const W dACBC = g[0], dBCCD = g[1], dACCD = g[2], dADBD = g[3], dACAD = g[4], dBCBD = g[5];
+              const W dADBC = dACBC + dBCCD, dACBD = dACBC + dACCD;
+              const W dCDBD = dADBD - dACBD, dADCD = dADBD - dADBC;
+              const W dCDCD = dADCD - dACCD, dADAD = dADCD + dACAD, dACAC = dACAD - dACCD;
+              const W dBDBD = dBCBD + dCDBD, dBCBC = dBCBD - dBCCD;
+              const W A = w_make((double)TA, W{}), B = w_make((double)TB, W{}), C = w_make((double)TC, W{}),
+                      D = w_make((double)TD, W{});
               // in a check and in a visit's last sweep only the owned apexes count
               // (the copies of other blocks' corners are dropped), so the FP64
               // updates of the others are left out there
@@ -639,15 +687,16 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
               // an apex at or below the plane-distance bound of its FP64 update (the
               // upwind bound where the tet has none: polish of unflagged tets) keeps
               // its time, which nw already holds
-              const uint2* hs = (f >= 0 && a.hs64) ? a.hs64 + f : nullptr;
+              const uint2* hs = (f >= 0) ? (a.hs64 ? a.hs64 + f : nullptr)
+                                         : (a.hsu64 ? a.hsu64 + bd.slot_begin + j : nullptr);
               if ((all || own[3]) && !plane_skip(TD, fminf(fminf(TA, TB), TC), slot_bound(hs, 0, 3)))
-                nw[3] = fminf(TD, (float)tet_update_f64(A, B, C, dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD));
+                nw[3] = fminf(TD, w_float(tet_update_wide<W>(A, B, C, dACAC, dACBC, dACCD, dBCBC, dBCCD, dCDCD)));
               if ((all || own[0]) && !plane_skip(TA, fminf(fminf(TB, TD), TC), slot_bound(hs, 0, 0)))
-                nw[0] = fminf(TA, (float)tet_update_f64(B, D, C, dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC));
+                nw[0] = fminf(TA, w_float(tet_update_wide<W>(B, D, C, dBCBC, -dBCCD, -dACBC, dCDCD, dACCD, dACAC)));
               if ((all || own[1]) && !plane_skip(TB, fminf(fminf(TA, TD), TC), slot_bound(hs, 0, 1)))
-                nw[1] = fminf(TB, (float)tet_update_f64(A, D, C, dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC));
+                nw[1] = fminf(TB, w_float(tet_update_wide<W>(A, D, C, dACAC, -dACCD, -dACBC, dCDCD, dBCCD, dBCBC)));
               if ((all || own[2]) && !plane_skip(TC, fminf(fminf(TA, TB), TD), slot_bound(hs, 0, 2)))
-                nw[2] = fminf(TC, (float)tet_update_f64(A, B, D, dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD));
+                nw[2] = fminf(TC, w_float(tet_update_wide<W>(A, B, D, dADAD, dADBD, -dADCD, dBDBD, -dCDBD, dCDCD)));
             }
           }
         }
@@ -830,8 +879,13 @@ __device__ __forceinline__ SmemItems carve_items(unsigned char* sm, const DevArg
 }
 
 // at most 56 registers: three CTAs of 384 threads fit one SM's register file
-__global__ void __maxnreg__(56) k_sweep3d(DevArgs a) {
+// role: 0 runs every iteration; where the loop body holds two sweep launches of
+// different CTA sizes, 1 runs only iterations with at least a.sweep_split active
+// blocks and 2 only the others (few blocks: a visit's latency, which more threads
+// per block shorten, sets the launch's time)
+__global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
   pdl_begin();
+  if (role != 0 && ((a.ctl->nact >= a.sweep_split) != (role == 1))) return;
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
@@ -1776,7 +1830,10 @@ __global__ void k_gather_result(const float* Ta, const unsigned char* visited, c
 // update over its incident tets, from the final travel times.  Every tet incident
 // to a vertex is a slot of the vertex's own block, and every copy of a tet holds the
 // same products, so each block computes only its owned apexes.
-__global__ void k_residual3d(DevArgs a, unsigned long long* cand) {
+// lower_only: only candidates that can lie below a vertex's time are needed (the
+// polish's marking): apexes at or below the plane-distance bound of their FP64
+// update are left out.
+__global__ void k_residual3d(DevArgs a, unsigned long long* cand, int lower_only) {
   for (int b = blockIdx.x; b < a.nb; b += gridDim.x) {
     const BlockDesc bd = a.blocks[b];
     const size_t np = (size_t)bd.nslots_pad;
@@ -1798,10 +1855,21 @@ __global__ void k_residual3d(DevArgs a, unsigned long long* cand) {
       const double CDCD = ADCD - ACCD, ADAD = ADCD + ACAD, ACAC = ACAD - ACCD, BDBD = BCBD + CDBD;
       const double BCBC = BCBD - BCCD;
       double u[4] = {-1.0, -1.0, -1.0, -1.0};
-      if (id[3] < bd.nowned) u[3] = tet_update_f64(T[0], T[1], T[2], ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
-      if (id[0] < bd.nowned) u[0] = tet_update_f64(T[1], T[3], T[2], BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC);
-      if (id[1] < bd.nowned) u[1] = tet_update_f64(T[0], T[3], T[2], ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC);
-      if (id[2] < bd.nowned) u[2] = tet_update_f64(T[0], T[1], T[3], ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD);
+      bool run[4];
+      {
+        const uint2* hs = !lower_only ? nullptr
+                          : (f >= 0) ? (a.hs64 ? a.hs64 + f : nullptr)
+                                     : (a.hsu64 ? a.hsu64 + bd.slot_begin + j : nullptr);
+        const float Tf[4] = {(float)T[0], (float)T[1], (float)T[2], (float)T[3]};
+        for (int k = 0; k < 4; ++k) {
+          const float m = fminf(fminf(Tf[(k + 1) & 3], Tf[(k + 2) & 3]), Tf[(k + 3) & 3]);
+          run[k] = id[k] < bd.nowned && !(lower_only && plane_skip(Tf[k], m, slot_bound(hs, 0, k)));
+        }
+      }
+      if (run[3]) u[3] = tet_update_f64(T[0], T[1], T[2], ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
+      if (run[0]) u[0] = tet_update_f64(T[1], T[3], T[2], BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC);
+      if (run[1]) u[1] = tet_update_f64(T[0], T[3], T[2], ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC);
+      if (run[2]) u[2] = tet_update_f64(T[0], T[1], T[3], ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD);
       for (int k = 0; k < 4; ++k)
         if (u[k] >= 0.0) atomicMin(&cand[gid[k]], (unsigned long long)__double_as_longlong(u[k]));
     }
@@ -2187,7 +2255,8 @@ struct DeviceSolve::Impl {
   float tune_cost[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
   uint4* chk_memo = nullptr;
   uint2* hsb = nullptr;  // 3D: coef_n / 6 slots of apex distance bounds (k_plane_bounds)
-  uint2* hs64 = nullptr;  // precision mode: bounds of the FP64 updates (k_plane_bounds64)  // 3D: check memos of the coef_n / 6 slots, then their sweep memos
+  uint2* hs64 = nullptr;  // precision mode: bounds of the FP64 updates (k_plane_bounds64)
+  uint2* hsu64 = nullptr;  // precision mode: per slot, bounds of the polish's FP64 updates  // 3D: check memos of the coef_n / 6 slots, then their sweep memos
   // host staging for the initial state
   std::vector<float> h_prev;  // caller's initial values (renumbered), empty when none
   std::vector<int> h_seed_ids, h_act, h_vblock, h_done, h_maxit;
@@ -2252,11 +2321,12 @@ struct DeviceSolve::Impl {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
                   blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids,
-                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo, hsb, hs64};
+                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo, hsb, hs64, hsu64};
     for (void* p : ps)
       if (p) cudaFree(p);
     hsb = nullptr;
     hs64 = nullptr;
+    hsu64 = nullptr;
     slot_f64 = nullptr;
     coef64 = nullptr;
     res_cand = nullptr;
@@ -2317,6 +2387,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.chk_memo = (L.dim == 3) ? P.chk_memo : nullptr;
     a.hsb = (L.dim == 3) ? P.hsb : nullptr;
     a.hs64 = P.hs64;
+    a.hsu64 = P.hsu64;
     if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
@@ -2425,8 +2496,9 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     // consecutive kernels of the body are joined by programmatic edges (every body
     // kernel begins with pdl_begin); where the driver refuses them, ordinary edges
     const bool pdl = EIK_PDL && g_pdl_ok;
-    auto add = [&](void* f, int grid, int block, size_t sm, void** params) -> std::string {
-      if (record) P.body.push_back(Impl::Launch{f, grid, block, sm, (f == (void*)k_snapshot) ? L.dim : 0});
+    auto add = [&](void* f, int grid, int block, size_t sm, void** params, int extra = -1) -> std::string {
+      if (record)
+        P.body.push_back(Impl::Launch{f, grid, block, sm, extra >= 0 ? extra : (f == (void*)k_snapshot) ? L.dim : 0});
       cudaKernelNodeParams q{};
       q.func = f; q.gridDim = dim3(grid); q.blockDim = dim3(block); q.sharedMemBytes = (unsigned)sm;
       q.kernelParams = params;
@@ -2457,10 +2529,27 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     static int copy_idx[kBodyCopies] = {0, 1, 2, 3};  // read-only kernel arguments
     static_assert(kBodyCopies == 4, "copy_idx lists every copy");
     const int copies = serve ? 1 : kBodyCopies;
+    // the item sweep at its usual CTA size for iterations with many active blocks
+    // and at 1024 threads for the others (roles of k_sweep3d), each launch leaving
+    // the other's iterations at once
+    static int role_vals[3] = {0, 1, 2};  // read-only kernel arguments
+    void* sweep_args[3][2] = {{&P.args, &role_vals[0]}, {&P.args, &role_vals[1]}, {&P.args, &role_vals[2]}};
+    int grid_small = 0;
+    if (kv_fim == (void*)k_sweep3d && EIK_SWEEP_SPLIT > 0 && vthreads == kItemThreads) {
+      int occ2 = 0;
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_sweep3d, 1024, vsmem));
+      if (occ2 >= 1) grid_small = std::min(occ2 * nsm, std::max(L.nb, 1));
+    }
+    a.sweep_split = grid_small ? EIK_SWEEP_SPLIT : 0;
     for (int u = 0; u < copies; ++u) {
       record = (u == 0);
       void* close_args[] = {&P.args, &copy_idx[u]};
-      if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
+      if (grid_small) {
+        if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, sweep_args[1], 1)).empty()) return e;
+        if (!(e = add(kv_fim, grid_small, 1024, vsmem, sweep_args[2], 2)).empty()) return e;
+      } else if (!(e = add(kv_fim, P.grid_visit, vthreads, vsmem, sweep_args[0], 0)).empty()) {
+        return e;
+      }
       if (L.dim == 3) {
         if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
         if (!(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
@@ -2741,6 +2830,9 @@ std::string DeviceSolve::finish_upload(const Layout& L, bool layout_on_device) {
       k_plane_bounds64<<<std::max(1, std::min(4096, (nf64 + 255) / 256)), 256, 0, st>>>(P.coef64, nf64, P.hs64);
       CK(cudaGetLastError());
     }
+    if (!(e = dev_alloc(P.hsu64, std::max<size_t>(P.coef_n / 6, 1))).empty()) return e;
+    k_plane_bounds_u64<<<std::max(1, std::min(L.nb, 4096)), 256, 0, st>>>(P.blocks, L.nb, P.coef, P.hsu64);
+    CK(cudaGetLastError());
     P.prec = true;
   }
   std::vector<int> bi(L.blk_inst);
@@ -2992,7 +3084,7 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     for (int round = 0; round < kPolishRounds; ++round) {
       CK(cudaMemsetAsync(P.res_cand, 0x7f, sizeof(unsigned long long) * L.nv, st));
-      k_residual3d<<<std::max(1, std::min(L.nb, 8 * nsm)), 256, 0, st>>>(P.args, P.res_cand);
+      k_residual3d<<<std::max(1, std::min(L.nb, 8 * nsm)), 256, 0, st>>>(P.args, P.res_cand, 1);
       k_polish_begin<<<1, 256, 0, st>>>(P.args, kPolishIterations);
       k_polish_mark<<<std::max(1, std::min(4 * nsm, (L.nv + 255) / 256)), 256, 0, st>>>(P.args, P.res_cand, P.stampC,
                                                                                       -(round + 1), kPolishTol);
@@ -3062,7 +3154,7 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    k_residual3d<<<std::max(1, std::min(L.nb, 8 * nsm)), 256, 0, st>>>(P.args, P.res_cand);
+    k_residual3d<<<std::max(1, std::min(L.nb, 8 * nsm)), 256, 0, st>>>(P.args, P.res_cand, 0);
     k_residual_reduce<<<std::max(1, std::min(4 * nsm, (L.nv + 255) / 256)), 256, 0, st>>>(P.args, P.res_cand,
                                                                                        P.res_cand + L.nv);
     CK(cudaGetLastError());

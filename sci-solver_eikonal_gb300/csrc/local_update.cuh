@@ -715,103 +715,188 @@ __device__ __forceinline__ float apex_update(const float T[4], const TetGram& g)
   return kLarge3DDev;
 }
 
-// Square root of a non-negative candidate distance for the FP64 update: the
-// argument is formed in FP64 (where the cancellation is), the root taken in FP32
-// (relative error below 1e-7, far inside the scheme's 1e-5 tolerance), which
+// Double-float numbers (precision mode, EIK_PREC_DS): an unevaluated sum hi + lo of
+// two floats, |lo| <= ulp(hi) / 2, with about 48 bits of significand, built from
+// error-free transformations (Knuth's two-sum, the FMA two-product; Dekker 1971,
+// Hida, Li and Bailey 2001).  GB300's FP64 rate is 1/64 of FP32: a double-float
+// operation costs a handful of FP32 ones.
+struct dsf {
+  float hi, lo;
+};
+__device__ __forceinline__ dsf ds_make(float a) { return dsf{a, 0.0f}; }
+__device__ __forceinline__ dsf ds_make(double a) {
+  const float h = (float)a;
+  return dsf{h, (float)(a - (double)h)};
+}
+__device__ __forceinline__ dsf ds_quick(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return dsf{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dsf ds_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return dsf{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ dsf operator+(dsf x, dsf y) {
+  dsf s = ds_two_sum(x.hi, y.hi);
+  const dsf t = ds_two_sum(x.lo, y.lo);
+  s = ds_quick(s.hi, __fadd_rn(s.lo, t.hi));
+  return ds_quick(s.hi, __fadd_rn(s.lo, t.lo));
+}
+__device__ __forceinline__ dsf operator-(dsf x) { return dsf{-x.hi, -x.lo}; }
+__device__ __forceinline__ dsf operator-(dsf x, dsf y) { return x + (-y); }
+__device__ __forceinline__ dsf operator*(dsf x, dsf y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return ds_quick(p, e);
+}
+__device__ __forceinline__ dsf operator*(float f, dsf x) {
+  const float p = __fmul_rn(x.hi, f);
+  return ds_quick(p, __fmaf_rn(x.lo, f, __fmaf_rn(x.hi, f, -p)));
+}
+__device__ __forceinline__ dsf ds_div(dsf x, dsf y) {
+  const float q1 = __fdiv_rn(x.hi, y.hi);
+  const dsf r = x - q1 * y;
+  const float q2 = __fdiv_rn(r.hi, y.hi);
+  const dsf r2 = r - q2 * y;
+  return ds_quick(q1, q2) + ds_make(__fdiv_rn(r2.hi, y.hi));
+}
+__device__ __forceinline__ dsf ds_sqrt(dsf x) {
+  if (!(x.hi > 0.0f)) return ds_make(x.hi == 0.0f ? 0.0f : __int_as_float(0x7fc00000));
+  const float sq = __fsqrt_rn(x.hi);
+  const dsf r = x - ds_make(sq) * ds_make(sq);
+  return ds_quick(sq, __fdiv_rn(r.hi, __fmul_rn(2.0f, sq)));
+}
+
+// The operations of the wide (precision mode) update for double and double-float.
+__device__ __forceinline__ double w_make(double a, double) { return a; }
+__device__ __forceinline__ dsf w_make(double a, dsf) { return ds_make(a); }
+__device__ __forceinline__ double w_min(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ dsf w_min(dsf a, dsf b) {  // fmin: a NaN operand is ignored
+  if (b.hi != b.hi) return a;
+  if (a.hi != a.hi) return b;
+  return (a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo)) ? a : b;
+}
+__device__ __forceinline__ double w_sqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ dsf w_sqrt(dsf a) { return ds_sqrt(a); }
+__device__ __forceinline__ double w_recip(double a) { return 1.0 / a; }
+__device__ __forceinline__ dsf w_recip(dsf a) { return ds_div(ds_make(1.0f), a); }
+__device__ __forceinline__ bool w_ge0(double a) { return a >= 0.0; }
+__device__ __forceinline__ bool w_ge0(dsf a) { return a.hi > 0.0f || (a.hi == 0.0f && a.lo >= 0.0f); }
+__device__ __forceinline__ bool w_in01(double a) { return a >= 0 && a <= 1; }
+__device__ __forceinline__ bool w_in01(dsf a) {
+  return w_ge0(a) && (a.hi < 1.0f || (a.hi == 1.0f && a.lo <= 0.0f));
+}
+__device__ __forceinline__ bool w_large(double a) { return a >= (double)kLarge3DDev; }
+__device__ __forceinline__ bool w_large(dsf a) { return a.hi >= kLarge3DDev; }
+__device__ __forceinline__ float w_float(double a) { return (float)a; }
+__device__ __forceinline__ float w_float(dsf a) { return __fadd_rn(a.hi, a.lo); }
+
+// Square root of a non-negative candidate distance for the wide update: the
+// argument is formed in the wide type (where the cancellation is), the root taken in
+// FP32 (relative error below 1e-7, far inside the scheme's 1e-5 tolerance), which
 // spares the slow FP64 unit.
 __device__ __forceinline__ double sqrt_pos(double x) { return (double)sqrtf((float)x); }
+__device__ __forceinline__ dsf sqrt_pos(dsf x) { return ds_make(sqrtf(w_float(x))); }
 
-// The same tet update carried out in FP64 (precision mode: slots of sliver or
-// ill-conditioned tets).  Same candidates and order as tet_update; the metric
-// edge products come from FP64 setup values, quotients are FP64 (one reciprocal
-// per candidate face); only the candidate roots use sqrt_pos.
-__device__ __forceinline__ double tet_update_f64(double TA, double TB, double TC, double ACAC, double ACBC,
-                                                 double ACCD, double BCBC, double BCCD, double CDCD) {
-  const double L = (double)kLarge3DDev;
-  if (TA >= L && TB >= L && TC >= L) return L;
-  double p, q, r, l1, l2, l3, delta, TE;
-  double fBC = L, fAB = L, fAC = L, TD = L;
-  const double TAC = TC - TA, TBC = TC - TB, TAB = TB - TA;
+// The same tet update carried out in a wide type R (precision mode: slots of sliver
+// or ill-conditioned tets): FP64, or double-float.  Same candidates and order as
+// tet_update; the metric edge products come from FP64 setup values, quotients are
+// wide (one reciprocal per candidate face); only the candidate roots use sqrt_pos.
+template <typename R>
+__device__ __forceinline__ R tet_update_wide(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD, R BCBC, R BCCD, R CDCD) {
+  const R L = w_make((double)kLarge3DDev, R{});
+  if (w_large(TA) && w_large(TB) && w_large(TC)) return L;
+  const R one = w_make(1.0, R{}), eps8 = w_make(0.00000001, R{});
+  R p, q, r, l1, l2, l3, delta, TE;
+  R fBC = L, fAB = L, fAC = L, TD = L;
+  const R TAC = TC - TA, TBC = TC - TB, TAB = TB - TA;
   // face BC
   p = BCBC * TBC * TBC - BCBC * BCBC;
-  q = (BCCD + BCCD) * TBC * TBC - 2 * BCBC * BCCD;
+  q = (BCCD + BCCD) * TBC * TBC - 2.0f * BCBC * BCCD;
   r = TBC * TBC * CDCD - BCCD * BCCD;
-  delta = q * q - 4 * p * r;
-  if (delta >= 0.0) {
-    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p);
+  delta = q * q - 4.0f * p * r;
+  if (w_ge0(delta)) {
+    const R sd = w_sqrt(delta), i2p = w_recip(2.0f * p);
     for (int sg = 0; sg < 2; ++sg) {
       l2 = (-q + (sg ? -sd : sd)) * i2p;
-      l3 = 1.0 - l2;
-      if (l2 >= 0 && l2 <= 1) {
+      l3 = one - l2;
+      if (w_in01(l2)) {
         TE = TB * l2 + TC * l3;
-        fBC = fmin(fBC, TE + sqrt_pos((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD)));
+        fBC = w_min(fBC, TE + sqrt_pos((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD)));
       }
     }
   }
-  fBC = fmin(fBC, fmin(TB + sqrt_pos((BCBC + BCCD) + (BCCD + CDCD)), TC + sqrt_pos(CDCD)));
+  fBC = w_min(fBC, w_min(TB + sqrt_pos((BCBC + BCCD) + (BCCD + CDCD)), TC + sqrt_pos(CDCD)));
   // face AB
-  const double gx = ACAC - ACBC, gy = ACBC - BCBC, gz = ACCD - BCCD;
-  p = (TAB * TAB * ACAC - gx * gx) + (BCBC * TAB * TAB - gy * gy) - ((ACBC + ACBC) * TAB * TAB - 2 * gx * gy);
-  q = -(BCBC * TAB * TAB - gy * gy) * 2 + ((ACBC + ACBC) * TAB * TAB - 2 * gx * gy) +
-      ((ACCD + ACCD) * TAB * TAB - 2 * gx * gz) - ((BCCD + BCCD) * TAB * TAB - 2 * gy * gz);
-  r = (TAB * TAB * BCBC - gy * gy) + ((BCCD + BCCD) * TAB * TAB - 2 * gy * gz) + (TAB * TAB * CDCD - gz * gz);
-  delta = q * q - 4 * p * r;
-  if (delta >= 0.0) {
-    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p);
+  const R gx = ACAC - ACBC, gy = ACBC - BCBC, gz = ACCD - BCCD;
+  p = (TAB * TAB * ACAC - gx * gx) + (BCBC * TAB * TAB - gy * gy) - ((ACBC + ACBC) * TAB * TAB - 2.0f * gx * gy);
+  q = -(BCBC * TAB * TAB - gy * gy) * w_make(2.0, R{}) + ((ACBC + ACBC) * TAB * TAB - 2.0f * gx * gy) +
+      ((ACCD + ACCD) * TAB * TAB - 2.0f * gx * gz) - ((BCCD + BCCD) * TAB * TAB - 2.0f * gy * gz);
+  r = (TAB * TAB * BCBC - gy * gy) + ((BCCD + BCCD) * TAB * TAB - 2.0f * gy * gz) + (TAB * TAB * CDCD - gz * gz);
+  delta = q * q - 4.0f * p * r;
+  if (w_ge0(delta)) {
+    const R sd = w_sqrt(delta), i2p = w_recip(2.0f * p);
     for (int sg = 0; sg < 2; ++sg) {
       l1 = (-q + (sg ? -sd : sd)) * i2p;
-      l2 = 1 - l1;
-      if (l1 >= 0 && l1 <= 1) {
+      l2 = one - l1;
+      if (w_in01(l1)) {
         TE = TA * l1 + TB * l2;
-        fAB = fmin(fAB, TE + sqrt_pos((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                                  (l1 * ACCD + l2 * BCCD + CDCD)));
+        fAB = w_min(fAB, TE + sqrt_pos((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                                       (l1 * ACCD + l2 * BCCD + CDCD)));
       }
     }
   }
-  fAB = fmin(fAB, fmin(TB + sqrt_pos((BCBC + BCCD) + (BCCD + CDCD)), TA + sqrt_pos((ACAC + ACCD) + (ACCD + CDCD))));
+  fAB = w_min(fAB, w_min(TB + sqrt_pos((BCBC + BCCD) + (BCCD + CDCD)), TA + sqrt_pos((ACAC + ACCD) + (ACCD + CDCD))));
   // face AC
   p = ACAC * TAC * TAC - ACAC * ACAC;
-  q = (ACCD + ACCD) * TAC * TAC - 2 * ACAC * ACCD;
+  q = (ACCD + ACCD) * TAC * TAC - 2.0f * ACAC * ACCD;
   r = TAC * TAC * CDCD - ACCD * ACCD;
-  delta = q * q - 4 * p * r;
-  if (delta >= 0.0) {
-    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p);
+  delta = q * q - 4.0f * p * r;
+  if (w_ge0(delta)) {
+    const R sd = w_sqrt(delta), i2p = w_recip(2.0f * p);
     for (int sg = 0; sg < 2; ++sg) {
       l1 = (-q + (sg ? -sd : sd)) * i2p;
-      l3 = 1 - l1;
-      if (l1 >= 0 && l1 <= 1) {
+      l3 = one - l1;
+      if (w_in01(l1)) {
         TE = TA * l1 + TC * l3;
-        fAC = fmin(fAC, TE + sqrt_pos((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD)));
+        fAC = w_min(fAC, TE + sqrt_pos((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD)));
       }
     }
   }
-  fAC = fmin(fAC, fmin(TA + sqrt_pos((ACAC + ACCD) + (ACCD + CDCD)), TC + sqrt_pos(CDCD)));
+  fAC = w_min(fAC, w_min(TA + sqrt_pos((ACAC + ACCD) + (ACCD + CDCD)), TC + sqrt_pos(CDCD)));
   // inside face ABC
-  const double s = TAC * ACBC - TBC * ACAC;
-  const double t = TAC * BCCD - TBC * ACCD;
-  const double h = -(TAC * BCBC - TBC * ACBC);
+  const R s = TAC * ACBC - TBC * ACAC;
+  const R t = TAC * BCCD - TBC * ACCD;
+  const R h = -(TAC * BCBC - TBC * ACBC);
   p = (TAC * TAC * ACAC - ACAC * ACAC) * h * h + (BCBC * TAC * TAC - ACBC * ACBC) * s * s +
-      ((ACBC + ACBC) * TAC * TAC - 2 * ACAC * ACBC) * s * h;
-  q = (BCBC * TAC * TAC - ACBC * ACBC) * 2 * s * t + ((ACBC + ACBC) * TAC * TAC - 2 * ACAC * ACBC) * t * h +
-      ((ACCD + ACCD) * TAC * TAC - 2 * ACAC * ACCD) * h * h +
-      ((BCCD + BCCD) * TAC * TAC - 2 * ACBC * ACCD) * s * h;
-  r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - 2 * ACBC * ACCD) * t * h +
+      ((ACBC + ACBC) * TAC * TAC - 2.0f * ACAC * ACBC) * s * h;
+  q = (BCBC * TAC * TAC - ACBC * ACBC) * w_make(2.0, R{}) * s * t +
+      ((ACBC + ACBC) * TAC * TAC - 2.0f * ACAC * ACBC) * t * h +
+      ((ACCD + ACCD) * TAC * TAC - 2.0f * ACAC * ACCD) * h * h +
+      ((BCCD + BCCD) * TAC * TAC - 2.0f * ACBC * ACCD) * s * h;
+  r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - 2.0f * ACBC * ACCD) * t * h +
       (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
-  delta = q * q - 4 * p * r;
-  if (delta >= 0.0) {
-    const double sd = sqrt(delta), i2p = 1.0 / (2.0 * p), ih = 1.0 / (h + 0.00000001);
+  delta = q * q - 4.0f * p * r;
+  if (w_ge0(delta)) {
+    const R sd = w_sqrt(delta), i2p = w_recip(2.0f * p), ih = w_recip(h + eps8);
     for (int sg = 0; sg < 2; ++sg) {
       l1 = (-q + (sg ? -sd : sd)) * i2p;
       l2 = (s * l1 + t) * ih;
-      l3 = 1 - l1 - l2;
-      if (l1 >= 0 && l1 <= 1 && l2 >= 0 && l2 <= 1 && l3 >= 0 && l3 <= 1) {
+      l3 = one - l1 - l2;
+      if (w_in01(l1) && w_in01(l2) && w_in01(l3)) {
         TE = TA * l1 + TB * l2 + TC * l3;
-        TD = fmin(TD, TE + sqrt_pos((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                                (l1 * ACCD + l2 * BCCD + CDCD)));
+        TD = w_min(TD, TE + sqrt_pos((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                                     (l1 * ACCD + l2 * BCCD + CDCD)));
       }
     }
   }
-  return fmin(TD, fmin(fBC, fmin(fAB, fAC)));
+  return w_min(TD, w_min(fBC, w_min(fAB, fAC)));
+}
+__device__ __forceinline__ double tet_update_f64(double TA, double TB, double TC, double ACAC, double ACBC,
+                                                 double ACCD, double BCBC, double BCCD, double CDCD) {
+  return tet_update_wide<double>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD);
 }
 
 // Triangle update of corner C from A and B; F is the inverse speed.  Uses the
