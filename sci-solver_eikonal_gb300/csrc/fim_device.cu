@@ -168,11 +168,7 @@ __device__ __forceinline__ float settle_eps(float T, int polish) {
 }
 constexpr float kEps2D = 1e-5f;
 constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
-#if EIK_PREC_DS
-typedef dsf PrecWide;
-#else
-typedef double PrecWide;
-#endif
+typedef double PrecWide;  // precision mode's wide updates
 // whether the driver accepted programmatic edges in a conditional loop body
 bool g_pdl_ok = true;
 constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::ktime)
@@ -182,10 +178,6 @@ constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::kt
 // active blocks below which the 3D sweep runs as 1024-thread CTAs (0: never)
 #ifndef EIK_SWEEP_SPLIT
 #define EIK_SWEEP_SPLIT 0
-#endif
-// precision mode's wide updates: double-float (1) or FP64 (0)
-#ifndef EIK_PREC_DS
-#define EIK_PREC_DS 0
 #endif
 #ifndef EIK_MEMO_PREFETCH
 #define EIK_MEMO_PREFETCH 0

@@ -715,95 +715,28 @@ __device__ __forceinline__ float apex_update(const float T[4], const TetGram& g)
   return kLarge3DDev;
 }
 
-// Double-float numbers (precision mode, EIK_PREC_DS): an unevaluated sum hi + lo of
-// two floats, |lo| <= ulp(hi) / 2, with about 48 bits of significand, built from
-// error-free transformations (Knuth's two-sum, the FMA two-product; Dekker 1971,
-// Hida, Li and Bailey 2001).  GB300's FP64 rate is 1/64 of FP32: a double-float
-// operation costs a handful of FP32 ones.
-struct dsf {
-  float hi, lo;
-};
-__device__ __forceinline__ dsf ds_make(float a) { return dsf{a, 0.0f}; }
-__device__ __forceinline__ dsf ds_make(double a) {
-  const float h = (float)a;
-  return dsf{h, (float)(a - (double)h)};
-}
-__device__ __forceinline__ dsf ds_quick(float a, float b) {  // |a| >= |b|
-  const float s = __fadd_rn(a, b);
-  return dsf{s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ dsf ds_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
-  return dsf{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
-}
-__device__ __forceinline__ dsf operator+(dsf x, dsf y) {
-  dsf s = ds_two_sum(x.hi, y.hi);
-  const dsf t = ds_two_sum(x.lo, y.lo);
-  s = ds_quick(s.hi, __fadd_rn(s.lo, t.hi));
-  return ds_quick(s.hi, __fadd_rn(s.lo, t.lo));
-}
-__device__ __forceinline__ dsf operator-(dsf x) { return dsf{-x.hi, -x.lo}; }
-__device__ __forceinline__ dsf operator-(dsf x, dsf y) { return x + (-y); }
-__device__ __forceinline__ dsf operator*(dsf x, dsf y) {
-  const float p = __fmul_rn(x.hi, y.hi);
-  float e = __fmaf_rn(x.hi, y.hi, -p);
-  e = __fmaf_rn(x.hi, y.lo, e);
-  e = __fmaf_rn(x.lo, y.hi, e);
-  return ds_quick(p, e);
-}
-__device__ __forceinline__ dsf operator*(float f, dsf x) {
-  const float p = __fmul_rn(x.hi, f);
-  return ds_quick(p, __fmaf_rn(x.lo, f, __fmaf_rn(x.hi, f, -p)));
-}
-__device__ __forceinline__ dsf ds_div(dsf x, dsf y) {
-  const float q1 = __fdiv_rn(x.hi, y.hi);
-  const dsf r = x - q1 * y;
-  const float q2 = __fdiv_rn(r.hi, y.hi);
-  const dsf r2 = r - q2 * y;
-  return ds_quick(q1, q2) + ds_make(__fdiv_rn(r2.hi, y.hi));
-}
-__device__ __forceinline__ dsf ds_sqrt(dsf x) {
-  if (!(x.hi > 0.0f)) return ds_make(x.hi == 0.0f ? 0.0f : __int_as_float(0x7fc00000));
-  const float sq = __fsqrt_rn(x.hi);
-  const dsf r = x - ds_make(sq) * ds_make(sq);
-  return ds_quick(sq, __fdiv_rn(r.hi, __fmul_rn(2.0f, sq)));
-}
-
-// The operations of the wide (precision mode) update for double and double-float.
+// The operations of the wide (precision mode) update, named so the update reads
+// like the FP32 one.
 __device__ __forceinline__ double w_make(double a, double) { return a; }
-__device__ __forceinline__ dsf w_make(double a, dsf) { return ds_make(a); }
 __device__ __forceinline__ double w_min(double a, double b) { return fmin(a, b); }
-__device__ __forceinline__ dsf w_min(dsf a, dsf b) {  // fmin: a NaN operand is ignored
-  if (b.hi != b.hi) return a;
-  if (a.hi != a.hi) return b;
-  return (a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo)) ? a : b;
-}
 __device__ __forceinline__ double w_sqrt(double a) { return sqrt(a); }
-__device__ __forceinline__ dsf w_sqrt(dsf a) { return ds_sqrt(a); }
 __device__ __forceinline__ double w_recip(double a) { return 1.0 / a; }
-__device__ __forceinline__ dsf w_recip(dsf a) { return ds_div(ds_make(1.0f), a); }
 __device__ __forceinline__ bool w_ge0(double a) { return a >= 0.0; }
-__device__ __forceinline__ bool w_ge0(dsf a) { return a.hi > 0.0f || (a.hi == 0.0f && a.lo >= 0.0f); }
 __device__ __forceinline__ bool w_in01(double a) { return a >= 0 && a <= 1; }
-__device__ __forceinline__ bool w_in01(dsf a) {
-  return w_ge0(a) && (a.hi < 1.0f || (a.hi == 1.0f && a.lo <= 0.0f));
-}
 __device__ __forceinline__ bool w_large(double a) { return a >= (double)kLarge3DDev; }
-__device__ __forceinline__ bool w_large(dsf a) { return a.hi >= kLarge3DDev; }
 __device__ __forceinline__ float w_float(double a) { return (float)a; }
-__device__ __forceinline__ float w_float(dsf a) { return __fadd_rn(a.hi, a.lo); }
 
-// Square root of a non-negative candidate distance for the wide update: the
-// argument is formed in the wide type (where the cancellation is), the root taken in
-// FP32 (relative error below 1e-7, far inside the scheme's 1e-5 tolerance), which
+// Square root of a non-negative candidate distance for the FP64 update: the
+// argument is formed in FP64 (where the cancellation is), the root taken in FP32 (relative error below 1e-7, far inside the scheme's 1e-5 tolerance), which
 // spares the slow FP64 unit.
 __device__ __forceinline__ double sqrt_pos(double x) { return (double)sqrtf((float)x); }
-__device__ __forceinline__ dsf sqrt_pos(dsf x) { return ds_make(sqrtf(w_float(x))); }
 
-// The same tet update carried out in a wide type R (precision mode: slots of sliver
-// or ill-conditioned tets): FP64, or double-float.  Same candidates and order as
-// tet_update; the metric edge products come from FP64 setup values, quotients are
-// wide (one reciprocal per candidate face); only the candidate roots use sqrt_pos.
+// The same tet update carried out in FP64 (precision mode: slots of sliver or
+// ill-conditioned tets), written over a type R for the helpers above.  Same
+// candidates and order as tet_update; the metric edge products come from FP64 setup
+// values, quotients are FP64 (one reciprocal per candidate face); only the candidate
+// roots use sqrt_pos.  (A double-float R, two FP32 numbers per value, ran slower on
+// GB300 than the FP64 unit and was dropped.)
 template <typename R>
 __device__ __forceinline__ R tet_update_wide(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD, R BCBC, R BCCD, R CDCD) {
   const R L = w_make((double)kLarge3DDev, R{});
