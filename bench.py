@@ -806,7 +806,13 @@ def main():
                                        "kernel; cold caches), set beside this run's algorithmic bytes of the same "
                                        "iterations",
                      "note": "the sweep kernel is bound by CTA barriers and instruction latency in the tet local "
-                             "solver, not by HBM"},
+                             "solver, not by HBM",
+                     # compute side, from the committed full capture of one sweep launch (outer
+                     # iteration 40 of the same solve, kernel-by-kernel mode)
+                     "compute": {"bound": "issue", "issue_active_pct": 53.9, "ipc_per_sm": 2.13,
+                                 "fma_pipe_pct": 17.1, "alu_pipe_pct": 33.7, "xu_pipe_pct": 8.1,
+                                 "top_stall": "barrier",
+                                 "source": "profiles/fim3d_items_c3d.md (ncu --set full, one k_sweep3d launch)"}},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times),
                 "note": "each step re-solves the resident mesh through the C ABI: seeds copied in, the solve, the "

@@ -2,37 +2,39 @@
 // the block-partitioned Fast Iterative Method.
 //
 // Reference mapping (paths inside SCI-Solver_Eikonal):
-//   k_visit3d<false>  FIMCuda           src/core3d/cuda/CUDA_kernels.cu:383-489   (2 sweeps)
+//   k_sweep3d         FIMCuda           src/core3d/cuda/CUDA_kernels.cu:383-489   (2 sweeps, apex items)
+//   k_check3d         run_check_neghbor CUDA_kernels.cu:493-602                    (1 sweep, flags only)
+//   k_visit3d<false>  FIMCuda, slot per thread (blocks too large for the item kernels'
+//                     shared memory, and precision mode)
+//   k_visit3d<true>   run_check_neghbor, slot per thread (the same cases)
 //   k_commit3d        CopyOutBack + host activation, meshFIM3dEikonal.cu:438-488, CUDA_kernels.cu:604-668
-//   k_visit3d<true>   run_check_neghbor CUDA_kernels.cu:493-602                    (1 sweep, flags only)
-//   k_visit2d<false>  FIMCuda           src/core2d/cuda/CUDA_kernels.cu:36-409    (7 sweeps)
+//   k_visit2d_slot / k_visit2d <false>  FIMCuda  src/core2d/cuda/CUDA_kernels.cu:36-409  (7 sweeps)
+//   k_visit2d_slot / k_visit2d <true>   run_check_neighbor CUDA_kernels.cu:415-799    (1 sweep, writes values)
 //   k_activate2d      host activation   src/core2d/cuda/meshFIM2d_eikonal.cu:734-756
-//   k_visit2d<true>   run_check_neighbor CUDA_kernels.cu:415-799                   (1 sweep, writes values)
 //   k_vertex_test2d   all-vertex convergence test, meshFIM2d_eikonal.cu:801-815
 //   k_close3d         end of the 3D host loop iteration, meshFIM3dEikonal.cu:411-417
 //   run_reduction (both dims) is a __syncthreads_and inside the visit kernels.
 //
 // Design (GB300-first, not a translation):
-//   * One CTA visits one block at a time and pulls blocks from a device work
-//     counter; grids are sized by occupancy x 152 SMs and stay fixed so the whole
-//     iteration is a CUDA-graph body.  A conditional while-node repeats the body
-//     (four iterations a pass outside the server) until no block is active: no
-//     host round trip per iteration.
-//   * A block's metric terms and corner ids are contiguous in HBM (block-major
-//     slots, SoA coefficient runs, 16-byte aligned) and arrive in shared memory by
-//     two cp.async.bulk copies completing on an mbarrier, while the threads gather
-//     owned and halo travel times.
+//   * One CTA visits one block at a time: its own index first, then blocks from a
+//     device counter; grids are sized by occupancy x 152 SMs and stay fixed so the
+//     whole iteration is a CUDA-graph body.  A conditional while-node repeats the
+//     body (four iterations a pass outside the server) until no block is active:
+//     no host round trip per iteration.  Consecutive kernels of the body are joined
+//     by programmatic dependencies.
+//   * A block's metric terms, corner ids, memos and apex bounds are contiguous in
+//     HBM (block-major slots, SoA runs, 16-byte aligned) and arrive in shared memory
+//     by bulk copies completing on an mbarrier, while the threads gather owned and
+//     halo travel times.
 //   * Travel times live once per vertex in HBM (block-contiguous renumbering).
 //     Owned vertices keep one shared-memory copy per visit; every slot corner that
 //     belongs to another block keeps its own per-slot copy, as the reference's
 //     per-slot storage does, and the per-vertex minimum is a shared-memory atomic.
-//   * Sweeps after the first recompute a slot only when one of its values changed
-//     in the previous sweep; unchanged inputs reproduce the previous candidates
-//     bit for bit, so skipping them cannot change any result.  The last sweep of a
-//     3D visit runs only slots that can still lower an owned vertex, from a packed
-//     list, and 3D checks skip slots whose inputs an earlier check found settled.
-//   * 3D visit CTAs are 512 threads (two per SM, overlapping two visits) or one
-//     thread per slot, whichever a handle's first solves measure faster.
+//   * The tet update is explicitly rounded with the reference kernel's fused
+//     roundings (local_update.cuh), so its bits do not depend on the kernel around
+//     it; the item kernels then run only the apex updates that can change
+//     something (all-far, unchanged-input, memo and plane-distance skips, each
+//     exact) in 384-thread CTAs, three per SM.
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
