@@ -181,9 +181,6 @@ constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::kt
 #ifndef EIK_SWEEP_SPLIT
 #define EIK_SWEEP_SPLIT 0
 #endif
-#ifndef EIK_MEMO_PREFETCH
-#define EIK_MEMO_PREFETCH 0
-#endif
 #ifndef EIK_SWEEP_MEMO
 #define EIK_SWEEP_MEMO 1
 #endif
@@ -919,12 +916,6 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
       continue;
     }
     SmemItems s = s0;
-#if EIK_MEMO_PREFETCH
-    // the first sweep reads every slot's memo: start those loads with the block's
-    if (a.fim_memo)
-      for (int j = tid * 8; j < bd.nslots; j += NT * 8)
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(a.fim_memo + bd.slot_begin + j));
-#endif
     if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, nullptr, a.hsb ? s.hs : nullptr)) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);
