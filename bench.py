@@ -415,14 +415,31 @@ def check_bytes(it):
     return 56 * it[7] + 4 * (it[9] + it[8]) + 4 * it[6]
 
 
-def traffic_vs_algorithmic(its, profile):
+def launch_bytes(its, fused):
+    """Algorithmic bytes of every sweep launch and every check launch of one solve,
+    by outer iteration.  With the checks inside the sweep kernel (fused), the sweep
+    launch of iteration k also runs the checks of iteration k - 1 (row k - 1's check
+    columns) and there is no check launch; a block that its check activated is
+    swept in the same visit, so its metric terms, ids and bounds (40 B per slot) and
+    its owned + halo times are read once (columns 12-15 count those visits)."""
+    n = len(its)
+    sweep = [sweep_bytes(its[i]) for i in range(n)]
+    check = [check_bytes(its[i]) for i in range(n)]
+    if fused:
+        once = [40 * its[i][13] + 4 * (its[i][14] + its[i][15]) if len(its[i]) > 15 else 0 for i in range(n)]
+        return [sweep[i] + (check[i - 1] if i > 0 else 0) - once[i] for i in range(n)], [0] * n
+    return sweep, check
+
+
+def traffic_vs_algorithmic(its, profile, fused):
     """Mean DRAM bytes per launch from the capture beside the mean algorithmic bytes
     of the same launches (same iterations of the same deterministic solve) in this
     run, for the sweep and the check kernel."""
     rows = launch_dram(profile)
     out = {}
-    for k, (col, fn, name) in enumerate(((0, sweep_bytes, "sweep"), (1, check_bytes, "check"))):
-        alg = [fn(its[i]) for i in range(len(its))]
+    per_launch = launch_bytes(its, fused)
+    for k, (col, name) in enumerate(((0, "sweep"), (1, "check"))):
+        alg = per_launch[k]
         if rows:
             common = [i for i in sorted(rows) if i < len(its) and rows[i][col] > 0]
             if common:
@@ -740,10 +757,13 @@ def main():
         fim_ms += st["fim_kernel_ms"]
         chk_ms += st["check_kernel_ms"]
         its = e.iterationStats()
-        fim_bytes += sum(sweep_bytes(it) for it in its)
+        # the checks run inside the sweep kernel: no check launches, check visits counted
+        fused = st["check_launches"] == 0 and st["check_visits"] > 0
+        fim_bytes += sum(launch_bytes(its, fused)[0])
         iters.append(st["iterations"])
-        # start + 4 kernels per iteration, the graph body running 4 iterations a pass
-        launches += 1 + 4 * 4 * ((st["iterations"] + 3) // 4)
+        # start + 3 kernels (sweep with checks, commit, close) or 4 per iteration, the
+        # graph body running 4 iterations a pass (loop iterations = sweep launches)
+        launches += 1 + (3 if fused else 4) * 4 * ((st["fim_launches"] + 3) // 4)
     barrier()
     clocks = sampler.stop()
     total_ms, upd_all = aggregate_replicas(torch, sum(times), upd, world, "cuda")
@@ -778,7 +798,7 @@ def main():
     else:
         peak, peak_src = 6800.0, "fallback"
     achieved = fim_bytes / (fim_ms * 1e-3) / 1e9 if fim_ms > 0 else 0.0
-    tva = traffic_vs_algorithmic(its, DRAM_PROFILE)
+    tva = traffic_vs_algorithmic(its, DRAM_PROFILE, fused)
     lat = sorted(times)
     res = {
         "metric": METRIC, "value": value, "unit": "vertex-updates/s", "n_gpus": world, "steps": args.steps,
@@ -796,11 +816,12 @@ def main():
                                   "process whose kernels are loaded"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": tva["sweep"]["traffic"], "peak_source": peak_src,
-                     "kernel": "k_sweep3d (block sweeps)",
+                     "kernel": ("k_sweep3d (block sweeps and the previous iteration's neighbour checks)"
+                                if fused else "k_sweep3d (block sweeps)"),
                      "kernel_ms_per_step": fim_ms / args.steps,
                      "algorithmic_bytes_per_launch": tva["sweep"]["algorithmic"],
                      "traffic_over_algorithmic": tva["sweep"]["traffic_over_algorithmic"],
-                     "check_kernel": dict(tva["check"], kernel_ms_per_step=chk_ms / args.steps),
+                     "check_kernel": (None if fused else dict(tva["check"], kernel_ms_per_step=chk_ms / args.steps)),
                      "traffic_source": f"profiles/{DRAM_PROFILE}: ncu dram__bytes_read.sum + dram__bytes_write.sum "
                                        "of every sweep and check launch of one solve of this workload (kernel by "
                                        "kernel; cold caches), set beside this run's algorithmic bytes of the same "

@@ -101,8 +101,9 @@ typedef struct eik_stats {
   int device_error;          /* device error flags of the last solve */
   /* per-kernel figures of the last solve, from a device timer around every launch */
   float fim_kernel_ms;       /* summed launch spans of the block-sweep kernel */
-  float check_kernel_ms;     /* summed launch spans of the neighbour-check kernel */
-  int fim_launches, check_launches;
+  float check_kernel_ms;     /* summed launch spans of the neighbour-check kernel (0 where the
+                                3D checks run inside the sweep kernel: the item kernels) */
+  int fim_launches, check_launches;  /* launches that visited blocks (check: 0 as above) */
   long long fim_slots, fim_halo, fim_owned; /* inputs streamed by the block-sweep kernel */
   long long h2d_bytes;       /* host-to-device bytes copied by the last solve (initial state) */
   /* precision mode (precision = 1) */
@@ -184,10 +185,15 @@ int eik_get_partition(const eik_solver* h, int* labels, int nv, int* nblocks);
 int eik_get_stats(const eik_solver* h, eik_stats* s);
 /* Per-outer-iteration figures of the last solve (no counterpart in the reference,
  * whose GenerateData only prints totals under verbose, meshFIM3dEikonal.cu:544-548).
- * For iteration i, out[10*i .. 10*i+9] = sweep-kernel launch span (ns, device
+ * For iteration i, out[16*i .. 16*i+15] = sweep-kernel launch span (ns, device
  * timer), check-kernel launch span (ns), then the sweep kernel's block visits,
  * element slots, halo vertices and owned vertices, then the same four for the
- * check kernel.  Writes min(iterations, cap) rows and returns that count (>= 0), or
+ * neighbour checks of iteration i, then the sweep and check kernels' start times
+ * (ns after the first iteration's sweep start; -1 where the kernel recorded none),
+ * then the same four counts for the sweep visits of iteration i whose block was
+ * staged by a check in the same visit.  Where the 3D checks run inside the sweep
+ * kernel (the item kernels), the checks of iteration i run in the sweep launch of
+ * iteration i+1 and there is no check launch (span 0, start -1).  Writes min(iterations, cap) rows and returns that count (>= 0), or
  * a negative status (-EIK_ERR_ARG, -EIK_ERR_STATE before the first solve). */
 int eik_get_iteration_stats(const eik_solver* h, long long* out, int cap);
 /* writeVTK — src/Eikonal.cu:50-60: <prefix><i>.vtk for the last (all=0) or every

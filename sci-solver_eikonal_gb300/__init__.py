@@ -337,14 +337,18 @@ class Eikonal:
         return s.as_dict()
 
     ITERATION_STAT_COLUMNS = ("fim_ns", "check_ns", "fim_visits", "fim_slots", "fim_halo", "fim_owned",
-                              "check_visits", "check_slots", "check_halo", "check_owned")
+                              "check_visits", "check_slots", "check_halo", "check_owned",
+                              "fim_start_ns", "check_start_ns",
+                              "fused_visits", "fused_slots", "fused_halo", "fused_owned")
 
     def iterationStats(self):
         """Per outer iteration of the last solve: launch spans of the sweep and check
-        kernels (ns) and the block visits, slots, halo and owned vertices each kernel
-        processed, as an (iterations, 10) int64 array (ITERATION_STAT_COLUMNS)."""
+        kernels (ns), the block visits, slots, halo and owned vertices of the sweeps
+        and of the neighbour checks, the two kernels' start times (ns after the first
+        sweep start) and the counts of the sweep visits that followed a check in the
+        same visit, as an (iterations, 16) int64 array (ITERATION_STAT_COLUMNS)."""
         n = max(self.numIterations(), 0)
-        out = np.zeros((n, 10), dtype=np.int64)
+        out = np.zeros((n, len(self.ITERATION_STAT_COLUMNS)), dtype=np.int64)
         rc = self._lib.eik_get_iteration_stats(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), n)
         if rc < 0:
             self._check(-rc)

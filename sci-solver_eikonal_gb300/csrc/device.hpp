@@ -20,7 +20,7 @@ typedef struct CUstream_st* cudaStream_t;
 
 namespace eikgb {
 
-constexpr int kIterStatWords = 10;
+constexpr int kIterStatWords = 16;
 
 struct SolveStats {
   int iterations = 0;
@@ -39,7 +39,10 @@ struct SolveStats {
   int fim_launches = 0, check_launches = 0;
   // per outer iteration, kIterStatWords values: sweep-kernel and check-kernel
   // launch spans (ns, device timer), then the sweep kernel's block visits, element
-  // slots, halo vertices and owned vertices, then the same four for the check kernel
+  // slots, halo vertices and owned vertices, then the same four for the check kernel,
+  // then the two kernels' start times (ns after the first iteration's sweep start),
+  // then visits, slots, halo and owned vertices of the sweep visits that followed a
+  // check in the same visit (checks inside the sweep kernel)
   std::vector<long long> iter_stats;
   long long h2d_bytes = 0;       // host-to-device bytes the last solve copied (initial state)
   std::vector<int> inst_iters;   // outer iterations run by every instance

@@ -66,6 +66,13 @@ struct Ctl {
   int stop;       // set when the outer loop must end (read by the direct-launch loop)
   int f64_all;    // precision mode's polish: every slot's update in FP64
   int polish;     // precision mode's polish: blocks settle to a few ulps, not EPS
+  // 3D checks inside the sweep kernel (DevArgs::fused): blocks a check activated
+  // and appended behind the carried-over ones of this iteration's active list, and
+  // per iteration parity the check candidates queued by that iteration's commit
+  int nadd;
+  int ncand[2];
+  int idle_iters;  // trailing iterations that swept no block (their checks only)
+  int last_idle;   // the last iteration swept no block
   unsigned long long updates, fim_visits, chk_visits, slot_visits, halo_visits, owned_visits;
   unsigned long long fim_slots, fim_halo, fim_owned;  // per-visit inputs of the sweep kernel only
 };
@@ -98,7 +105,9 @@ struct DevArgs {
   // per iteration, kKStride words: [~sweep start, sweep end, ~check start, check
   // end] (globaltimer ns; starts stored complemented so the zeroed buffer and
   // atomicMax give the earliest start), then the sweep kernel's visits, slots, halo and owned
-  // vertices, then the same four for the check kernel
+  // vertices, then the same four for the check kernel, then the same four for the
+  // sweep visits whose block arrived with a check in the same visit (checks inside
+  // the sweep kernel)
   unsigned long long* ktime;
   int ktime_cap;
   int fim_sweeps;
@@ -141,6 +150,16 @@ struct DevArgs {
   // products, per slot (k_plane_bounds_u64); null: none
   const uint2* hsu64;
   int sweep_split;  // active blocks from which the large-grid sweep launch runs
+  // 3D item path: the neighbour checks of iteration k run inside the sweep kernel
+  // of iteration k+1 (they read the same committed times), a block that moves being
+  // swept in the same visit.  cand: two lists of nb check candidates (by the parity
+  // of the iteration whose commit queued them); per instance the blocks swept this
+  // iteration and the candidates queued.  inst_done is then 0 running, 1 finished,
+  // 2 at its iteration cap with checks still to run (checked, never swept).
+  int fused;
+  int* cand;
+  int* inst_swept;
+  int* inst_ncand;
 };
 
 constexpr float kEps3DLe = 0x1.4f8b58p-17f;  // largest float below the double 1e-5
@@ -173,7 +192,7 @@ constexpr int kBodyCopies = 4;  // iterations per pass of the graph's loop body
 typedef double PrecWide;  // precision mode's wide updates
 // whether the driver accepted programmatic edges in a conditional loop body
 bool g_pdl_ok = true;
-constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::ktime)
+constexpr int kKStride = 16;    // words of per-iteration telemetry (DevArgs::ktime)
 #ifndef EIK_SWEEP_ITEMS
 #define EIK_SWEEP_ITEMS 1
 #endif
@@ -200,6 +219,11 @@ constexpr int kKStride = 12;    // words of per-iteration telemetry (DevArgs::kt
 #endif
 #ifndef EIK_CHECK_ITEMS
 #define EIK_CHECK_ITEMS 1
+#endif
+// 3D item kernels: the neighbour checks of an iteration run inside the next
+// iteration's sweep launch (1) or as their own launch, k_check3d (0)
+#ifndef EIK_FUSED_CHECK
+#define EIK_FUSED_CHECK 1
 #endif
 
 // ---------------------------------------------------------------------------
@@ -869,11 +893,112 @@ __device__ __forceinline__ SmemItems carve_items(unsigned char* sm, const DevArg
   return s;
 }
 
+// One check visit over a loaded block (run_check_neghbor, CUDA_kernels.cu:493-602):
+// lists the owned apex updates that the check memo (smemo, staged with the block)
+// and the plane bound (shs) do not settle, runs them until one lowers its vertex
+// by more than EPS, and when none does records every slot's input times as
+// settled.  Returns whether the block moved.  Called by all threads of the CTA.
+template <class S>
+__device__ __forceinline__ bool check_pass(const DevArgs& a, const BlockDesc& bd, const S& s, uint4* smemo,
+                                           const uint2* shs, int* s_cnt, volatile int* s_moved) {
+  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
+  const int np = a.max_slots_pad;
+  if (tid == 0) *s_moved = 0;
+  if (tid < 5) s_cnt[tid] = 0;
+  __syncthreads();
+  const int ns = bd.nslots, nown = bd.nowned, pitch = bd.nslots_pad;
+  for (int j0 = 0; j0 < ns; j0 += NT) {
+    const int j = j0 + tid;
+    unsigned need = 0;
+    if (j < ns) {
+      const uint2 l = s.lv[j];
+      const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+      float T[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) T[q] = s.vt[id[q]];
+      bool memo = false;
+      if (smemo) {
+        const uint4 R = smemo[j];
+        memo = R.x == __float_as_uint(T[0]) && R.y == __float_as_uint(T[1]) && R.z == __float_as_uint(T[2]) &&
+               R.w == __float_as_uint(T[3]);
+      }
+      if (!memo) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float m = fminf(fminf(T[(k + 1) & 3], T[(k + 2) & 3]), T[(k + 3) & 3]);
+          const bool run = id[k] < nown && m < kLarge3DDev && !plane_skip(T[k], m, slot_bound(shs, j, k));
+          need |= (run ? 1u : 0u) << k;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const unsigned bal = __ballot_sync(0xffffffffu, (need >> k) & 1u);
+      if (bal) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&s_cnt[k], __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if ((need >> k) & 1u) s.items[k * np + base + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)j;
+      }
+    }
+  }
+  __syncthreads();
+  const int c0 = s_cnt[0], c01 = c0 + s_cnt[1], c012 = c01 + s_cnt[2], total = c012 + s_cnt[3];
+#if EIK_ITEM_STEAL
+  for (;;) {
+    int i0 = 0;
+    if (lane == 0) i0 = *s_moved ? total : atomicAdd(&s_cnt[4], 32);
+    i0 = __shfl_sync(0xffffffffu, i0, 0);
+    if (i0 >= total) break;
+    const int i = i0 + lane;
+    if (i >= total) continue;
+#else
+  for (int i = tid; i < total; i += NT) {
+    if (*s_moved) break;
+#endif
+    const int k = (i < c0) ? 0 : (i < c01) ? 1 : (i < c012) ? 2 : 3;
+    const int r = i - ((k == 0) ? 0 : (k == 1) ? c0 : (k == 2) ? c01 : c012);
+    const int j = s.items[k * np + r];
+    const uint2 l = s.lv[j];
+    const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
+    float T[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) T[q] = s.vt[id[q]];
+    const TetGram gm = tet_gram9(s.coef[0 * pitch + j], s.coef[1 * pitch + j], s.coef[2 * pitch + j],
+                                 s.coef[3 * pitch + j], s.coef[4 * pitch + j], s.coef[5 * pitch + j]);
+    float u;
+    switch (k) {
+      case 0: u = apex_update<0>(T, gm); break;
+      case 1: u = apex_update<1>(T, gm); break;
+      case 2: u = apex_update<2>(T, gm); break;
+      default: u = apex_update<3>(T, gm); break;
+    }
+    const float Tk = (k == 0) ? T[0] : (k == 1) ? T[1] : (k == 2) ? T[2] : T[3];
+    // (double)(old - candidate) >= 1e-5 in the reference
+    if (!((Tk - fminf(Tk, u)) <= kEps3DLe)) *s_moved = 1;
+  }
+  __syncthreads();
+  const int allc = *s_moved ? 0 : 1;
+  if (allc && smemo)
+    for (int j = tid; j < ns; j += NT) {
+      const uint2 l = s.lv[j];
+      const uint4 R = smemo[j];
+      const uint4 W = make_uint4(__float_as_uint(s.vt[l.x & 0xffffu]), __float_as_uint(s.vt[l.x >> 16]),
+                                 __float_as_uint(s.vt[l.y & 0xffffu]), __float_as_uint(s.vt[l.y >> 16]));
+      if (R.x != W.x || R.y != W.y || R.z != W.z || R.w != W.w) a.chk_memo[bd.slot_begin + j] = W;
+    }
+  return allc == 0;
+}
+
 // at most 56 registers: three CTAs of 384 threads fit one SM's register file
 // role: 0 runs every iteration; where the loop body holds two sweep launches of
 // different CTA sizes, 1 runs only iterations with at least a.sweep_split active
 // blocks and 2 only the others (few blocks: a visit's latency, which more threads
-// per block shorten, sets the launch's time)
+// per block shorten, sets the launch's time).
+// With a.fused, the CTAs also claim the check candidates queued by the previous
+// iteration's commit (items nact.. of the claim range): a candidate's check runs
+// on the staged block, and a block that moves is appended to this iteration's
+// active list and swept in the same visit.
 __global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
   pdl_begin();
   if (role != 0 && ((a.ctl->nact >= a.sweep_split) != (role == 1))) return;
@@ -881,14 +1006,18 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int s_item;
   __shared__ int s_cnt[5];  // items per apex kind, then the next unclaimed item
+  __shared__ volatile int s_moved;
   const SmemItems s0 = carve_items(sm, a);
   const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
   const int np = a.max_slots_pad;
-  const Ctl* ctl = a.ctl;
+  Ctl* ctl = a.ctl;
   const int iter = ctl->iter;
   const int stamp = iter + 1;
-  const int count = ctl->nact;
-  const int* list = act_list(a, iter);
+  const int nact = ctl->nact;
+  const int ncand = a.fused ? ctl->ncand[(iter + 1) & 1] : 0;
+  const int* cand = a.fused ? a.cand + (size_t)((iter + 1) & 1) * a.nb : nullptr;
+  const int count = nact + ncand;
+  int* list = act_list(a, iter);
   const int nsweeps = a.fim_sweeps;
   stamp_start(a, iter, 0);
   if (tid == 0) mbar_init(&bar, 1);
@@ -909,14 +1038,20 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
     }
     first_item = -1;
     if (item >= count) break;
-    const int b = list[item];
+    const bool chk = item >= nact;  // a check candidate
+    const int b = chk ? cand[item - nact] : list[item];
     const BlockDesc bd = a.blocks[b];
-    if (done1 >= 0 ? done1 : a.inst_done[a.blk_inst[b]]) {  // instance finished: leave its blocks alone
+    // instance finished: leave its blocks alone; at its cap: its checks only
+    const int ist = done1 >= 0 ? done1 : a.inst_done[a.blk_inst[b]];
+    if (ist == 1 || (ist != 0 && !chk)) {
       __syncthreads();
       continue;
     }
     SmemItems s = s0;
-    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, nullptr, a.hsb ? s.hs : nullptr)) {
+    // a candidate's check memos arrive in the per-slot copy buffer h0, which the
+    // first sweep neither reads nor writes
+    uint4* const smemo = (chk && a.chk_memo) ? reinterpret_cast<uint4*>(s.h0) : nullptr;
+    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo, a.hsb ? s.hs : nullptr)) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);
       __syncthreads();
@@ -924,6 +1059,23 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
     }
     __syncthreads();
     const int ns = bd.nslots, nown = bd.nowned, pitch = bd.nslots_pad;
+    if (chk) {
+      const bool moved = check_pass(a, bd, s, smemo, a.hsb ? s.hs : nullptr, s_cnt, &s_moved);
+      if (tid == 0) {  // the previous iteration's check (run_check_neghbor)
+        atomicAdd(&a.ctl->chk_visits, 1ull);
+        atomicAdd(&a.ctl->updates, (unsigned long long)nown);
+        count_visit(a, iter - 1, 1, ns, bd.nhalo, nown);
+        atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
+        atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
+        atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+        if (moved && ist == 0) list[nact + atomicAdd(&ctl->nadd, 1)] = b;
+      }
+      if (!moved || ist != 0) {
+        __syncthreads();
+        continue;
+      }
+    }
+    const bool fusedv = chk;  // the block arrived with this visit's check
     // per-slot copies of corners owned by other blocks start from the halo values,
     // which stay in vt for the whole visit: the first sweep reads them there, and
     // the second compares its copies with them
@@ -1051,12 +1203,17 @@ __global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
     if (tid == 0) {
       a.conv[b] = allc;
       if (!allc) a.stampA[b] = stamp;
+      if (a.fused) atomicAdd(&a.inst_swept[a.blk_inst[b]], 1);
       atomicAdd(&a.ctl->fim_visits, 1ull);
       atomicAdd(&a.ctl->updates, (unsigned long long)nown * nsweeps);
       count_visit(a, iter, 0, ns, bd.nhalo, nown);
-      atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
-      atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
-      atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+      if (fusedv) {  // streamed once, with the check
+        count_visit(a, iter, 2, ns, bd.nhalo, nown);
+      } else {
+        atomicAdd(&a.ctl->slot_visits, (unsigned long long)ns);
+        atomicAdd(&a.ctl->halo_visits, (unsigned long long)bd.nhalo);
+        atomicAdd(&a.ctl->owned_visits, (unsigned long long)nown);
+      }
       atomicAdd(&a.ctl->fim_slots, (unsigned long long)ns);
       atomicAdd(&a.ctl->fim_halo, (unsigned long long)bd.nhalo);
       atomicAdd(&a.ctl->fim_owned, (unsigned long long)nown);
@@ -1164,90 +1321,8 @@ __global__ void __maxnreg__(56) k_check3d(DevArgs a) {
       __syncthreads();
       continue;
     }
-    if (tid == 0) s_moved = 0;
-    if (tid < 5) s_cnt[tid] = 0;
-    __syncthreads();
-    const int ns = bd.nslots, nown = bd.nowned, pitch = bd.nslots_pad;
-    for (int j0 = 0; j0 < ns; j0 += NT) {
-      const int j = j0 + tid;
-      unsigned need = 0;
-      if (j < ns) {
-        const uint2 l = s.lv[j];
-        const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
-        float T[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) T[q] = s.vt[id[q]];
-        bool memo = false;
-        if (smemo) {
-          const uint4 R = smemo[j];
-          memo = R.x == __float_as_uint(T[0]) && R.y == __float_as_uint(T[1]) && R.z == __float_as_uint(T[2]) &&
-                 R.w == __float_as_uint(T[3]);
-        }
-        if (!memo) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const float m = fminf(fminf(T[(k + 1) & 3], T[(k + 2) & 3]), T[(k + 3) & 3]);
-            const bool run = id[k] < nown && m < kLarge3DDev && !plane_skip(T[k], m, slot_bound(shs, j, k));
-            need |= (run ? 1u : 0u) << k;
-          }
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const unsigned bal = __ballot_sync(0xffffffffu, (need >> k) & 1u);
-        if (bal) {
-          int base = 0;
-          if (lane == 0) base = atomicAdd(&s_cnt[k], __popc(bal));
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if ((need >> k) & 1u) s.items[k * np + base + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)j;
-        }
-      }
-    }
-    __syncthreads();
-    const int c0 = s_cnt[0], c01 = c0 + s_cnt[1], c012 = c01 + s_cnt[2], total = c012 + s_cnt[3];
-#if EIK_ITEM_STEAL
-    for (;;) {
-      int i0 = 0;
-      if (lane == 0) i0 = s_moved ? total : atomicAdd(&s_cnt[4], 32);
-      i0 = __shfl_sync(0xffffffffu, i0, 0);
-      if (i0 >= total) break;
-      const int i = i0 + lane;
-      if (i >= total) continue;
-#else
-    for (int i = tid; i < total; i += NT) {
-      if (s_moved) break;
-#endif
-      const int k = (i < c0) ? 0 : (i < c01) ? 1 : (i < c012) ? 2 : 3;
-      const int r = i - ((k == 0) ? 0 : (k == 1) ? c0 : (k == 2) ? c01 : c012);
-      const int j = s.items[k * np + r];
-      const uint2 l = s.lv[j];
-      const int id[4] = {(int)(l.x & 0xffffu), (int)(l.x >> 16), (int)(l.y & 0xffffu), (int)(l.y >> 16)};
-      float T[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) T[q] = s.vt[id[q]];
-      const TetGram gm = tet_gram9(s.coef[0 * pitch + j], s.coef[1 * pitch + j], s.coef[2 * pitch + j],
-                                   s.coef[3 * pitch + j], s.coef[4 * pitch + j], s.coef[5 * pitch + j]);
-      float u;
-      switch (k) {
-        case 0: u = apex_update<0>(T, gm); break;
-        case 1: u = apex_update<1>(T, gm); break;
-        case 2: u = apex_update<2>(T, gm); break;
-        default: u = apex_update<3>(T, gm); break;
-      }
-      const float Tk = (k == 0) ? T[0] : (k == 1) ? T[1] : (k == 2) ? T[2] : T[3];
-      // (double)(old - candidate) >= 1e-5 in the reference
-      if (!((Tk - fminf(Tk, u)) <= kEps3DLe)) s_moved = 1;
-    }
-    __syncthreads();
-    const int allc = s_moved ? 0 : 1;
-    if (allc && smemo)
-      for (int j = tid; j < ns; j += NT) {
-        const uint2 l = s.lv[j];
-        const uint4 R = smemo[j];
-        const uint4 W = make_uint4(__float_as_uint(s.vt[l.x & 0xffffu]), __float_as_uint(s.vt[l.x >> 16]),
-                                   __float_as_uint(s.vt[l.y & 0xffffu]), __float_as_uint(s.vt[l.y >> 16]));
-        if (R.x != W.x || R.y != W.y || R.z != W.z || R.w != W.w) a.chk_memo[bd.slot_begin + j] = W;
-      }
+    const int ns = bd.nslots, nown = bd.nowned;
+    const int allc = check_pass(a, bd, s, smemo, shs, s_cnt, &s_moved) ? 0 : 1;
     if (tid == 0) {
       if (!allc) {
         nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
@@ -1610,9 +1685,13 @@ __global__ void k_commit3d(DevArgs a) {
   pdl_begin();
   const int lane = threadIdx.x & 31;
   const int iter = a.ctl->iter, stamp = iter + 1;
-  const int count = a.ctl->nact;
+  // with the checks inside the sweep kernel: the carried-over blocks and those its
+  // checks activated; the candidates go to the list the next sweep launch reads
+  const int count = a.ctl->nact + (a.fused ? a.ctl->nadd : 0);
   const int* act = act_list(a, iter);
   int* nxt = next_list(a, iter);
+  int* const cl = a.fused ? a.cand + (size_t)(iter & 1) * a.nb : a.list_new;
+  int* const cn = a.fused ? &a.ctl->ncand[iter & 1] : &a.ctl->nnew;
   // one warp per list entry, assigned by warp index (no claim round trip)
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   for (int item = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); item < count; item += nwarps) {
@@ -1624,8 +1703,10 @@ __global__ void k_commit3d(DevArgs a) {
     if (a.conv[b]) {
       for (int e = a.nbr_off[b] + lane; e < a.nbr_off[b + 1]; e += 32) {
         const int nb = a.nbr[e];
-        if (a.stampA[nb] != stamp && atomicExch(&a.stampC[nb], stamp) != stamp)
-          a.list_new[atomicAdd(&a.ctl->nnew, 1)] = nb;
+        if (a.stampA[nb] != stamp && atomicExch(&a.stampC[nb], stamp) != stamp) {
+          cl[atomicAdd(cn, 1)] = nb;
+          if (a.fused) atomicAdd(&a.inst_ncand[a.blk_inst[nb]], 1);
+        }
       }
     } else if (lane == 0) {
       nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
@@ -1662,29 +1743,53 @@ __global__ void k_activate2d(DevArgs a) {
 __device__ void finish_iteration_cta(const DevArgs& a, bool vertex_test) {
   Ctl* c = a.ctl;
   const int it = c->iter + 1;
-  int any = 0, fin = 0;
+  int any = 0, fin = 0, swept = 0;
   for (int i = threadIdx.x; i < a.ninst; i += blockDim.x) {
-    if (!a.inst_done[i]) {
+    const int st = a.inst_done[i];
+    if (st == 0 && a.fused && a.inst_swept[i] == 0) {
+      // its checks activated nothing: the reference's loop ended with the previous
+      // iteration, which this one does not count
+      a.inst_done[i] = 1;
+      fin = 1;
+    } else if (st == 0) {
+      swept = 1;
       const int own = a.inst_iters[i] + 1;  // iterations of this instance since it started
       a.inst_iters[i] = own;
-      const bool stop = a.inst_nnext[i] == 0 || own >= a.inst_maxit[i] || (vertex_test && a.inst_fail[i] == 0);
-      if (stop) {
+      // blocks waiting: carried over, or (checks in the sweep kernel) to be checked
+      const int pend = a.inst_nnext[i] + (a.fused ? a.inst_ncand[i] : 0);
+      const bool stop = pend == 0 || own >= a.inst_maxit[i] || (vertex_test && a.inst_fail[i] == 0);
+      if (!stop) {
+        any = 1;
+      } else if (a.fused && a.inst_ncand[i] > 0) {
+        a.inst_done[i] = 2;  // at its cap: the checks of this iteration still run
+        any = 1;
+      } else {
         a.inst_done[i] = 1;
         fin = 1;
-      } else {
-        any = 1;
       }
+    } else if (st == 2) {
+      a.inst_done[i] = 1;
+      fin = 1;
     }
     a.inst_nnext[i] = 0;
     a.inst_fail[i] = 0;
+    if (a.fused) {
+      a.inst_swept[i] = 0;
+      a.inst_ncand[i] = 0;
+    }
   }
   any = __syncthreads_or(any);
   fin = __syncthreads_or(fin);
+  swept = __syncthreads_or(swept);
   if (threadIdx.x == 0) {
     c->iter = it;
     c->nact = c->nnext;
     c->nnext = 0;
     c->nnew = 0;
+    c->nadd = 0;
+    c->ncand[it & 1] = 0;  // consumed by this iteration's sweep launch
+    c->last_idle = a.fused && !swept;
+    c->idle_iters += c->last_idle;
     c->work_a = c->work_c = 0;
     c->done_d = 0;
     bool go = any && c->error == 0;
@@ -1786,18 +1891,20 @@ __global__ void k_seed_state(const int* ids, int n, float* Ta, float* Tb, float*
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nact; i += gridDim.x * blockDim.x) stampA[act[i]] = 1;
 }
 
+// work waiting: active blocks, or (checks inside the sweep kernel) check candidates
+// queued by the last iteration's commit
+__device__ __host__ inline bool has_work(const Ctl& c, int fused) {
+  return (c.nact > 0 || (fused && c.ncand[(c.iter + 1) & 1] > 0)) && c.max_iters > 0;
+}
 __global__ void k_start(DevArgs a) {
-  if (threadIdx.x == 0) {
-    const Ctl* c = a.ctl;
-    cudaGraphSetConditional(a.cond, (c->nact > 0 && c->max_iters > 0) ? 1u : 0u);
-  }
+  if (threadIdx.x == 0) cudaGraphSetConditional(a.cond, has_work(*a.ctl, a.fused) ? 1u : 0u);
 }
 
 // per-iteration snapshot in renumbered order (iteration index = iter - 1)
 __global__ void k_snapshot(DevArgs a, int dim) {
   pdl_begin();
   const int slot = a.ctl->iter - 1;
-  if (slot < 0 || slot >= a.hist_cap) return;
+  if (slot < 0 || slot >= a.hist_cap || a.ctl->last_idle) return;
   float* dst = a.hist + (size_t)slot * a.nv;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nv; v += gridDim.x * blockDim.x)
     dst[v] = (dim == 3) ? (a.visited[a.vblock[v]] ? a.Ta[v] : 0.0f) : a.Ta[v];
@@ -1899,7 +2006,8 @@ __global__ void k_polish_begin(DevArgs a, int cap) {
   }
   if (threadIdx.x == 0) {
     c->max_iters = c->iter + cap;
-    c->nact = c->nnext = c->nnew = 0;
+    c->nact = c->nnext = c->nnew = c->nadd = 0;
+    c->ncand[0] = c->ncand[1] = 0;
     c->work_a = c->work_c = 0;
     c->done_d = 0;
     c->stop = 0;
@@ -1930,22 +2038,27 @@ __global__ void k_gather_hist(const float* h, const int* perm, int nv, float* ou
 // ---------------------------------------------------------------------------
 
 // Drops entries of finished instances from the active list of the coming
-// iteration (one CTA; list order does not affect results).
-__global__ void k_compact_active(DevArgs a) {
+// iteration and (checks in the sweep kernel) from its pending check candidates
+// (one CTA; list order does not affect results; list_new is scratch here).
+__device__ void compact_list(const DevArgs& a, int* list, int* count) {
   __shared__ int s_n;
-  Ctl* c = a.ctl;
-  int* act = act_list(a, c->iter);
-  const int n = c->nact;
+  const int n = *count;
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int b = act[i];
-    if (!a.inst_done[a.blk_inst[b]]) a.list_new[atomicAdd(&s_n, 1)] = b;
+    const int b = list[i];
+    if (a.inst_done[a.blk_inst[b]] != 1) a.list_new[atomicAdd(&s_n, 1)] = b;
   }
   __syncthreads();
   const int m = s_n;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) act[i] = a.list_new[i];
-  if (threadIdx.x == 0) c->nact = m;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) list[i] = a.list_new[i];
+  __syncthreads();
+  if (threadIdx.x == 0) *count = m;
+}
+__global__ void k_compact_active(DevArgs a) {
+  Ctl* c = a.ctl;
+  compact_list(a, act_list(a, c->iter), &c->nact);
+  if (a.fused) compact_list(a, a.cand + (size_t)((c->iter + 1) & 1) * a.nb, &c->ncand[(c->iter + 1) & 1]);
 }
 
 // Cancelled instances stop: marked finished, so visits skip their blocks.
@@ -2058,6 +2171,10 @@ __global__ void k_admit_seeds(DevArgs a, int inst, const int* seed_ids, int nsee
     a.inst_iters[inst] = 0;
     a.inst_nnext[inst] = 0;
     a.inst_fail[inst] = 0;
+    if (a.fused) {
+      a.inst_swept[inst] = 0;
+      a.inst_ncand[inst] = 0;
+    }
     const_cast<int*>(a.inst_maxit)[inst] = maxit;
   }
   __syncthreads();
@@ -2232,6 +2349,9 @@ struct DeviceSolve::Impl {
   int* inst_nnext = nullptr;
   int* inst_fail = nullptr;
   int* inst_maxit = nullptr;
+  int* cand = nullptr;        // 2 x nb check candidates (checks inside the sweep kernel)
+  int* inst_swept = nullptr;  // per instance: blocks swept this iteration
+  int* inst_ncand = nullptr;  // per instance: check candidates queued this iteration
   int ninst = 1;
   size_t coef_n = 0;
   // online choice of the 3D visit CTA size (FP32 / precision kernels): candidates
@@ -2306,7 +2426,7 @@ struct DeviceSolve::Impl {
     void* ps[] = {blocks, coef, lv, halo, nbr_off, nbr, vblock, perm, Ta, Tb, Tinit, prev, conv,
                   stampA, stampC, visited, list0, list1, list_new, ctl, hist, ktime, out_tmp,
                   blk_inst, inst_done, inst_iters, inst_nnext, inst_fail, inst_maxit, seed_ids,
-                  slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo, hsb, hs64, hsu64};
+                  cand, inst_swept, inst_ncand, slot_f64, coef64, res_cand, inst_vbeg, chunks, chk_memo, hsb, hs64, hsu64};
     for (void* p : ps)
       if (p) cudaFree(p);
     hsb = nullptr;
@@ -2329,6 +2449,7 @@ struct DeviceSolve::Impl {
     list1 = nullptr; list_new = nullptr; ctl = nullptr; hist = nullptr; ktime = nullptr; out_tmp = nullptr;
     blk_inst = nullptr; inst_done = nullptr; inst_iters = nullptr; inst_nnext = nullptr; inst_fail = nullptr;
     inst_maxit = nullptr;
+    cand = nullptr; inst_swept = nullptr; inst_ncand = nullptr;
     hist_cap = 0;
     ktime_cap = 0;
     drop_graph();
@@ -2373,6 +2494,9 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.hsb = (L.dim == 3) ? P.hsb : nullptr;
     a.hs64 = P.hs64;
     a.hsu64 = P.hsu64;
+    a.cand = P.cand;
+    a.inst_swept = P.inst_swept;
+    a.inst_ncand = P.inst_ncand;
     if (serve) { a.ktime = nullptr; a.ktime_cap = 0; }
     CK(cudaGraphCreate(&P.graph, 0));
     CK(cudaGraphConditionalHandleCreate(&a.cond, P.graph, 0, 0));
@@ -2434,6 +2558,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
         (void)si;
         (void)sc;
       }
+      a.fused = (EIK_FUSED_CHECK && kv_fim == (void*)k_sweep3d && kv_chk == (void*)k_check3d) ? 1 : 0;
     } else if (slot2d) {
       vthreads = std::max(32, (P.max_slots_pad + 31) & ~31);
       vsmem = vsmem_chk = smem_bytes_slot2d(P.max_slots_pad, P.max_local, P.max_owned);
@@ -2520,7 +2645,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     static int role_vals[3] = {0, 1, 2};  // read-only kernel arguments
     void* sweep_args[3][2] = {{&P.args, &role_vals[0]}, {&P.args, &role_vals[1]}, {&P.args, &role_vals[2]}};
     int grid_small = 0;
-    if (kv_fim == (void*)k_sweep3d && EIK_SWEEP_SPLIT > 0 && vthreads == kItemThreads) {
+    if (kv_fim == (void*)k_sweep3d && EIK_SWEEP_SPLIT > 0 && vthreads == kItemThreads && !a.fused) {
       int occ2 = 0;
       CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_sweep3d, 1024, vsmem));
       if (occ2 >= 1) grid_small = std::min(occ2 * nsm, std::max(L.nb, 1));
@@ -2537,7 +2662,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
       }
       if (L.dim == 3) {
         if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
-        if (!(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
+        if (!a.fused && !(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
         if (!(e = add((void*)k_close3d, 1, 256, 0, close_args)).empty()) return e;
       } else {
         if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
@@ -2789,8 +2914,10 @@ std::string DeviceSolve::finish_upload(const Layout& L, bool layout_on_device) {
   if (!(e = dev_alloc(P.ctl, 1)).empty()) return e;
   P.ninst = std::max(L.ninst, 1);
   if (!(e = dev_alloc(P.blk_inst, (size_t)L.nb)).empty()) return e;
-  for (int** t : {&P.inst_done, &P.inst_iters, &P.inst_nnext, &P.inst_fail, &P.inst_maxit})
+  for (int** t : {&P.inst_done, &P.inst_iters, &P.inst_nnext, &P.inst_fail, &P.inst_maxit, &P.inst_swept,
+                  &P.inst_ncand})
     if (!(e = dev_alloc(*t, (size_t)P.ninst)).empty()) return e;
+  if (!(e = dev_alloc(P.cand, 2 * (size_t)L.nb)).empty()) return e;
   if (!(e = dev_alloc(P.inst_vbeg, (size_t)P.ninst + 1)).empty()) return e;
   cudaStream_t st = (cudaStream_t)stream_;
   std::vector<int>& vb = P.h_vblock;
@@ -3011,9 +3138,8 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     P.h_maxit = cap;
     CK(cudaMemcpyAsync(P.inst_done, done.data(), sizeof(int) * P.ninst, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(P.inst_maxit, P.h_maxit.data(), sizeof(int) * P.ninst, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(P.inst_iters, 0, sizeof(int) * P.ninst, st));
-    CK(cudaMemsetAsync(P.inst_nnext, 0, sizeof(int) * P.ninst, st));
-    CK(cudaMemsetAsync(P.inst_fail, 0, sizeof(int) * P.ninst, st));
+    for (int* t : {P.inst_iters, P.inst_nnext, P.inst_fail, P.inst_swept, P.inst_ncand})
+      CK(cudaMemsetAsync(t, 0, sizeof(int) * P.ninst, st));
   }
   stats_.h2d_bytes = (long long)sizeof(float) * P.h_prev.size() + (long long)sizeof(int) * nseed +
                      (long long)sizeof(int) * P.h_act.size() + 2ll * sizeof(int) * P.ninst + (long long)sizeof(Ctl);
@@ -3039,11 +3165,12 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     // between iterations (profilers cannot see kernels inside conditional graphs)
     DevArgs d = P.args;
     d.use_cond = 0;
-    for (;;) {
+    for (bool first = true;; first = false) {
       Ctl h{};
       CK(cudaMemcpyAsync(&h, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      if (h.stop || h.error || h.nact <= 0 || h.iter >= h.max_iters) break;
+      // the graph's start node's test, then its closes' decision
+      if (h.error || (first ? !has_work(h, d.fused) : h.stop != 0)) break;
       for (const Impl::Launch& l : P.body) {
         void* args[2] = {&d, (void*)&l.extra};
         CK(cudaLaunchKernel(l.func, dim3(l.grid), dim3(l.block), args, l.smem, st));
@@ -3091,7 +3218,9 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   Ctl out{};
   CK(cudaMemcpy(&out, P.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
   cudaEventElapsedTime(&stats_.solve_ms, P.ev0, P.ev1);
-  stats_.iterations = out.iter;
+  // a trailing iteration that swept nothing (its checks activated no block) is not
+  // one of the reference's iterations
+  stats_.iterations = out.iter - out.idle_iters;
   stats_.vertex_updates = (long long)out.updates;
   stats_.fim_visits = (long long)out.fim_visits;
   stats_.check_visits = (long long)out.chk_visits;
@@ -3111,15 +3240,22 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     CK(cudaMemcpy(kt.data(), P.ktime, sizeof(unsigned long long) * kt.size(), cudaMemcpyDeviceToHost));
     double fim = 0, chk = 0;
     int nf = 0, nc = 0;
-    const int nit = std::min(out.iter, P.ktime_cap);
+    // launch spans of every loop iteration; rows for the counted ones
+    const int nloop = std::min(out.iter, P.ktime_cap);
+    const int nit = std::min(stats_.iterations, nloop);
     stats_.iter_stats.assign(kIterStatWords * (size_t)nit, 0);
-    for (int i = 0; i < nit; ++i) {
+    const unsigned long long t00 = (nloop > 0 && kt[0]) ? ~kt[0] : 0;
+    long long row[kIterStatWords];
+    for (int i = 0; i < nloop; ++i) {
       const unsigned long long* k = &kt[kKStride * (size_t)i];
-      long long* o = &stats_.iter_stats[kIterStatWords * (size_t)i];
+      long long* o = (i < nit) ? &stats_.iter_stats[kIterStatWords * (size_t)i] : row;
       const unsigned long long f0 = ~k[0], c0 = ~k[2];
       if (k[0] && k[1] > f0) { fim += (double)(k[1] - f0); ++nf; o[0] = (long long)(k[1] - f0); }
       if (k[2] && k[3] > c0) { chk += (double)(k[3] - c0); ++nc; o[1] = (long long)(k[3] - c0); }
       for (int w = 0; w < 8; ++w) o[2 + w] = (long long)k[4 + w];
+      o[10] = (k[0] && t00) ? (long long)(f0 - t00) : -1;
+      o[11] = (k[2] && t00) ? (long long)(c0 - t00) : -1;
+      for (int w = 0; w < 4; ++w) o[12 + w] = (long long)k[12 + w];
     }
     stats_.fim_kernel_ms = (float)(fim * 1e-6);
     if (measured && fim > 0) {  // sweep-kernel time per slot visit of this CTA size
@@ -3276,7 +3412,7 @@ size_t device_footprint(const Layout& L, const Built3D* b) {
   return nb * sizeof(BlockDesc) + ncoef * sizeof(float) + (size_t)L.total_slots * (sizeof(uint2) + sizeof(int)) +
          (L.dim == 3 ? (size_t)L.total_slots * (2 * sizeof(uint4) + sizeof(uint2)) : 0) + nhalo * sizeof(int) +
          ngraph * sizeof(int) +
-         nv * (2 * sizeof(int) + 5 * sizeof(float)) + nb * (7 * sizeof(int) + 1) + 5 * sizeof(int);
+         nv * (2 * sizeof(int) + 5 * sizeof(float)) + nb * (9 * sizeof(int) + 1) + 7 * sizeof(int);
 }
 
 cudaStream_t new_stream() {
@@ -3367,7 +3503,7 @@ std::string DeviceSolve::serve_setup(const std::vector<ServeSource>& meshes, con
   // every instance idle, every vertex at LARGENUM
   std::vector<int> ones(P.ninst, 1);
   CK(cudaMemcpyAsync(P.inst_done, ones.data(), sizeof(int) * P.ninst, cudaMemcpyHostToDevice, st));
-  for (int* t : {P.inst_iters, P.inst_nnext, P.inst_fail, P.inst_maxit})
+  for (int* t : {P.inst_iters, P.inst_nnext, P.inst_fail, P.inst_maxit, P.inst_swept, P.inst_ncand})
     CK(cudaMemsetAsync(t, 0, sizeof(int) * P.ninst, st));
   for (int* t : {P.conv, P.stampA, P.stampC}) CK(cudaMemsetAsync(t, 0, sizeof(int) * L.nb, st));
   CK(cudaMemsetAsync(P.visited, 0, L.nb, st));
@@ -3500,6 +3636,8 @@ std::string DeviceSolve::serve_poll(std::vector<int>& done, std::vector<int>& it
   CK(cudaMemcpyAsync(done.data(), P.inst_done, sizeof(int) * P.ninst, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(iters.data(), P.inst_iters, sizeof(int) * P.ninst, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  // an instance at its cap whose last checks have not run yet (2) is still running
+  for (int& d : done) d = (d == 1) ? 1 : 0;
   return "";
 }
 
