@@ -1692,25 +1692,54 @@ __global__ void k_commit3d(DevArgs a) {
   int* nxt = next_list(a, iter);
   int* const cl = a.fused ? a.cand + (size_t)(iter & 1) * a.nb : a.list_new;
   int* const cn = a.fused ? &a.ctl->ncand[iter & 1] : &a.ctl->nnew;
-  // one warp per list entry, assigned by warp index (no claim round trip)
+  // a single instance's state, read with the control block
+  const int done1 = (a.ninst == 1) ? a.inst_done[0] : -1;
+  if (done1 > 0) return;
+  // one warp per list entry, assigned by warp index (no claim round trip).  The
+  // launch is a chain of dependent loads, so every load that depends only on the
+  // block is issued in one round before any branch on them.
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   for (int item = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); item < count; item += nwarps) {
     const int b = act[item];
-    if (a.inst_done[a.blk_inst[b]]) continue;
     const BlockDesc bd = a.blocks[b];
-    for (int k = lane; k < bd.nowned; k += 32) a.Ta[bd.vbase + k] = a.Tb[bd.vbase + k];
+    const int cv = a.conv[b];
+    const int e0 = a.nbr_off[b], e1 = a.nbr_off[b + 1];
+    const int inst = (done1 >= 0) ? 0 : a.blk_inst[b];
+    const int dn = (done1 >= 0) ? 0 : a.inst_done[inst];
+    const float t0 = (lane < bd.nowned) ? a.Tb[bd.vbase + lane] : 0.0f;
+    const float t1 = (lane + 32 < bd.nowned) ? a.Tb[bd.vbase + lane + 32] : 0.0f;
+    const int nb0 = (e0 + lane < e1) ? a.nbr[e0 + lane] : -1;
+    if (dn) continue;
+    if (lane < bd.nowned) a.Ta[bd.vbase + lane] = t0;
+    if (lane + 32 < bd.nowned) a.Ta[bd.vbase + lane + 32] = t1;
+    for (int k = lane + 64; k < bd.nowned; k += 32) a.Ta[bd.vbase + k] = a.Tb[bd.vbase + k];
     if (lane == 0) a.visited[b] = 1;
-    if (a.conv[b]) {
-      for (int e = a.nbr_off[b] + lane; e < a.nbr_off[b + 1]; e += 32) {
-        const int nb = a.nbr[e];
-        if (a.stampA[nb] != stamp && atomicExch(&a.stampC[nb], stamp) != stamp) {
-          cl[atomicAdd(cn, 1)] = nb;
-          if (a.fused) atomicAdd(&a.inst_ncand[a.blk_inst[nb]], 1);
+    if (cv) {
+      // queue each neighbour not left unconverged this iteration, once: the stamp
+      // test and the exchange go out together (an unconverged neighbour marked as
+      // queued is never queued, which is what it needs)
+      for (int base = e0; base < e1; base += 32) {
+        const int nb = (base == e0) ? nb0 : ((base + lane < e1) ? a.nbr[base + lane] : -1);
+        bool q = false;
+        if (nb >= 0) {
+          const int sa = a.stampA[nb];
+          const int old = atomicExch(&a.stampC[nb], stamp);
+          q = sa != stamp && old != stamp;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, q);
+        if (bal) {
+          int pos = 0;
+          if (lane == 0) pos = atomicAdd(cn, __popc(bal));
+          pos = __shfl_sync(0xffffffffu, pos, 0) + __popc(bal & ((1u << lane) - 1u));
+          if (q) {
+            cl[pos] = nb;
+            if (a.fused) atomicAdd(&a.inst_ncand[inst], 1);
+          }
         }
       }
     } else if (lane == 0) {
       nxt[atomicAdd(&a.ctl->nnext, 1)] = b;
-      atomicAdd(&a.inst_nnext[a.blk_inst[b]], 1);
+      atomicAdd(&a.inst_nnext[inst], 1);
     }
   }
 }
@@ -1742,25 +1771,32 @@ __global__ void k_activate2d(DevArgs a) {
 // 813-815); the loop goes on while any instance runs.
 __device__ void finish_iteration_cta(const DevArgs& a, bool vertex_test) {
   Ctl* c = a.ctl;
+  // the control block's words and (below) each instance's, loaded in one round
+  // before any decision: the close is a short chain of dependent loads
   const int it = c->iter + 1;
+  const int nnext = c->nnext, err = c->error, idle0 = c->idle_iters;
+  const int pending = (a.serve && threadIdx.x == 0) ? *a.pending : 0;
   int any = 0, fin = 0, swept = 0;
   for (int i = threadIdx.x; i < a.ninst; i += blockDim.x) {
     const int st = a.inst_done[i];
-    if (st == 0 && a.fused && a.inst_swept[i] == 0) {
+    const int nsw = a.fused ? a.inst_swept[i] : 1, ncd = a.fused ? a.inst_ncand[i] : 0;
+    const int its = a.inst_iters[i], nn = a.inst_nnext[i], mx = a.inst_maxit[i];
+    const int fl = vertex_test ? a.inst_fail[i] : 1;
+    if (st == 0 && nsw == 0) {
       // its checks activated nothing: the reference's loop ended with the previous
       // iteration, which this one does not count
       a.inst_done[i] = 1;
       fin = 1;
     } else if (st == 0) {
       swept = 1;
-      const int own = a.inst_iters[i] + 1;  // iterations of this instance since it started
+      const int own = its + 1;  // iterations of this instance since it started
       a.inst_iters[i] = own;
       // blocks waiting: carried over, or (checks in the sweep kernel) to be checked
-      const int pend = a.inst_nnext[i] + (a.fused ? a.inst_ncand[i] : 0);
-      const bool stop = pend == 0 || own >= a.inst_maxit[i] || (vertex_test && a.inst_fail[i] == 0);
+      const int pend = nn + ncd;
+      const bool stop = pend == 0 || own >= mx || fl == 0;
       if (!stop) {
         any = 1;
-      } else if (a.fused && a.inst_ncand[i] > 0) {
+      } else if (ncd > 0) {
         a.inst_done[i] = 2;  // at its cap: the checks of this iteration still run
         any = 1;
       } else {
@@ -1783,17 +1819,18 @@ __device__ void finish_iteration_cta(const DevArgs& a, bool vertex_test) {
   swept = __syncthreads_or(swept);
   if (threadIdx.x == 0) {
     c->iter = it;
-    c->nact = c->nnext;
+    c->nact = nnext;
     c->nnext = 0;
     c->nnew = 0;
     c->nadd = 0;
     c->ncand[it & 1] = 0;  // consumed by this iteration's sweep launch
-    c->last_idle = a.fused && !swept;
-    c->idle_iters += c->last_idle;
+    const int idle = (a.fused && !swept) ? 1 : 0;
+    c->last_idle = idle;
+    c->idle_iters = idle0 + idle;
     c->work_a = c->work_c = 0;
     c->done_d = 0;
-    bool go = any && c->error == 0;
-    if (a.serve && (fin || *a.pending != 0)) go = false;
+    bool go = any && err == 0;
+    if (a.serve && (fin || pending != 0)) go = false;
     c->stop = go ? 0 : 1;
     if (a.use_cond) cudaGraphSetConditional(a.cond, go ? 1u : 0u);
   }
