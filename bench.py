@@ -823,15 +823,14 @@ def main():
                      "traffic_over_algorithmic": tva["sweep"]["traffic_over_algorithmic"],
                      "check_kernel": (None if fused else dict(tva["check"], kernel_ms_per_step=chk_ms / args.steps)),
                      "traffic_source": f"profiles/{DRAM_PROFILE}: ncu dram__bytes_read.sum + dram__bytes_write.sum "
-                                       "of every sweep and check launch of one solve of this workload (kernel by "
-                                       "kernel; cold caches), set beside this run's algorithmic bytes of the same "
-                                       "iterations",
+                                       "of every sweep launch of one solve of this workload (kernel by kernel; cold "
+                                       "caches), set beside this run's algorithmic bytes of the same launches",
                      "note": "the sweep kernel is bound by CTA barriers and instruction latency in the tet local "
                              "solver, not by HBM",
                      # compute side, from the committed full capture of one sweep launch (outer
                      # iteration 40 of the same solve, kernel-by-kernel mode)
-                     "compute": {"bound": "issue", "issue_active_pct": 53.9, "ipc_per_sm": 2.13,
-                                 "fma_pipe_pct": 17.1, "alu_pipe_pct": 33.7, "xu_pipe_pct": 8.1,
+                     "compute": {"bound": "issue", "issue_active_pct": 51.3, "ipc_per_sm": 2.01,
+                                 "fma_pipe_pct": 15.4, "alu_pipe_pct": 31.0, "xu_pipe_pct": 6.9,
                                  "top_stall": "barrier",
                                  "source": "profiles/fim3d_items_c3d.md (ncu --set full, one k_sweep3d launch)"}},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,

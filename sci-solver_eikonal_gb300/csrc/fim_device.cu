@@ -220,6 +220,14 @@ constexpr int kKStride = 16;    // words of per-iteration telemetry (DevArgs::kt
 #ifndef EIK_CHECK_ITEMS
 #define EIK_CHECK_ITEMS 1
 #endif
+// item kernels: CTA size when the caller gives none, and the register cap that
+// lets three such CTAs share an SM's 64 K registers
+#ifndef EIK_ITEM_THREADS
+#define EIK_ITEM_THREADS 384
+#endif
+#ifndef EIK_ITEM_MAXNREG
+#define EIK_ITEM_MAXNREG 56
+#endif
 // 3D item kernels: the neighbour checks of an iteration run inside the next
 // iteration's sweep launch (1) or as their own launch, k_check3d (0)
 #ifndef EIK_FUSED_CHECK
@@ -999,7 +1007,7 @@ __device__ __forceinline__ bool check_pass(const DevArgs& a, const BlockDesc& bd
 // iteration's commit (items nact.. of the claim range): a candidate's check runs
 // on the staged block, and a block that moves is appended to this iteration's
 // active list and swept in the same visit.
-__global__ void __maxnreg__(56) k_sweep3d(DevArgs a, int role) {
+__global__ void __maxnreg__(EIK_ITEM_MAXNREG) k_sweep3d(DevArgs a, int role) {
   pdl_begin();
   if (role != 0 && ((a.ctl->nact >= a.sweep_split) != (role == 1))) return;
   extern __shared__ __align__(16) unsigned char sm[];
@@ -1265,7 +1273,7 @@ __host__ __device__ inline size_t smem_bytes_check(int np, int max_local, int ma
   return check_offsets(np, max_local, max_owned, off);
 }
 
-__global__ void __maxnreg__(56) k_check3d(DevArgs a) {
+__global__ void __maxnreg__(EIK_ITEM_MAXNREG) k_check3d(DevArgs a) {
   pdl_begin();
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long bar;
@@ -2307,7 +2315,7 @@ cudaError_t raise_smem_limit(const void* func, size_t bytes) {
 }
 
 // CTA size of the item sweep and check kernels when the caller gives none
-constexpr int kItemThreads = 384;
+constexpr int kItemThreads = EIK_ITEM_THREADS;
 
 // Precision mode's polish: rounds, iterations per round, and the relative gap
 // between a vertex's time and its FP64 update above which its block runs again.
