@@ -1700,15 +1700,19 @@ __global__ void k_commit3d(DevArgs a) {
   int* nxt = next_list(a, iter);
   int* const cl = a.fused ? a.cand + (size_t)(iter & 1) * a.nb : a.list_new;
   int* const cn = a.fused ? &a.ctl->ncand[iter & 1] : &a.ctl->nnew;
-  // a single instance's state, read with the control block
+  // a single instance's state and the first list entries, read with the control block
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int done1 = (a.ninst == 1) ? a.inst_done[0] : -1;
+  // the warp's first entry of either list (the iteration's parity picks one): a
+  // dependent round trip less (65^3 solve 0.3% faster)
+  const int spec0 = (gw < a.nb) ? a.list0[gw] : 0, spec1 = (gw < a.nb) ? a.list1[gw] : 0;
   if (done1 > 0) return;
   // one warp per list entry, assigned by warp index (no claim round trip).  The
   // launch is a chain of dependent loads, so every load that depends only on the
   // block is issued in one round before any branch on them.
-  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-  for (int item = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); item < count; item += nwarps) {
-    const int b = act[item];
+  for (int item = gw; item < count; item += nwarps) {
+    const int b = (item == gw) ? ((iter & 1) ? spec1 : spec0) : act[item];
     const BlockDesc bd = a.blocks[b];
     const int cv = a.conv[b];
     const int e0 = a.nbr_off[b], e1 = a.nbr_off[b + 1];
