@@ -228,6 +228,11 @@ constexpr int kKStride = 16;    // words of per-iteration telemetry (DevArgs::kt
 #ifndef EIK_ITEM_MAXNREG
 #define EIK_ITEM_MAXNREG 56
 #endif
+// sweep visits: the block's sweep memos arrive with its bulk copies (1) or are read
+// from memory while the first sweep's updates are listed (0)
+#ifndef EIK_STAGE_SWEEP_MEMO
+#define EIK_STAGE_SWEEP_MEMO 1
+#endif
 // 3D item kernels: the neighbour checks of an iteration run inside the next
 // iteration's sweep launch (1) or as their own launch, k_check3d (0)
 #ifndef EIK_FUSED_CHECK
@@ -358,12 +363,14 @@ __host__ __device__ inline size_t smem_bytes(int ncoef, int max_slots_pad, int m
   return (n + 15) & ~(size_t)15;
 }
 
-// Issue the two bulk copies of block `bd` (coefficients + corner ids) and gather
-// the owned / halo travel times from `Tsrc`.  Returns false on a copy timeout.
+// Issue the bulk copies of block `bd` (coefficients + corner ids; the memos of
+// `gmemo`, the check memos by default, into smemo; the apex bounds into shs) and
+// gather the owned / halo travel times from `Tsrc`.  Returns false on a copy timeout.
 template <class S>
 __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd, int ncoef, const S& s,
                                            unsigned long long* bar, unsigned& parity, const float* Tsrc,
-                                           uint4* smemo = nullptr, uint2* shs = nullptr) {
+                                           uint4* smemo = nullptr, uint2* shs = nullptr,
+                                           const uint4* gmemo = nullptr) {
   const int tid = threadIdx.x, NT = blockDim.x;
   if (tid == 0) {
     fence_proxy_async();
@@ -374,7 +381,7 @@ __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd
       mbar_expect_tx(bar, bc + bl + bm + bh);
       bulk_g2s(s.coef, a.coef + (size_t)ncoef * bd.slot_begin, bc, bar);
       bulk_g2s(s.lv, a.lv + bd.slot_begin, bl, bar);
-      if (bm) bulk_g2s(smemo, a.chk_memo + bd.slot_begin, bm, bar);
+      if (bm) bulk_g2s(smemo, (gmemo ? gmemo : a.chk_memo) + bd.slot_begin, bm, bar);
       if (bh) bulk_g2s(shs, a.hsb + bd.slot_begin, bh, bar);
     } else {
       mbar_expect_tx(bar, 0);
@@ -1056,10 +1063,12 @@ __global__ void __maxnreg__(EIK_ITEM_MAXNREG) k_sweep3d(DevArgs a, int role) {
       continue;
     }
     SmemItems s = s0;
-    // a candidate's check memos arrive in the per-slot copy buffer h0, which the
-    // first sweep neither reads nor writes
-    uint4* const smemo = (chk && a.chk_memo) ? reinterpret_cast<uint4*>(s.h0) : nullptr;
-    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo, a.hsb ? s.hs : nullptr)) {
+    // a candidate's check memos, or an active block's sweep memos, arrive in the
+    // per-slot copy buffer h0, which the first sweep neither reads nor writes
+    uint4* const smemo = (chk ? a.chk_memo != nullptr : (EIK_STAGE_SWEEP_MEMO && a.fim_memo != nullptr))
+                             ? reinterpret_cast<uint4*>(s.h0)
+                             : nullptr;
+    if (!load_block(a, bd, 6, s, &bar, parity, a.Ta, smemo, a.hsb ? s.hs : nullptr, chk ? nullptr : a.fim_memo)) {
       if (tid == 0) atomicOr(&a.ctl->error, kErrWait);
       (void)mbar_wait(&bar, parity ^ 1u);
       __syncthreads();
@@ -1122,7 +1131,8 @@ __global__ void __maxnreg__(EIK_ITEM_MAXNREG) k_sweep3d(DevArgs a, int role) {
           // result its time has already absorbed (times only decrease)
           unsigned same = 0;
           if (first && a.fim_memo) {
-            const uint4 mm = a.fim_memo[bd.slot_begin + j];
+            // staged with the block, or (a block its check activated) from memory
+            const uint4 mm = (smemo && !chk) ? smemo[j] : a.fim_memo[bd.slot_begin + j];
             same = (__float_as_uint(Tq[0]) == mm.x ? 1u : 0u) | (__float_as_uint(Tq[1]) == mm.y ? 2u : 0u) |
                    (__float_as_uint(Tq[2]) == mm.z ? 4u : 0u) | (__float_as_uint(Tq[3]) == mm.w ? 8u : 0u);
           }
