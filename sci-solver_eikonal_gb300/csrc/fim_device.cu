@@ -1773,15 +1773,39 @@ __global__ void k_activate2d(DevArgs a) {
   const int iter = a.ctl->iter, stamp = iter + 1;
   const int count = a.ctl->nact;
   const int* act = act_list(a, iter);
-  // one warp per list entry, assigned by warp index (no claim round trip)
+  // one warp per list entry, assigned by warp index (no claim round trip).  As in
+  // k_commit3d, the launch is a chain of dependent loads: a single instance's state
+  // and the warp's first entry of either list come with the control block, and
+  // every load that depends only on the block goes out before any branch on them.
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-  for (int item = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); item < count; item += nwarps) {
-    const int b = act[item];
-    if (a.inst_done[a.blk_inst[b]] || !a.conv[b]) continue;
-    for (int e = a.nbr_off[b] + lane; e < a.nbr_off[b + 1]; e += 32) {
-      const int nb = a.nbr[e];
-      if (a.stampA[nb] != stamp && atomicExch(&a.stampC[nb], stamp) != stamp)
-        a.list_new[atomicAdd(&a.ctl->nnew, 1)] = nb;
+  const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int done1 = (a.ninst == 1) ? a.inst_done[0] : -1;
+  const int spec0 = (gw < a.nb) ? a.list0[gw] : 0, spec1 = (gw < a.nb) ? a.list1[gw] : 0;
+  if (done1 > 0) return;
+  for (int item = gw; item < count; item += nwarps) {
+    const int b = (item == gw) ? ((iter & 1) ? spec1 : spec0) : act[item];
+    const int cv = a.conv[b];
+    const int e0 = a.nbr_off[b], e1 = a.nbr_off[b + 1];
+    const int dn = (done1 >= 0) ? 0 : a.inst_done[a.blk_inst[b]];
+    const int nb0 = (e0 + lane < e1) ? a.nbr[e0 + lane] : -1;
+    if (dn || !cv) continue;
+    for (int base = e0; base < e1; base += 32) {
+      const int nb = (base == e0) ? nb0 : ((base + lane < e1) ? a.nbr[base + lane] : -1);
+      // the active-list test and the exchange go out together (a block already
+      // in the list marked as queued is never queued, which is what it needs)
+      bool q = false;
+      if (nb >= 0) {
+        const int sa = a.stampA[nb];
+        const int old = atomicExch(&a.stampC[nb], stamp);
+        q = sa != stamp && old != stamp;
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, q);
+      if (bal) {
+        int pos = 0;
+        if (lane == 0) pos = atomicAdd(&a.ctl->nnew, __popc(bal));
+        pos = __shfl_sync(0xffffffffu, pos, 0) + __popc(bal & ((1u << lane) - 1u));
+        if (q) a.list_new[pos] = nb;
+      }
     }
   }
 }
