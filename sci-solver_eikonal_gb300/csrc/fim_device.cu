@@ -233,6 +233,9 @@ constexpr int kKStride = 16;    // words of per-iteration telemetry (DevArgs::kt
 #ifndef EIK_STAGE_SWEEP_MEMO
 #define EIK_STAGE_SWEEP_MEMO 1
 #endif
+#ifndef EIK_SIZED_AUX
+#define EIK_SIZED_AUX 1
+#endif
 // 3D item kernels: the neighbour checks of an iteration run inside the next
 // iteration's sweep launch (1) or as their own launch, k_check3d (0)
 #ifndef EIK_FUSED_CHECK
@@ -2670,6 +2673,15 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
       else cthreads = vthreads;
     }
     P.grid_aux = nsm * 4;
+    // the per-block launches (one warp per list entry, eight a CTA) and the 2D vertex
+    // test (a CTA per chunk) need no more CTAs than they have work for; every CTA of
+    // the vertex test also takes part in its last-CTA close
+#if EIK_SIZED_AUX
+    const int grid_blocks = std::max(1, std::min(P.grid_aux, (L.nb + 7) / 8));
+    const int grid_chunks = std::max(1, std::min(P.grid_aux, P.nchunks));
+#else
+    const int grid_blocks = P.grid_aux, grid_chunks = P.grid_aux;
+#endif
     // start node
     void* args_ptr[] = {&P.args};
     cudaGraphNode_t n_start, n_while;
@@ -2744,13 +2756,13 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
         return e;
       }
       if (L.dim == 3) {
-        if (!(e = add((void*)k_commit3d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+        if (!(e = add((void*)k_commit3d, grid_blocks, 256, 0, args_ptr)).empty()) return e;
         if (!a.fused && !(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
         if (!(e = add((void*)k_close3d, 1, 256, 0, close_args)).empty()) return e;
       } else {
-        if (!(e = add((void*)k_activate2d, P.grid_aux, 256, 0, args_ptr)).empty()) return e;
+        if (!(e = add((void*)k_activate2d, grid_blocks, 256, 0, args_ptr)).empty()) return e;
         if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
-        if (!(e = add((void*)k_vertex_test2d, P.grid_aux, 256, 0, close_args)).empty()) return e;
+        if (!(e = add((void*)k_vertex_test2d, grid_chunks, 256, 0, close_args)).empty()) return e;
       }
       if (want_hist)
         if (!(e = add((void*)k_snapshot, P.grid_aux, 256, 0, snap_args)).empty()) return e;
