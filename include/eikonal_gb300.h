@@ -57,11 +57,13 @@ typedef struct eik_options {
   int direct_launch;       /* 0 (default): a solve is one CUDA-graph launch; 1: the same kernels
                               launched one by one with a host check per iteration, for profilers
                               that cannot see kernels inside conditional graphs */
-  int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/512/1024).  0 (default):
-                              chosen per handle over its first solves between one thread per slot
-                              of the largest block and 512 (two CTAs per SM), by measured speed;
-                              results do not depend on it.  The check kernel runs CTAs of half
-                              the size when this is 1024. */
+  int threads_per_block;   /* CTA size of the 3D block-sweep kernels (128/256/384/512/768/1024).
+                              0 (default): 384 for the apex-item kernels (three CTAs per SM);
+                              for the slot kernels (precision mode, blocks too large for the
+                              item kernels' shared memory) chosen per handle over its first
+                              solves between one thread per slot of the largest block and 512,
+                              by measured speed.  Results do not depend on it.  The slot check
+                              kernel runs CTAs of half the size when this is 1024. */
   int precision;           /* 0 (default): the reference's FP32 arithmetic, bit for bit.  1 (3D):
                               tets whose metric edge Gram matrix has condition number above
                               precision_kappa (slivers, strong anisotropy) run their local
