@@ -914,9 +914,27 @@ def c2d_summary(E):
     init[0] = 0
     r64 = O.solve2d(xyz, ff, np.ones(ff.shape[0], np.float32), obt, off, vfv, lab, nb, [0], init, precision=64)
     dist = np.linalg.norm(xyz.astype(np.float64) - xyz[0].astype(np.float64), axis=1)
-    return {"workload": C2D_WORKLOAD, "solve_ms_p50": statistics.median(ms), "iterations": e.numIterations(),
-            "blocks": int(nb), "error_vs_fp64": error_stats(got, r64["result"]),
-            "error_vs_exact_distance": error_stats(got, dist)}
+    out = {"workload": C2D_WORKLOAD, "solve_ms_p50": statistics.median(ms), "iterations": e.numIterations(),
+           "blocks": int(nb), "error_vs_fp64": error_stats(got, r64["result"]),
+           "error_vs_exact_distance": error_stats(got, dist)}
+    # the reference's own 2D kernels (FIMCuda, run_check_neighbor, run_reduction built
+    # from its sources) under the restatement of its host loop (meshFIM2d_eikonal.cu:
+    # 683-816), same mesh, seed and partition (reference baseline only)
+    if O.ref_gpu() is None:
+        out["reference_gpu"] = {"unavailable": "the reference's kernels were not built (oracle/_ref/ref2d.cubin)"}
+    else:
+        loops = []
+        for _ in range(5):
+            r = O.ref_gpu_solve2d(xyz, ff, np.ones(ff.shape[0], np.float32), obt, off, vfv, lab, nb, [0], init,
+                                  max_iters=MAX_ITERS)
+            loops.append(r["loop_ms"])
+        out["reference_gpu"] = {
+            "ms_per_solve": statistics.median(loops), "iterations": r["iterations"],
+            "bitwise_equal_to_ours": bool(np.array_equal(np.asarray(r["result"], np.float32).view(np.uint32),
+                                                         np.asarray(got, np.float32).view(np.uint32))),
+            "what": "outer loop of the reference's CUDA kernels compiled from its sources for sm_103a, host round "
+                    "trips every iteration, median of 5 solves"}
+    return out
 
 
 def first_solve_2d(E, batch_count=256, vpb=128):

@@ -388,7 +388,8 @@ def ref_gpu_solve2d(xyz, faces, speed_inv, obtuse, vf_off, vf_verts, labels, nbl
         iv.ctypes.data_as(_FP), int(max_iters), out.ctypes.data_as(_FP),
         hist.ctypes.data_as(_FP) if history else None, int(max_iters) if history else 0, ctypes.byref(upd),
         ctypes.byref(mf)))
-    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_faces": mf.value}
+    res = {"result": out, "iterations": it, "vertex_updates": upd.value, "max_faces": mf.value,
+           "loop_ms": ref_gpu().refgpu_last_loop_ms()}
     if history:
         res["history"] = hist[:it]
     return res

@@ -23,7 +23,7 @@ using namespace oracle;
 namespace {
 
 std::string g_err;
-double g_loop_ms = 0;  // wall time of the last 3D solve's outer loop
+double g_loop_ms = 0;  // wall time of the last solve's outer loop (3D or 2D)
 
 #define RCK(x)                                                         \
   do {                                                                 \
@@ -292,6 +292,7 @@ int refgpu_solve2d(const char* cubin2d, int nv, const float* xyz, int nf, const 
   int iters = 0, total = 0;
   long long nupd = 0;
   htm = O.triMem;
+  const auto t_loop = std::chrono::steady_clock::now();
   while (!act.empty()) {
     if (++total > max_iters) break;
     int na = (int)act.size();
@@ -336,6 +337,7 @@ int refgpu_solve2d(const char* cubin2d, int nv, const float* xyz, int nf, const 
     act.swap(next);
     if (allConv) break;
   }
+  g_loop_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_loop).count();
   for (int v = 0; v < nv; ++v) out_final[v] = first(v);
   if (updates) *updates = nupd;
   return iters;
