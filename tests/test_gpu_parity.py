@@ -209,6 +209,23 @@ def test_3d_bitwise_vs_reference_kernels(need_gpu, eik, O, mg, golden, idx):
         assert bits_equal(e.getResultAtIteration(i), r["history"][i]), (name, i)
 
 
+@pytest.mark.parametrize("cap", [1, 2, 5, 11, 19])
+def test_3d_iteration_cap_vs_reference_kernels(need_gpu, eik, O, mg, cap):
+    """Solves cut off by maxIterations_: the reference's loop runs the neighbour
+    checks of its last iteration before it stops (meshFIM3dEikonal.cu:411-542), which
+    the product runs in one more sweep launch that sweeps nothing; iteration count,
+    vertex-update count and bits equal the reference kernels' at every cap."""
+    need_ref(O)
+    xyz, tets, sp, seed = cube(mg, 17)
+    e = solve3d(eik, xyz, tets, sp, [seed], maxIterations_=cap, maxVertsPerBlock_=32)
+    lab, nb = e.getPartition()
+    M = O.metrics_from_speeds(tets.shape[0], sp)
+    r = O.ref_gpu_solve3d(xyz, tets, M, lab, nb, [seed], max_iters=cap)
+    assert e.numIterations() == r["iterations"] <= cap
+    assert e.stats()["vertex_updates"] == r["vertex_updates"]
+    assert bits_equal(e.getFinalResult(), r["result"])
+
+
 def test_3d_against_reference_kernel_fixtures(need_gpu, eik, ref_outputs):
     """Travel times the reference's kernels produced on the GPU machine
     (tests/golden/ref_gpu_outputs.npz), reproduced through the C ABI."""
