@@ -761,9 +761,10 @@ def main():
         fused = st["check_launches"] == 0 and st["check_visits"] > 0
         fim_bytes += sum(launch_bytes(its, fused)[0])
         iters.append(st["iterations"])
-        # start + 3 kernels (sweep with checks, commit, close) or 4 per iteration, the
-        # graph body running 4 iterations a pass (loop iterations = sweep launches)
-        launches += 1 + (3 if fused else 4) * 4 * ((st["fim_launches"] + 3) // 4)
+        # the state initialisation (k_init_state, k_seed_state), the graph's start node,
+        # then 3 kernels (sweep with checks, commit, close) or 4 per iteration, the graph
+        # body running 4 iterations a pass (loop iterations = sweep launches)
+        launches += 3 + (3 if fused else 4) * 4 * ((st["fim_launches"] + 3) // 4)
     barrier()
     clocks = sampler.stop()
     total_ms, upd_all = aggregate_replicas(torch, sum(times), upd, world, "cuda")
