@@ -408,14 +408,13 @@ __device__ __forceinline__ bool load_block(const DevArgs& a, const BlockDesc& bd
 // which the minimum ignores) to it; the edge candidates are an input plus a square
 // root.  So an apex time T <= RN(m (1 - 2^-20)) < m (1 - 2^-21) keeps its value:
 // min(T, update) = T, and the update can be skipped without changing any bit.
-__device__ __forceinline__ bool upwind_skip(float Tk, float m) { return Tk <= __fmul_rn(m, 0x1.ffffep-1f); }
-
+//
 // The same with a lower bound hs on the distance term of every candidate: each
 // candidate is a convex combination of the three other times (>= m (1 - 2^-22)) plus
 // the rounded square root of a computed metric distance from the apex to a point of
 // the opposite face's plane, which k_plane_bounds shows is >= hs^2; the rounded sum
 // is then > RN(RN(m + hs) (1 - 2^-20)), and an apex at or below that keeps its time.
-// hs = 0 gives upwind_skip.
+// hs = 0 gives the upwind bound above.
 __device__ __forceinline__ bool plane_skip(float Tk, float m, float hs) {
   return Tk <= __fmul_rn(__fadd_rn(m, hs), 0x1.ffffep-1f);
 }
@@ -852,8 +851,9 @@ __global__ void __launch_bounds__(1024) k_visit3d(DevArgs a) {
 //     apex, the slot's copy for a corner owned elsewhere);
 //   * in the last sweep only owned apexes run (the per-slot copies of other
 //     blocks' corners are dropped after the visit);
-//   * an apex already at or below (1 - 2^-20) x the smallest of its three other
-//     corners is skipped (upwind_skip): no candidate of its update can be lower.
+//   * an apex already at or below (1 - 2^-20) x (the smallest of its three other
+//     corners + a lower bound of its distance terms) is skipped (plane_skip): no
+//     candidate of its update can be lower.
 // The four apex updates of a slot round differently (the reference's inlined
 // copies), so the lists are kept per apex and warps run one apex kind at a time.
 // Every update that runs is the reference's, bit for bit (apex_update); skipped
@@ -1305,8 +1305,7 @@ __global__ void __maxnreg__(EIK_ITEM_MAXNREG) k_check3d(DevArgs a) {
   s.hs = reinterpret_cast<uint2*>(sm + off[6]);
   uint4* const smemo = a.chk_memo ? s.memo : nullptr;
   const uint2* const shs = a.hsb ? s.hs : nullptr;
-  const int tid = threadIdx.x, NT = blockDim.x, lane = tid & 31;
-  const int np = a.max_slots_pad;
+  const int tid = threadIdx.x;
   const Ctl* ctl = a.ctl;
   const int iter = ctl->iter;
   const int count = ctl->nnew;
