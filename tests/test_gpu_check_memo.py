@@ -74,3 +74,26 @@ def test_precision_toggle_matches_fresh_handle(need_gpu, eik, mg):
     f.solveEikonal()
     assert f.stats()["flagged_tets"] > 0
     _same(e, f)
+
+
+def test_checks_inside_the_sweep_launch_are_counted(need_gpu, eik, mg):
+    """On the item path the neighbour checks of iteration k run in the sweep launch
+    of iteration k + 1: no check launch, the per-iteration counts add up to the
+    solve's totals, and the vertex-update count is the reference's (owned vertices x
+    2 per sweep visit + owned vertices per check visit)."""
+    xyz, tets, m1, _ = _cube(mg, 21)
+    e = _handle(eik, xyz, tets, m1, [0])
+    e.solveEikonal()
+    st = e.stats()
+    its = e.iterationStats()
+    assert its.shape == (e.numIterations(), len(e.ITERATION_STAT_COLUMNS)) == (e.numIterations(), 16)
+    assert st["check_launches"] == 0 and st["check_kernel_ms"] == 0.0
+    assert st["check_visits"] > 0
+    assert its[:, 2].sum() == st["fim_visits"] and its[:, 6].sum() == st["check_visits"]
+    assert its[:, 5].sum() * 2 + its[:, 9].sum() == st["vertex_updates"]
+    # sweeps of blocks staged by their own check: a subset of each iteration's visits
+    assert (its[:, 12] <= its[:, 2]).all() and its[:, 12].sum() > 0
+    assert (its[:, 13] <= its[:, 3]).all()
+    # launch start offsets on the device timer, in iteration order
+    starts = its[:, 10]
+    assert starts[0] == 0 and (np.diff(starts) > 0).all()
