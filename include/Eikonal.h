@@ -59,6 +59,7 @@ class Eikonal {
     precisionKappa_ = o.precision_kappa;
     deviceSetup_ = o.device_setup;
     partitioner_ = o.partitioner;
+    telemetry_ = o.telemetry;
     if (eik_create(isTriMesh ? 1 : 0, &h_) != EIK_OK) throw std::runtime_error("eik_create failed");
   }
   virtual ~Eikonal() { eik_destroy(h_); }
@@ -186,6 +187,9 @@ class Eikonal {
   // EIK_PARTITION_RCB (default) or EIK_PARTITION_METIS (the reference's partitioner
   // kind; METIS 5 here, METIS 4 in the reference)
   int partitioner_;
+  // 1 (default): per-iteration launch spans and visit counts on the device timer;
+  // 0: none (a slightly faster solve)
+  int telemetry_;
 
  private:
   // the reference's exit codes for the failures it exits on (src/Eikonal.cu:71-88,
@@ -224,6 +228,7 @@ class Eikonal {
     o.precision_kappa = precisionKappa_;
     o.device_setup = deviceSetup_;
     o.partitioner = partitioner_;
+    o.telemetry = telemetry_;
     check(eik_set_options(h_, &o));
   }
   eik_solver* h_ = nullptr;

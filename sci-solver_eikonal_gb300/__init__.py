@@ -40,7 +40,7 @@ class EikOptions(ctypes.Structure):
         ("max_iterations", ctypes.c_int), ("verbose", ctypes.c_int), ("keep_history", ctypes.c_int),
         ("fim_sweeps", ctypes.c_int), ("direct_launch", ctypes.c_int), ("threads_per_block", ctypes.c_int),
         ("precision", ctypes.c_int), ("precision_kappa", ctypes.c_float), ("device_setup", ctypes.c_int),
-        ("partitioner", ctypes.c_int),
+        ("partitioner", ctypes.c_int), ("telemetry", ctypes.c_int),
     ]
 
 
@@ -206,7 +206,7 @@ class Eikonal:
         "verbose_": "verbose", "keepHistory_": "keep_history", "fimSweeps_": "fim_sweeps",
         "directLaunch_": "direct_launch", "threadsPerBlock_": "threads_per_block",
         "precisionMode_": "precision", "precisionKappa_": "precision_kappa", "deviceSetup_": "device_setup",
-        "partitioner_": "partitioner",
+        "partitioner_": "partitioner", "telemetry_": "telemetry",
     }
 
     def __init__(self, isTriMesh, fname="../src/test/test_data/sphere_74verts.ply", verbose=False):

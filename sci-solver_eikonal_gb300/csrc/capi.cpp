@@ -243,6 +243,7 @@ SolveOptions solve_options(const eik_options& o) {
   so.keep_history = o.keep_history != 0;
   so.history_cap = o.max_iterations;
   so.direct_launch = o.direct_launch != 0;
+  so.telemetry = o.telemetry != 0;
   if (o.threads_per_block > 0) so.threads = o.threads_per_block;
   return so;
 }
@@ -389,6 +390,7 @@ void eik_default_options(eik_options* o) {
   o->precision_kappa = 1e4f;
   o->device_setup = DEVICE_SETUP_DEFAULT;
   o->partitioner = EIK_PARTITION_RCB;
+  o->telemetry = 1;
 }
 
 int eik_create(int is_tri_mesh, eik_solver** out) {
@@ -417,6 +419,7 @@ int eik_set_options(eik_solver* h, const eik_options* o) {
   if (o->device_setup != 0 && o->device_setup != 1) return fail(h, EIK_ERR_ARG, "device_setup must be 0 or 1");
   if (o->partitioner != EIK_PARTITION_RCB && o->partitioner != EIK_PARTITION_METIS)
     return fail(h, EIK_ERR_ARG, "partitioner must be EIK_PARTITION_RCB or EIK_PARTITION_METIS");
+  if (o->telemetry != 0 && o->telemetry != 1) return fail(h, EIK_ERR_ARG, "telemetry must be 0 or 1");
   if (o->partitioner == EIK_PARTITION_METIS && !metis_available())
     return fail(h, EIK_ERR_ARG, "this build has no METIS (libmetis_static.a was not found at build time)");
   h->opt = *o;

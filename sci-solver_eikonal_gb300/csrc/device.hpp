@@ -60,6 +60,7 @@ struct SolveOptions {
   int history_cap = 0;       // snapshots kept when keep_history
   int threads = 0;           // CTA size of the 3D visit kernels (0: from the largest block)
   bool direct_launch = false; // launch the loop body kernel by kernel (for profilers)
+  bool telemetry = true;      // per-launch spans and visit counts on the device timer
   std::vector<int> inst_max_iterations;  // per instance; empty: max_iterations for all
 };
 

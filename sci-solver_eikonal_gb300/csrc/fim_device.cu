@@ -236,6 +236,10 @@ constexpr int kKStride = 16;    // words of per-iteration telemetry (DevArgs::kt
 #ifndef EIK_SIZED_AUX
 #define EIK_SIZED_AUX 1
 #endif
+#ifndef EIK_TELEMETRY
+#define EIK_TELEMETRY 1
+#endif
+
 // 3D item kernels: the neighbour checks of an iteration run inside the next
 // iteration's sweep launch (1) or as their own launch, k_check3d (0)
 #ifndef EIK_FUSED_CHECK
@@ -284,9 +288,12 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // flag the host reads instead of a kernel that never ends.
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-  const unsigned long long t0 = global_ns();
+  // the clock is read only once the wait has spun a while: most waits end at once,
+  // and a timer read per visit cost the 65^3 solve 1.1%
+  unsigned long long t0 = 0;
   for (int i = 0; i < (1 << 26); ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (i == 16) t0 = global_ns();
     if (i > 16) {
       __nanosleep(256);
       if ((i & 63) == 0 && global_ns() - t0 > kWaitLimitNs) return false;
@@ -300,16 +307,16 @@ __device__ __forceinline__ void fence_proxy_async() {
 
 // launch span of a visit kernel: earliest CTA start, latest CTA end
 __device__ __forceinline__ void stamp_start(const DevArgs& a, int iter, int which) {
-  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap)
+  if (EIK_TELEMETRY && threadIdx.x == 0 && a.ktime && iter < a.ktime_cap)
     atomicMax(&a.ktime[kKStride * iter + 2 * which], ~global_ns());
 }
 __device__ __forceinline__ void stamp_end(const DevArgs& a, int iter, int which) {
-  if (threadIdx.x == 0 && a.ktime && iter < a.ktime_cap)
+  if (EIK_TELEMETRY && threadIdx.x == 0 && a.ktime && iter < a.ktime_cap)
     atomicMax(&a.ktime[kKStride * iter + 2 * which + 1], global_ns());
 }
 // one visit's inputs into this iteration's telemetry (caller: one thread)
 __device__ __forceinline__ void count_visit(const DevArgs& a, int iter, int which, int slots, int halo, int owned) {
-  if (a.ktime && iter < a.ktime_cap) {
+  if (EIK_TELEMETRY && a.ktime && iter < a.ktime_cap) {
     unsigned long long* w = a.ktime + kKStride * iter + 4 + 4 * which;
     atomicAdd(w, 1ull);
     atomicAdd(w + 1, (unsigned long long)slots);
@@ -2465,6 +2472,8 @@ struct DeviceSolve::Impl {
   bool g_hist = false;
   int g_histcap = -1;
   int g_serve = -1;
+  bool g_tele = true;    // the graph's kernels record per-launch telemetry
+  bool want_tele = true;  // what the next graph build records
   int device = 0;  // the device current when the object was created
   // serving: host flag (mapped pinned memory) that ends the device loop early
   int* pending_host = nullptr;
@@ -2561,7 +2570,8 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     a.vblock = P.vblock; a.nb = L.nb; a.nv = L.nv; a.Ta = P.Ta; a.Tb = P.Tb; a.Tinit = P.Tinit; a.prev = P.prev;
     a.conv = P.conv; a.stampA = P.stampA; a.stampC = P.stampC; a.visited = P.visited; a.list0 = P.list0;
     a.list1 = P.list1; a.list_new = P.list_new; a.ctl = P.ctl; a.hist = P.hist; a.hist_cap = hcap;
-    a.ktime = P.ktime; a.ktime_cap = P.ktime_cap;
+    a.ktime = P.want_tele ? P.ktime : nullptr;
+    a.ktime_cap = P.want_tele ? P.ktime_cap : 0;
     a.fim_sweeps = sweeps; a.max_slots_pad = P.max_slots_pad; a.max_local = P.max_local;
     a.max_owned = P.max_owned;
     a.use_cond = 1;
@@ -2777,6 +2787,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
     P.g_threads = threads;
     P.g_hist = want_hist;
     P.g_histcap = hcap;
+    P.g_tele = P.want_tele;
     P.g_serve = serve ? 1 : 0;
   }
   return "";
@@ -3183,7 +3194,8 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
     CK(cudaMalloc((void**)&P.ktime, sizeof(unsigned long long) * kKStride * (size_t)P.ktime_cap));
     P.drop_graph();
   }
-  CK(cudaMemsetAsync(P.ktime, 0, sizeof(unsigned long long) * kKStride * (size_t)P.ktime_cap, st));
+  if (opt.telemetry || tune_slot >= 0)
+    CK(cudaMemsetAsync(P.ktime, 0, sizeof(unsigned long long) * kKStride * (size_t)P.ktime_cap, st));
   // initial state
   // initial state built on the device: only the seed ids, the starting blocks and
   // (when given) the caller's initial values cross from the host
@@ -3242,10 +3254,12 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   c.nact = (int)P.h_act.size();
   CK(cudaMemcpyAsync(P.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, st));
 
-  // (re)build the graph when the launch shape changes
+  // (re)build the graph when the launch shape changes; the CTA-size tuning of the
+  // slot kernels measures with the telemetry whatever the option says
   const bool want_hist = hcap > 0;
+  P.want_tele = opt.telemetry || tune_slot >= 0;
   if (!P.exec || P.g_sweeps != sweeps || P.g_threads != threads || P.g_hist != want_hist || P.g_histcap != hcap ||
-      P.g_serve != 0) {
+      P.g_serve != 0 || P.g_tele != P.want_tele) {
     std::string e = P.build_graph(L, sweeps, threads, hcap, false);
     if (!e.empty()) return e;
   }
@@ -3329,7 +3343,10 @@ std::string DeviceSolve::solve(const SolveOptions& opt) {
   stats_.fim_halo = (long long)out.fim_halo;
   stats_.fim_owned = (long long)out.fim_owned;
   const bool measured = tune_slot >= 0 && stats_.error == 0 && stats_.fim_slots > 0;
-  {
+  stats_.fim_kernel_ms = stats_.check_kernel_ms = 0.0f;
+  stats_.fim_launches = stats_.check_launches = 0;
+  stats_.iter_stats.clear();
+  if (P.g_tele) {
     std::vector<unsigned long long> kt(kKStride * (size_t)P.ktime_cap);
     CK(cudaMemcpy(kt.data(), P.ktime, sizeof(unsigned long long) * kt.size(), cudaMemcpyDeviceToHost));
     double fim = 0, chk = 0;

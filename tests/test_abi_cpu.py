@@ -37,6 +37,18 @@ def test_default_options_are_the_references(eik):
     assert (o.square_length, o.square_width, o.square_depth) == (16, 16, 16)
     assert (o.square_block_length, o.square_block_width, o.square_block_depth) == (1, 1, 1)
     assert o.max_iterations == 100
+    # options of this build beside the reference's: telemetry on, checked values
+    assert o.telemetry == 1
+    e = eik.Eikonal(False)
+    o2 = eik.EikOptions()
+    e._check(e._lib.eik_get_options(e._h, ctypes.byref(o2)))
+    o2.telemetry = 0
+    e._check(e._lib.eik_set_options(e._h, ctypes.byref(o2)))
+    o3 = eik.EikOptions()
+    e._check(e._lib.eik_get_options(e._h, ctypes.byref(o3)))
+    assert o3.telemetry == 0
+    o2.telemetry = 2
+    assert e._lib.eik_set_options(e._h, ctypes.byref(o2)) == 1  # EIK_ERR_ARG
 
 
 def test_error_codes(eik, mg, tmp_path):

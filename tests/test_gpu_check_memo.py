@@ -97,3 +97,27 @@ def test_checks_inside_the_sweep_launch_are_counted(need_gpu, eik, mg):
     # launch start offsets on the device timer, in iteration order
     starts = its[:, 10]
     assert starts[0] == 0 and (np.diff(starts) > 0).all()
+
+
+def test_telemetry_off_keeps_results(need_gpu, eik, mg):
+    """Without telemetry the solve records no launch spans or per-iteration rows and
+    gives the same bits, iterations and vertex updates."""
+    xyz, tets, m1, _ = _cube(mg, 17)
+    out = []
+    for tele in (1, 0):
+        e = _handle(eik, xyz, tets, m1, [0])
+        e.telemetry_ = tele
+        e.solveEikonal()
+        out.append(e)
+    on, off = out
+    assert bits_equal(on.getFinalResult(), off.getFinalResult())
+    assert on.numIterations() == off.numIterations()
+    assert on.stats()["vertex_updates"] == off.stats()["vertex_updates"]
+    assert on.stats()["fim_kernel_ms"] > 0 and on.iterationStats().shape[0] == on.numIterations()
+    assert off.stats()["fim_kernel_ms"] == 0 and off.stats()["fim_launches"] == 0
+    assert off.iterationStats().shape[0] == 0
+    # switching back on rebuilds the loop with telemetry
+    off.telemetry_ = 1
+    off.solveEikonal()
+    assert off.iterationStats().shape[0] == off.numIterations()
+    assert bits_equal(on.getFinalResult(), off.getFinalResult())
