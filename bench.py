@@ -841,8 +841,8 @@ def main():
                              "solver, not by HBM",
                      # compute side, from the committed full capture of one sweep launch (outer
                      # iteration 40 of the same solve, kernel-by-kernel mode)
-                     "compute": {"bound": "issue", "issue_active_pct": 51.3, "ipc_per_sm": 2.01,
-                                 "fma_pipe_pct": 15.4, "alu_pipe_pct": 31.0, "xu_pipe_pct": 6.9,
+                     "compute": {"bound": "issue", "issue_active_pct": 50.5, "ipc_per_sm": 2.05,
+                                 "fma_pipe_pct": 16.0, "alu_pipe_pct": 30.9, "xu_pipe_pct": 7.3,
                                  "top_stall": "barrier",
                                  "source": "profiles/fim3d_items_c3d.md (ncu --set full, one k_sweep3d launch)"}},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
