@@ -2691,6 +2691,9 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
 #else
     const int grid_blocks = P.grid_aux, grid_chunks = P.grid_aux;
 #endif
+    // the one-CTA close: a thread per instance, one warp at least (its barriers are
+    // then a single warp's for a plain solve)
+    const int close_threads = std::min(256, std::max(32, (P.ninst + 31) & ~31));
     // start node
     void* args_ptr[] = {&P.args};
     cudaGraphNode_t n_start, n_while;
@@ -2767,7 +2770,7 @@ std::string DeviceSolve::Impl::build_graph(const Layout& L, int sweeps, int thre
       if (L.dim == 3) {
         if (!(e = add((void*)k_commit3d, grid_blocks, 256, 0, args_ptr)).empty()) return e;
         if (!a.fused && !(e = add(kv_chk, grid_chk, cthreads, vsmem_chk, args_ptr)).empty()) return e;
-        if (!(e = add((void*)k_close3d, 1, 256, 0, close_args)).empty()) return e;
+        if (!(e = add((void*)k_close3d, 1, close_threads, 0, close_args)).empty()) return e;
       } else {
         if (!(e = add((void*)k_activate2d, grid_blocks, 256, 0, args_ptr)).empty()) return e;
         if (!(e = add(kv_chk, P.grid_visit, vthreads, vsmem, args_ptr)).empty()) return e;
