@@ -564,3 +564,23 @@ def test_metis_partition_solves_bitwise_like_the_reference_kernels(need_gpu, eik
         e.solveEikonal()
         r = _tri_ref(eik, O, e, xyz, None, [0])
         assert bits_equal(e.getFinalResult(), r["result"]) and r["iterations"] == e.numIterations()
+
+
+def test_serving_pool_97_bitwise_vs_reference_kernels(need_gpu, eik, O, mg):
+    """The serving pool's largest mesh (97^3 jittered Kuhn cube, 912,673 vertices,
+    5,308,416 tets, its pool speeds) with a request's 16 seeds and speed scale, solved
+    on its own: bits, iterations and vertex updates equal the reference kernels'
+    (served results equal this solve, test_gpu_serve.py)."""
+    need_ref(O)
+    xyz, tets = mg.kuhn_cube(97, 0.2, seed=23)
+    v = mg.log_uniform_speeds(tets.shape[0], 0.5, 2.0, seed=33)
+    scale = np.float32(1.37)
+    metric = ((1.0 / (v.astype(np.float64) ** 2)).astype(np.float32) * np.float32(1.0 / (scale * scale))).astype(
+        np.float32)
+    seeds = np.random.default_rng(97).choice(xyz.shape[0], 16, replace=False).tolist()
+    e = solve3d(eik, xyz, tets, metric, seeds, maxVertsPerBlock_=64, maxIterations_=1000, keepHistory_=0)
+    lab, nb = e.getPartition()
+    r = O.ref_gpu_solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], metric), lab, nb, seeds, max_iters=1000)
+    assert e.numIterations() == r["iterations"] < 1000
+    assert e.stats()["vertex_updates"] == r["vertex_updates"]
+    assert bits_equal(e.getFinalResult(), r["result"])
