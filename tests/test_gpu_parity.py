@@ -584,3 +584,20 @@ def test_serving_pool_97_bitwise_vs_reference_kernels(need_gpu, eik, O, mg):
     assert e.numIterations() == r["iterations"] < 1000
     assert e.stats()["vertex_updates"] == r["vertex_updates"]
     assert bits_equal(e.getFinalResult(), r["result"])
+
+
+def test_precision_workload_fp32_bitwise_vs_reference_kernels(need_gpu, eik, O, mg):
+    """The precision workload at full size (49^3 jittered cube with 10% sliver tets,
+    anisotropic metrics, 4 seeds) in the FP32 mode: bits, iterations and vertex
+    updates equal the reference kernels' (the mixed mode departs from them on
+    purpose and is held to the FP64 run instead, test_gpu_precision.py)."""
+    need_ref(O)
+    xyz, tets, _ = mg.sliver_cube(49, 0.10, seed=5)
+    M6 = mg.anisotropic_metrics(tets.shape[0], seed=6).ravel()
+    seeds = np.random.Generator(np.random.PCG64(9)).choice(xyz.shape[0], 4, replace=False).tolist()
+    e = solve3d(eik, xyz, tets, M6, seeds, maxIterations_=1000, keepHistory_=0)
+    lab, nb = e.getPartition()
+    r = O.ref_gpu_solve3d(xyz, tets, O.metrics_from_speeds(tets.shape[0], M6), lab, nb, seeds, max_iters=1000)
+    assert e.numIterations() == r["iterations"] < 1000
+    assert e.stats()["vertex_updates"] == r["vertex_updates"]
+    assert bits_equal(e.getFinalResult(), r["result"])
