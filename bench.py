@@ -781,7 +781,8 @@ def main():
 
     # end to end through the C ABI with host buffers
     nv = xyz.shape[0]
-    out = np.empty(nv, dtype=np.float32)
+    # the travel times come back into pinned host memory (a direct copy, no staging)
+    out = torch.empty(nv, dtype=torch.float32, pin_memory=True).numpy()
     seeds = np.array([seed], dtype=np.int32)
     e2e_times = []
     for i in range(args.warmup + args.steps):
@@ -789,7 +790,7 @@ def main():
         t = time.perf_counter()
         e.setSeeds(seeds)
         e.solveEikonal()
-        out[:] = e.getFinalResult()
+        e.getFinalResult(out=out)
         dt = time.perf_counter() - t
         if i >= args.warmup:
             e2e_times.append(dt)
@@ -848,7 +849,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times),
                 "note": "each step re-solves the resident mesh through the C ABI: seeds copied in, the solve, the "
-                        "travel times copied out; the partition and block layout built by the first solve "
+                        "travel times copied out into pinned host memory; the partition and block layout built by the first solve "
                         "(first_solve_s) are kept, whereas the reference's solveEikonal rebuilds them on every "
                         "call"},
         "clocks": clocks,

@@ -308,8 +308,14 @@ class Eikonal:
     def numIterations(self):
         return self._lib.eik_num_iterations(self._h)
 
-    def getFinalResult(self):
-        out = np.empty(self.numVertices(), dtype=np.float32)
+    def getFinalResult(self, out=None):
+        """Travel times in original vertex order; `out` (optional): a contiguous
+        float32 array of numVertices() entries to fill, e.g. in pinned host memory
+        (the copy then runs without staging)."""
+        if out is None:
+            out = np.empty(self.numVertices(), dtype=np.float32)
+        elif out.dtype != np.float32 or out.size != self.numVertices() or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float32 array of numVertices() entries")
         self._check(self._lib.eik_get_result(self._h, _fptr(out), out.size))
         return out
 
