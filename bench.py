@@ -845,7 +845,8 @@ def main():
                      "compute": {"bound": "issue", "issue_active_pct": 50.5, "ipc_per_sm": 2.05,
                                  "fma_pipe_pct": 16.0, "alu_pipe_pct": 30.9, "xu_pipe_pct": 7.3,
                                  "top_stall": "barrier",
-                                 "source": "profiles/fim3d_items_c3d.md (ncu --set full, one k_sweep3d launch)"}},
+                                 "source": "ncu --set full capture of one k_sweep3d launch (outer iteration 40) "
+                                           "of this workload, summarised under profiles/"}},
         "e2e": {"value": e2e_value, "unit": "vertex-updates/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.median(e2e_times),
                 "note": "each step re-solves the resident mesh through the C ABI: seeds copied in, the solve, the "
