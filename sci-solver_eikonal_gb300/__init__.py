@@ -469,10 +469,16 @@ class EikonalBatch:
         self._check(self._lib.eik_batch_get_result(self._h, int(i), _fptr(out), out.size))
         return out
 
-    def getFinalResults(self):
-        """All instances' results, split per instance."""
+    def getFinalResults(self, out=None):
+        """All instances' results, split per instance; `out` (optional): a contiguous
+        float32 array of the instances' total vertex count to fill (e.g. pinned host
+        memory)."""
         sizes = [self._lib.eik_batch_num_vertices(self._h, i) for i in range(len(self))]
-        out = np.empty(int(sum(sizes)), dtype=np.float32)
+        total = int(sum(sizes))
+        if out is None:
+            out = np.empty(total, dtype=np.float32)
+        elif out.dtype != np.float32 or out.size != total or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float32 array of the batch's total vertex count")
         self._check(self._lib.eik_batch_get_results(self._h, _fptr(out), out.size))
         return np.split(out, np.cumsum(sizes)[:-1])
 
