@@ -122,3 +122,33 @@ def test_2d_blocks_above_1024_slots_use_the_slot_loop_kernel(need_gpu, eik, mg, 
     # reference does, so blocks this large can stop with vertices unreached; the
     # restatement does the same)
     assert np.max(relerr(got, want)) <= 1e-4
+
+
+def test_results_into_caller_buffers(need_gpu, eik, mg):
+    """getFinalResult / EikonalBatch.getFinalResults fill a caller's (pinned) buffer
+    with the same bits, and reject a buffer of the wrong type or size."""
+    import torch
+    xyz, tets = mg.kuhn_cube(9, 0.2, seed=1)
+    e = eik.Eikonal(False)
+    e.set_mesh(xyz, tets)
+    e.setSeeds([0])
+    e.solveEikonal()
+    buf = torch.empty(xyz.shape[0], dtype=torch.float32, pin_memory=True).numpy()
+    got = e.getFinalResult(out=buf)
+    assert got is buf and np.array_equal(buf.view(np.uint32), e.getFinalResult().view(np.uint32))
+    with pytest.raises(ValueError):
+        e.getFinalResult(out=np.empty(xyz.shape[0], np.float64))
+    with pytest.raises(ValueError):
+        e.getFinalResult(out=np.empty(xyz.shape[0] + 1, np.float32))
+    e2 = eik.Eikonal(False)
+    e2.set_mesh(xyz, tets)
+    e2.setSeeds([5])
+    b = eik.EikonalBatch([e, e2])
+    b.solveEikonal()
+    total = 2 * xyz.shape[0]
+    bbuf = torch.empty(total, dtype=torch.float32, pin_memory=True).numpy()
+    parts = b.getFinalResults(out=bbuf)
+    ref = b.getFinalResults()
+    assert all(np.array_equal(p.view(np.uint32), r.view(np.uint32)) for p, r in zip(parts, ref))
+    with pytest.raises(ValueError):
+        b.getFinalResults(out=np.empty(total - 1, np.float32))
